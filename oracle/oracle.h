@@ -1,0 +1,98 @@
+/*
+ * ORACLE -- test infrastructure only.
+ *
+ * CPU (FP64, OpenMP) restatement of the reference's exchange-correlation grid
+ * path (Serenity 1.6.2).  It exists to check the GPU product against, and to be
+ * timed as the CPU baseline.  Nothing in the product links, loads or calls it;
+ * only tests/, the smoke check and bench.py's CPU-baseline leg do.
+ *
+ * Parity status: pinned against the reference's own golden vectors (basis
+ * values/gradients/Hessians, rho/grad rho, adder matrix, H2 LDA Fock matrices)
+ * in tests/golden/.  PBE, B88 and LYP have no absolute golden value at this
+ * boundary in the reference (its libxc test only compares two libraries):
+ * for those functionals parity is unpinned and rests on literature formulas,
+ * limiting cases and finite-difference checks.
+ *
+ * Conventions (all follow the reference):
+ *   points  : xyz interleaved (x0,y0,z0,x1,...), bohr
+ *   matrices: n_bf x n_bf, column-major (symmetric inputs)
+ *   blocks  : consecutive runs of max_block_size points
+ *     (BasisFunctionOnGridController.cpp:75-148)
+ */
+#ifndef SERENITY_XC_ORACLE_H
+#define SERENITY_XC_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* functional identifiers (shared numbering with the product's C ABI) */
+enum {
+  ORC_FUNC_LDA = 1,  /* Slater + VWN5          (CompositeFunctionals.cpp:233-235) */
+  ORC_FUNC_PBE = 2,  /* PBE x + PBE c          (CompositeFunctionals.cpp:242-244) */
+  ORC_FUNC_BLYP = 3, /* B88 + LYP              (CompositeFunctionals.cpp:239-241) */
+  ORC_FUNC_SLATER = 16,
+  ORC_FUNC_VWN5 = 17,
+  ORC_FUNC_PBEX = 18,
+  ORC_FUNC_PBEC = 19,
+  ORC_FUNC_B88 = 20,
+  ORC_FUNC_LYP = 21,
+  ORC_FUNC_PW92 = 22
+};
+
+/* Basis: shells with raw (file) contraction coefficients; the oracle applies the
+ * libint2 normalisation convention itself (Shell.cpp:30-47). */
+void* orc_basis_create(int nshell, const int* l, const int* pure, const int* nprim, const double* centers,
+                       const double* alpha, const double* coef);
+void orc_basis_free(void* basis);
+int orc_basis_nbf(const void* basis);
+/* normalised primitive coefficients of shell s into out (nprim values) */
+void orc_basis_shell_coefs(const void* basis, int s, double* out);
+
+/* One block of points: values/gradients/Hessians (deriv 0,1,2) for all functions,
+ * column-major npts x nbf each; negligible[nbf] (1 = skipped for this block). */
+int orc_block_on_grid(const void* basis, const double* xyz, int npts, double radial_threshold, int deriv,
+                      double* values, double* grad /*3*npts*nbf or NULL*/, double* hess /*6*npts*nbf or NULL*/,
+                      int* negligible);
+
+/* rho (and grad rho) of nspin density matrices, block-wise with screening. */
+int orc_density(const void* basis, const double* xyz, long npts, int max_block, double radial_threshold, int nspin,
+                const double* P, double* rho /*nspin*npts*/, double* grad /*nspin*3*npts or NULL*/);
+
+/* Functional evaluation at points (GRADIENTS data type, order 1).
+ * rho: nspin*npts, grad: nspin*3*npts (GGA), outputs epuv[npts], dfdrho[nspin*npts],
+ * dfdgrad[nspin*3*npts] (GGA).  Blocks with sum|rho| < n*1e-12 are skipped as in
+ * XCFun.cpp:136-140 when max_block > 0. */
+int orc_functional(int func, int nspin, long npts, int max_block, const double* rho, const double* grad,
+                   double* epuv, double* dfdrho, double* dfdgrad);
+/* is the functional a GGA (needs gradients)? */
+int orc_functional_is_gga(int func);
+
+/* F += sum_p w v phi phi (+ GGA term), ScalarOperatorToMatrixAdder.cpp:178-303. */
+int orc_add_scalar(const void* basis, const double* xyz, const double* w, long npts, int max_block,
+                   double radial_threshold, double block_ave_threshold, int nspin, const double* v,
+                   const double* g /*nspin*3*npts or NULL*/, double* F /*nspin*nbf*nbf, added into*/);
+
+/* Whole XC build (FuncPotential.cpp:74-110 with FunctionalLibrary(128)).
+ * V (nspin*nbf*nbf) is overwritten; Exc = sum w*epuv; Nel = sum w*rho_total.
+ * threads <= 0 uses every core. */
+int orc_vxc(const void* basis, const double* xyz, const double* w, long npts, int max_block, double radial_threshold,
+            double block_ave_threshold, int func, int nspin, const double* P, double* V, double* Exc, double* Nel,
+            int threads);
+
+/* Atom-centred Becke grid (GridFactory.cpp:52-320, AtomGridFactory.cpp:78-290).
+ * Z[natoms], xyz[3*natoms] (bohr).  If accuracy > 0 the reference's pruned
+ * accuracy scheme is used, else n_rad x n_ang (unpruned).  lebedev_path points to
+ * the node table.  Returns the number of points written (<= capacity), or -1. */
+long orc_becke_grid(int natoms, const int* Z, const double* xyz, int n_rad, int n_ang, int accuracy,
+                    double weight_threshold, int smoothing, int sort, const char* lebedev_path, double* out_xyz,
+                    double* out_w, long capacity);
+
+/* Ahlrichs M3 radial rule (AtomGridFactory.cpp:238-260). */
+void orc_ahlrichs_radial(double alpha, int n, double* r, double* w);
+/* Real solid harmonic values at a point, m = -l..l (the reference's order). */
+void orc_solid_harmonics(int l, double x, double y, double z, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,175 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes binding of ``oracle/_build/liboracle.so`` (the CPU FP64 restatement of the
+reference's XC grid path, see ``oracle/oracle.h``).  Only ``tests/``, the smoke
+check and ``bench.py``'s CPU-baseline leg import this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+FUNC = {"LDA": 1, "PBE": 2, "BLYP": 3, "SLATER": 16, "VWN5": 17, "PBEX": 18, "PBEC": 19, "B88": 20, "LYP": 21,
+        "PW92": 22}
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_basis_create.restype = ctypes.c_void_p
+        L.orc_basis_create.argtypes = [ctypes.c_int, _ip, _ip, _ip, _dp, _dp, _dp]
+        L.orc_basis_free.argtypes = [ctypes.c_void_p]
+        L.orc_basis_nbf.argtypes = [ctypes.c_void_p]
+        L.orc_basis_shell_coefs.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
+        L.orc_block_on_grid.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp,
+                                        ctypes.c_void_p, ctypes.c_void_p, _ip]
+        L.orc_density.argtypes = [ctypes.c_void_p, _dp, ctypes.c_long, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                  _dp, _dp, ctypes.c_void_p]
+        L.orc_functional.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, ctypes.c_int, _dp, ctypes.c_void_p,
+                                     _dp, _dp, ctypes.c_void_p]
+        L.orc_functional_is_gga.argtypes = [ctypes.c_int]
+        L.orc_add_scalar.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_long, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_int, _dp, ctypes.c_void_p, _dp]
+        L.orc_vxc.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_long, ctypes.c_int, ctypes.c_double,
+                              ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        L.orc_becke_grid.restype = ctypes.c_long
+        L.orc_becke_grid.argtypes = [ctypes.c_int, _ip, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, _dp, _dp,
+                                     ctypes.c_long]
+        L.orc_ahlrichs_radial.argtypes = [ctypes.c_double, ctypes.c_int, _dp, _dp]
+        L.orc_solid_harmonics.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Basis:
+    def __init__(self, shells):
+        L = lib()
+        self.shells = shells
+        self.h = L.orc_basis_create(shells.nshell, shells.l, shells.pure, shells.nprim, shells.centers, shells.alpha,
+                                    shells.coef)
+        self.nbf = L.orc_basis_nbf(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_basis_free(self.h)
+            self.h = None
+
+    def shell_coefs(self, s):
+        out = np.zeros(int(self.shells.nprim[s]))
+        lib().orc_basis_shell_coefs(self.h, s, out)
+        return out
+
+    def block(self, xyz, thr, deriv=1):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = xyz.shape[0]
+        v = np.zeros(n * self.nbf)
+        g = np.zeros(3 * n * self.nbf) if deriv >= 1 else None
+        h = np.zeros(6 * n * self.nbf) if deriv >= 2 else None
+        neg = np.zeros(self.nbf, dtype=np.int32)
+        lib().orc_block_on_grid(self.h, xyz.reshape(-1), n, thr, deriv, v, _ptr(g), _ptr(h), neg)
+        out = {"values": v.reshape(self.nbf, n).T, "negligible": neg}
+        if deriv >= 1:
+            out["grad"] = g.reshape(3, self.nbf, n).transpose(0, 2, 1)
+        if deriv >= 2:
+            out["hess"] = h.reshape(6, self.nbf, n).transpose(0, 2, 1)
+        return out
+
+    def density(self, xyz, P, max_block=128, thr=1e-9, grad=True):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        n = xyz.size // 3
+        P = np.asarray(P, dtype=np.float64)
+        nspin = 1 if P.ndim == 2 else P.shape[0]
+        Pc = np.ascontiguousarray(np.stack([m.T for m in P.reshape(nspin, self.nbf, self.nbf)]).reshape(-1))
+        rho = np.zeros(nspin * n)
+        g = np.zeros(nspin * 3 * n) if grad else None
+        lib().orc_density(self.h, xyz, n, max_block, thr, nspin, Pc, rho, _ptr(g))
+        return rho.reshape(nspin, n), (g.reshape(nspin, 3, n) if grad else None)
+
+    def add_scalar(self, xyz, w, v, g=None, max_block=128, thr=1e-9, ave_thr=1e-11):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        n = xyz.size // 3
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        nspin = v.size // n
+        gg = None if g is None else np.ascontiguousarray(g, dtype=np.float64).reshape(-1)
+        F = np.zeros(nspin * self.nbf * self.nbf)
+        lib().orc_add_scalar(self.h, xyz, np.ascontiguousarray(w, dtype=np.float64), n, max_block, thr, ave_thr,
+                             nspin, v, _ptr(gg), F)
+        F = F.reshape(nspin, self.nbf, self.nbf).transpose(0, 2, 1)
+        return F
+
+    def vxc(self, xyz, w, func, P, max_block=128, thr=1e-9, ave_thr=1e-11, threads=0):
+        """Whole build: returns (V [nspin,nbf,nbf], Exc, Nel)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        n = xyz.size // 3
+        P = np.asarray(P, dtype=np.float64)
+        nspin = 1 if P.ndim == 2 else P.shape[0]
+        Pc = np.ascontiguousarray(np.stack([m.T for m in P.reshape(nspin, self.nbf, self.nbf)]).reshape(-1))
+        V = np.zeros(nspin * self.nbf * self.nbf)
+        exc, nel = ctypes.c_double(), ctypes.c_double()
+        fid = FUNC[func] if isinstance(func, str) else int(func)
+        lib().orc_vxc(self.h, xyz, np.ascontiguousarray(w, dtype=np.float64), n, max_block, thr, ave_thr, fid, nspin,
+                      Pc, V, ctypes.byref(exc), ctypes.byref(nel), threads)
+        return V.reshape(nspin, self.nbf, self.nbf).transpose(0, 2, 1), exc.value, nel.value
+
+
+def functional(func, rho, grad=None, max_block=0):
+    """rho [nspin, n], grad [nspin, 3, n] -> (epuv [n], dfdrho [nspin, n], dfdgrad [nspin, 3, n])."""
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    nspin, n = rho.shape
+    fid = FUNC[func] if isinstance(func, str) else int(func)
+    gga = bool(lib().orc_functional_is_gga(fid))
+    g = None if grad is None else np.ascontiguousarray(grad, dtype=np.float64).reshape(-1)
+    epuv = np.zeros(n)
+    dr = np.zeros(nspin * n)
+    dg = np.zeros(nspin * 3 * n) if gga else None
+    lib().orc_functional(fid, nspin, n, max_block, rho.reshape(-1), _ptr(g), epuv, dr, _ptr(dg))
+    return epuv, dr.reshape(nspin, n), (dg.reshape(nspin, 3, n) if gga else None)
+
+
+def becke_grid(Z, xyz_bohr, n_rad=0, n_ang=0, accuracy=0, weight_threshold=1e-14, smoothing=3, sort=True,
+               lebedev_path=None):
+    from serenity_gb300.basis import LEBEDEV_TABLE
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1)
+    cap = len(Z) * (max(n_rad, 100) * max(n_ang, 770) + 1)
+    out_x = np.zeros(3 * cap)
+    out_w = np.zeros(cap)
+    path = (lebedev_path or LEBEDEV_TABLE).encode()
+    n = lib().orc_becke_grid(len(Z), Z, xyz, n_rad, n_ang, accuracy, weight_threshold, smoothing, int(sort), path,
+                             out_x, out_w, cap)
+    if n < 0:
+        raise RuntimeError("grid capacity exceeded")
+    return out_x[:3 * n].reshape(n, 3).copy(), out_w[:n].copy()
+
+
+def ahlrichs_radial(alpha, n):
+    r, w = np.zeros(n), np.zeros(n)
+    lib().orc_ahlrichs_radial(alpha, n, r, w)
+    return r, w
+
+
+def solid_harmonics(l, x, y, z):
+    out = np.zeros(2 * l + 1)
+    lib().orc_solid_harmonics(l, x, y, z, out)
+    return out

@@ -1,0 +1,310 @@
+/*
+ * ORACLE -- test infrastructure only (see oracle.h).
+ *
+ * Density on the grid, functional evaluation over blocks, the scalar-operator
+ * adder and the whole XC build, restated from the reference:
+ *   MatrixOperatorToGridTransformer.cpp:37-198   (rho = rowsum((phi P_b) o phi),
+ *                                                 grad rho = 2 rowsum((phi P_b) o grad phi))
+ *   XCFun.cpp:39-158, 751-765                    (block skip, GRADIENTS outputs, E_xc)
+ *   ScalarOperatorToMatrixAdder.cpp:51-113,178-303 (per-thread matrices, block
+ *                                                 thresholds, F_b = tmp + tmp^T)
+ *   FuncPotential.cpp:74-110                     (the wiring: FunctionalLibrary(128),
+ *                                                 LDA -> scalar adder, GGA -> gradient adder)
+ * The three phases run one after the other over all blocks, with the basis
+ * evaluated again in the adder phase, as the reference does.
+ */
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "oracle_internal.h"
+
+namespace orc {
+
+// Basis data of one block restricted to its non-negligible functions:
+// phi[f*npts + p], grad[(3*f + k)*npts + p]; idx[f] = global function index.
+struct ActiveBlock {
+  int npts = 0, nact = 0;
+  std::vector<int> idx;
+  std::vector<double> phi, grad;
+};
+
+static void eval_active(const Basis& B, const double* xyz, int npts, double thr, int deriv, ActiveBlock& out,
+                        std::vector<double>& full_v, std::vector<double>& full_g, std::vector<int>& negl) {
+  const int nbf = B.nbf;
+  full_v.resize((size_t)npts * nbf);
+  if (deriv >= 1) full_g.resize((size_t)3 * npts * nbf);
+  negl.resize(nbf);
+  block_on_grid(B, xyz, npts, thr, deriv, full_v.data(), deriv >= 1 ? full_g.data() : nullptr, nullptr, negl.data());
+  out.npts = npts;
+  out.idx.clear();
+  for (int i = 0; i < nbf; ++i)
+    if (!negl[i]) out.idx.push_back(i);
+  out.nact = (int)out.idx.size();
+  out.phi.resize((size_t)out.nact * npts);
+  if (deriv >= 1) out.grad.resize((size_t)3 * out.nact * npts);
+  for (int f = 0; f < out.nact; ++f) {
+    const int mu = out.idx[f];
+    std::memcpy(&out.phi[(size_t)f * npts], &full_v[(size_t)mu * npts], sizeof(double) * npts);
+    if (deriv >= 1)
+      for (int k = 0; k < 3; ++k)
+        std::memcpy(&out.grad[((size_t)3 * f + k) * npts], &full_g[(size_t)k * npts * nbf + (size_t)mu * npts],
+                    sizeof(double) * npts);
+  }
+}
+
+static void density_block(const ActiveBlock& A, int nbf, const double* P, double* rho, double* grad, long gstride) {
+  const int n = A.npts, m = A.nact;
+  if (m == 0) {
+    for (int p = 0; p < n; ++p) rho[p] = 0.0;
+    if (grad)
+      for (int k = 0; k < 3; ++k)
+        for (int p = 0; p < n; ++p) grad[k * gstride + p] = 0.0;
+    return;
+  }
+  // X[nu][p] = sum_mu P[mu,nu] phi[mu][p]
+  std::vector<double> X((size_t)m * n, 0.0);
+  for (int nu = 0; nu < m; ++nu) {
+    double* x = &X[(size_t)nu * n];
+    const double* Pcol = P + (size_t)A.idx[nu] * nbf;
+    for (int mu = 0; mu < m; ++mu) {
+      const double pm = Pcol[A.idx[mu]];
+      const double* ph = &A.phi[(size_t)mu * n];
+      for (int p = 0; p < n; ++p) x[p] += pm * ph[p];
+    }
+  }
+  for (int p = 0; p < n; ++p) rho[p] = 0.0;
+  for (int nu = 0; nu < m; ++nu) {
+    const double* x = &X[(size_t)nu * n];
+    const double* ph = &A.phi[(size_t)nu * n];
+    for (int p = 0; p < n; ++p) rho[p] += x[p] * ph[p];
+  }
+  if (grad) {
+    for (int k = 0; k < 3; ++k) {
+      double* g = grad + k * gstride;
+      for (int p = 0; p < n; ++p) g[p] = 0.0;
+      for (int nu = 0; nu < m; ++nu) {
+        const double* x = &X[(size_t)nu * n];
+        const double* gp = &A.grad[((size_t)3 * nu + k) * n];
+        for (int p = 0; p < n; ++p) g[p] += x[p] * gp[p];
+      }
+      for (int p = 0; p < n; ++p) g[p] *= 2.0;
+    }
+  }
+}
+
+// adds the block's contribution of one spin into F (nbf x nbf, column-major)
+static void adder_block(const ActiveBlock& A, int nbf, const double* wv, const double* wg /*3*npts or null*/,
+                        double* F) {
+  const int n = A.npts, m = A.nact;
+  if (m == 0) return;
+  std::vector<double> G((size_t)m * n);
+  for (int f = 0; f < m; ++f) {
+    const double* ph = &A.phi[(size_t)f * n];
+    double* g = &G[(size_t)f * n];
+    if (wg) {
+      const double* gx = &A.grad[((size_t)3 * f + 0) * n];
+      const double* gy = &A.grad[((size_t)3 * f + 1) * n];
+      const double* gz = &A.grad[((size_t)3 * f + 2) * n];
+      for (int p = 0; p < n; ++p)
+        g[p] = wg[p] * gx[p] + wg[n + p] * gy[p] + wg[2 * n + p] * gz[p] + 0.5 * wv[p] * ph[p];
+    } else {
+      for (int p = 0; p < n; ++p) g[p] = wv[p] * ph[p];
+    }
+  }
+  for (int a = 0; a < m; ++a) {
+    const double* pa = &A.phi[(size_t)a * n];
+    double* Fcol = F + (size_t)A.idx[a] * nbf;
+    for (int b = 0; b < m; ++b) {
+      const double* gb = &G[(size_t)b * n];
+      double s = 0.0;
+      for (int p = 0; p < n; ++p) s += pa[p] * gb[p];
+      if (wg) {
+        // F_b = tmp + tmp^T with tmp = phi^T G
+        Fcol[A.idx[b]] += s;
+        F[(size_t)A.idx[b] * nbf + A.idx[a]] += s;
+      } else {
+        Fcol[A.idx[b]] += s;
+      }
+    }
+  }
+}
+
+static int block_size(long b, long nblocks, long npts, int maxb) {
+  if (b == nblocks - 1) {
+    int r = (int)(npts % maxb);
+    return r == 0 ? maxb : r;
+  }
+  return maxb;
+}
+
+static void add_scalar(const Basis& B, const double* xyz, const double* w, long npts, int maxb, double thr,
+                       double ave_thr, int nspin, const double* v, const double* g, double* F) {
+  const int nbf = B.nbf;
+  const long nblocks = (npts + maxb - 1) / maxb;
+  const int nthreads = omp_get_max_threads();
+  std::vector<std::vector<double>> Ft(nthreads, std::vector<double>((size_t)nspin * nbf * nbf, 0.0));
+#pragma omp parallel
+  {
+    ActiveBlock A;
+    std::vector<double> fv, fg, wv, wg;
+    std::vector<int> negl;
+    double* myF = Ft[omp_get_thread_num()].data();
+#pragma omp for schedule(dynamic)
+    for (long b = 0; b < nblocks; ++b) {
+      const long first = b * maxb;
+      const int n = block_size(b, nblocks, npts, maxb);
+      eval_active(B, xyz + 3 * first, n, thr, g ? 1 : 0, A, fv, fg, negl);
+      for (int s = 0; s < nspin; ++s) {
+        wv.resize(n);
+        double ave = 0.0;
+        for (int p = 0; p < n; ++p) {
+          wv[p] = v[s * npts + first + p] * w[first + p];
+          ave += std::fabs(wv[p]);
+        }
+        if (g) {
+          wg.resize(3 * n);
+          for (int k = 0; k < 3; ++k)
+            for (int p = 0; p < n; ++p) {
+              wg[k * n + p] = w[first + p] * g[(s * 3 + k) * npts + first + p];
+              ave += std::fabs(wg[k * n + p]);
+            }
+        }
+        if (ave / n < ave_thr) continue;
+        adder_block(A, nbf, wv.data(), g ? wg.data() : nullptr, myF + (size_t)s * nbf * nbf);
+      }
+    }
+  }
+  for (auto& m : Ft)
+    for (size_t i = 0; i < m.size(); ++i) F[i] += m[i];
+}
+
+static void density(const Basis& B, const double* xyz, long npts, int maxb, double thr, int nspin, const double* P,
+                    double* rho, double* grad) {
+  const int nbf = B.nbf;
+  const long nblocks = (npts + maxb - 1) / maxb;
+#pragma omp parallel
+  {
+    ActiveBlock A;
+    std::vector<double> fv, fg;
+    std::vector<int> negl;
+#pragma omp for schedule(dynamic)
+    for (long b = 0; b < nblocks; ++b) {
+      const long first = b * maxb;
+      const int n = block_size(b, nblocks, npts, maxb);
+      eval_active(B, xyz + 3 * first, n, thr, 1, A, fv, fg, negl);
+      for (int s = 0; s < nspin; ++s)
+        density_block(A, nbf, P + (size_t)s * nbf * nbf, rho + s * npts + first,
+                      grad ? grad + (size_t)s * 3 * npts + first : nullptr, npts);
+    }
+  }
+}
+
+static void functional(int func, int nspin, long npts, int maxb, const double* rho, const double* grad, double* epuv,
+                       double* dfdrho, double* dfdgrad) {
+  const bool gga = functional_is_gga(func);
+  const long blk = maxb > 0 ? maxb : npts;
+  const long nblocks = (npts + blk - 1) / blk;
+#pragma omp parallel for schedule(dynamic)
+  for (long b = 0; b < nblocks; ++b) {
+    const long first = b * blk;
+    const long n = std::min(blk, npts - first);
+    bool skip = maxb > 0;
+    for (int s = 0; s < nspin && skip; ++s) {
+      double sum = 0.0;
+      for (long p = 0; p < n; ++p) sum += std::fabs(rho[s * npts + first + p]);
+      skip = skip && (sum < n * 1e-12);
+    }
+    for (long p = first; p < first + n; ++p) {
+      double in[8] = {0, 0, 0, 0, 0, 0, 0, 0}, out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      if (!skip) {
+        if (nspin == 1) {
+          in[0] = rho[p];
+          if (gga)
+            for (int k = 0; k < 3; ++k) in[1 + k] = grad[k * npts + p];
+        } else {
+          in[0] = rho[p];
+          in[1] = rho[npts + p];
+          if (gga)
+            for (int k = 0; k < 3; ++k) {
+              in[2 + k] = grad[k * npts + p];
+              in[5 + k] = grad[(3 + k) * npts + p];
+            }
+        }
+        functional_point(func, nspin, in, out);
+      }
+      epuv[p] = out[0];
+      if (nspin == 1) {
+        dfdrho[p] = out[1];
+        if (gga && dfdgrad)
+          for (int k = 0; k < 3; ++k) dfdgrad[k * npts + p] = out[2 + k];
+      } else {
+        dfdrho[p] = out[1];
+        dfdrho[npts + p] = out[2];
+        if (gga && dfdgrad)
+          for (int k = 0; k < 3; ++k) {
+            dfdgrad[k * npts + p] = out[3 + k];
+            dfdgrad[(3 + k) * npts + p] = out[6 + k];
+          }
+      }
+    }
+  }
+}
+
+}  // namespace orc
+
+extern "C" {
+
+int orc_density(const void* basis, const double* xyz, long npts, int max_block, double thr, int nspin, const double* P,
+                double* rho, double* grad) {
+  orc::density(*static_cast<const orc::Basis*>(basis), xyz, npts, max_block, thr, nspin, P, rho, grad);
+  return 0;
+}
+
+int orc_functional(int func, int nspin, long npts, int max_block, const double* rho, const double* grad, double* epuv,
+                   double* dfdrho, double* dfdgrad) {
+  orc::functional(func, nspin, npts, max_block, rho, grad, epuv, dfdrho, dfdgrad);
+  return 0;
+}
+
+int orc_functional_is_gga(int func) { return orc::functional_is_gga(func) ? 1 : 0; }
+
+int orc_add_scalar(const void* basis, const double* xyz, const double* w, long npts, int max_block, double thr,
+                   double ave_thr, int nspin, const double* v, const double* g, double* F) {
+  orc::add_scalar(*static_cast<const orc::Basis*>(basis), xyz, w, npts, max_block, thr, ave_thr, nspin, v, g, F);
+  return 0;
+}
+
+int orc_vxc(const void* basis, const double* xyz, const double* w, long npts, int max_block, double thr,
+            double ave_thr, int func, int nspin, const double* P, double* V, double* Exc, double* Nel, int threads) {
+  const orc::Basis& B = *static_cast<const orc::Basis*>(basis);
+  const int saved = omp_get_max_threads();
+  if (threads > 0) omp_set_num_threads(threads);
+  const bool gga = orc::functional_is_gga(func);
+  std::vector<double> rho((size_t)nspin * npts), grad(gga ? (size_t)nspin * 3 * npts : 0);
+  orc::density(B, xyz, npts, max_block, thr, nspin, P, rho.data(), gga ? grad.data() : nullptr);
+  std::vector<double> epuv(npts), dfdrho((size_t)nspin * npts), dfdgrad(gga ? (size_t)nspin * 3 * npts : 0);
+  // FunctionalLibrary(128): the functional's block size is fixed at 128 (FuncPotential.cpp:86)
+  orc::functional(func, nspin, npts, 128, rho.data(), gga ? grad.data() : nullptr, epuv.data(), dfdrho.data(),
+                  gga ? dfdgrad.data() : nullptr);
+  double e = 0.0, ne = 0.0;
+#pragma omp parallel for reduction(+ : e, ne)
+  for (long p = 0; p < npts; ++p) {
+    e += epuv[p] * w[p];
+    double r = 0.0;
+    for (int s = 0; s < nspin; ++s) r += rho[s * npts + p];
+    ne += r * w[p];
+  }
+  const int nbf = B.nbf;
+  std::memset(V, 0, sizeof(double) * nspin * nbf * nbf);
+  orc::add_scalar(B, xyz, w, npts, max_block, thr, ave_thr, nspin, dfdrho.data(), gga ? dfdgrad.data() : nullptr, V);
+  *Exc = e;
+  *Nel = ne;
+  if (threads > 0) omp_set_num_threads(saved);
+  return 0;
+}
+
+}  // extern "C"
