@@ -1,0 +1,183 @@
+/*
+ * xcgpu -- GB300 (sm_103a) exchange-correlation numerical integration.
+ *
+ * C ABI of the drop-in for Serenity's XC grid path.  Every entry point takes
+ * plain pointers and sizes; handles are opaque; errors are status codes with a
+ * message from xcgpu_last_error() (the C++ facade in serenity_xc.hpp turns them
+ * back into exceptions, as the reference throws SerenityError).  One context
+ * drives one GPU; a context is not thread-safe (one context per host thread).
+ *
+ * Conventions (the reference's):
+ *   points      xyz interleaved (x0,y0,z0,x1,...), bohr; weights alongside
+ *   matrices    n_bf x n_bf FP64, column-major (Eigen default); spin-resolved
+ *               inputs/outputs are nspin consecutive matrices (alpha, beta)
+ *   grid data   nspin consecutive vectors of length n; gradients as x, y, z
+ *               vectors of length n per spin
+ *   blocks      consecutive runs of max_block points, the last one ragged
+ *   mem         XCGPU_MEM_HOST: arguments are host pointers (copied inside);
+ *               XCGPU_MEM_DEVICE: arguments are device pointers on the
+ *               context's GPU (no copies)
+ */
+#ifndef XCGPU_H
+#define XCGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  XCGPU_OK = 0,
+  XCGPU_ERR_INVALID = 1,     /* bad argument: sizes, mismatched grid/basis, unknown functional */
+  XCGPU_ERR_CUDA = 2,        /* a CUDA call failed; message holds cudaGetErrorString */
+  XCGPU_ERR_NO_MEMORY = 3,   /* device allocation failed */
+  XCGPU_ERR_BUDGET = 4,      /* request exceeds the context's HBM budget */
+  XCGPU_ERR_UNSUPPORTED = 5, /* e.g. angular momentum > 6, derivative order > 2 */
+  XCGPU_ERR_TIMEOUT = 6,     /* a bounded device-side wait gave up */
+  XCGPU_ERR_IO = 7           /* a data file could not be read */
+} xcgpu_status;
+
+enum { XCGPU_MEM_HOST = 0, XCGPU_MEM_DEVICE = 1 };
+
+/* precision of a whole build */
+enum {
+  XCGPU_PREC_FP64 = 0, /* every stage in FP64: the drop-in */
+  XCGPU_PREC_MIXED = 1 /* FP32 basis values, 3xTF32 tensor-core contractions with FP32
+                          accumulation; FP64 functional, grid sums and cross-block Vxc */
+};
+
+/* functionals (CompositeFunctionals.cpp:233-246; basic_functionals.dat) */
+enum {
+  XCGPU_FUNC_LDA = 1,  /* Slater + VWN5 */
+  XCGPU_FUNC_PBE = 2,  /* PBE exchange + PBE correlation */
+  XCGPU_FUNC_BLYP = 3, /* Becke 88 + LYP */
+  XCGPU_FUNC_SLATER = 16,
+  XCGPU_FUNC_VWN5 = 17,
+  XCGPU_FUNC_PBEX = 18,
+  XCGPU_FUNC_PBEC = 19,
+  XCGPU_FUNC_B88 = 20,
+  XCGPU_FUNC_LYP = 21,
+  XCGPU_FUNC_PW92 = 22
+};
+
+typedef struct xcgpu_ctx xcgpu_ctx;
+typedef struct xcgpu_grid xcgpu_grid;
+typedef struct xcgpu_basis xcgpu_basis;
+typedef struct xcgpu_plan xcgpu_plan;
+
+typedef struct {
+  int device;              /* CUDA device ordinal */
+  uint64_t hbm_budget;     /* bytes this context may hold; 0 = 90% of free memory at creation */
+  uint64_t scratch_bytes;  /* cap on per-build scratch; 0 = automatic */
+} xcgpu_config;
+
+/* ---- context ------------------------------------------------------------------------- */
+xcgpu_status xcgpu_ctx_create(const xcgpu_config* cfg, xcgpu_ctx** out);
+void xcgpu_ctx_destroy(xcgpu_ctx* ctx);
+const char* xcgpu_last_error(const xcgpu_ctx* ctx);
+/* stream the context launches on (a cudaStream_t); NULL = the context's own stream */
+xcgpu_status xcgpu_set_stream(xcgpu_ctx* ctx, void* stream);
+xcgpu_status xcgpu_synchronize(xcgpu_ctx* ctx);
+/* bytes currently held on the device by this context */
+uint64_t xcgpu_bytes_in_use(const xcgpu_ctx* ctx);
+/* number of this library's kernels launched by the context so far */
+uint64_t xcgpu_kernel_launches(const xcgpu_ctx* ctx);
+
+/* Per-kernel device timing: when enabled, every kernel launch of the context is
+ * bracketed by CUDA events on the context's stream; xcgpu_get_timing() synchronises
+ * and returns the summed milliseconds and launch counts per kernel class
+ * (XCGPU_KERNEL_* below), then resets them. */
+enum {
+  XCGPU_KERNEL_EVAL = 0,       /* basis functions on the grid (FP64 path) */
+  XCGPU_KERNEL_DENSITY = 1,    /* rho / grad rho */
+  XCGPU_KERNEL_FUNCTIONAL = 2, /* functional + grid sums */
+  XCGPU_KERNEL_ADDER = 3,      /* Vxc accumulation */
+  XCGPU_KERNEL_OTHER = 4,      /* screening, skip flags, reductions, symmetrisation */
+  XCGPU_KERNEL_CLASSES = 5
+};
+xcgpu_status xcgpu_set_timing(xcgpu_ctx* ctx, int enable);
+xcgpu_status xcgpu_get_timing(xcgpu_ctx* ctx, double* ms, uint64_t* launches);
+
+/* ---- grid: replaces GridController/AtomCenteredGridController ------------------------ */
+/* Wrap an existing grid (GridController::getGridPoints()/getWeights(),
+ * src/grid/GridController.h:58-69). */
+xcgpu_status xcgpu_grid_create(xcgpu_ctx* ctx, const double* xyz, const double* w, uint64_t npoints, xcgpu_grid** out);
+/* Build an atom-centred Becke grid (GridFactory::produce, GridFactory.cpp:52-320, with
+ * AtomGridFactory's Ahlrichs radial rule, AtomGridFactory.cpp:78-290): Becke partition
+ * weights on the GPU, Hilbert ordering (HilbertRTreeSorting.cpp:46-216) when sort != 0.
+ * accuracy in 1..7 selects the reference's pruned scheme; accuracy 0 uses n_rad x n_ang
+ * unpruned.  lebedev_table: path of serenity_gb300/data/lebedev.txt. */
+xcgpu_status xcgpu_grid_build(xcgpu_ctx* ctx, int natoms, const int* Z, const double* xyz_bohr, int n_rad, int n_ang,
+                              int accuracy, double weight_threshold, int smoothing, int sort,
+                              const char* lebedev_table, xcgpu_grid** out);
+uint64_t xcgpu_grid_npoints(const xcgpu_grid* grid);
+xcgpu_status xcgpu_grid_copy(const xcgpu_grid* grid, double* xyz, double* w); /* to host */
+void xcgpu_grid_destroy(xcgpu_grid* grid);
+
+/* ---- basis: replaces BasisController (src/basis/BasisController.h:157-175) ----------- */
+typedef struct {
+  int32_t l;      /* angular momentum, 0..6 */
+  int32_t pure;   /* 1 = real solid harmonics (m = -l..l), 0 = Cartesian (x^l ... z^l) */
+  int32_t nprim;
+  double center[3];
+  const double* alpha; /* nprim exponents */
+  const double* coef;  /* nprim raw contraction coefficients (normalised inside, Shell.cpp:30-47) */
+} xcgpu_shell;
+xcgpu_status xcgpu_basis_create(xcgpu_ctx* ctx, const xcgpu_shell* shells, uint32_t nshell, xcgpu_basis** out);
+uint32_t xcgpu_basis_nbf(const xcgpu_basis* basis);
+/* normalised coefficients of shell s (nprim values) */
+xcgpu_status xcgpu_basis_coefs(const xcgpu_basis* basis, uint32_t s, double* out);
+void xcgpu_basis_destroy(xcgpu_basis* basis);
+
+/* ---- plan: replaces BasisFunctionOnGridController -------------------------------------
+ * (BasisFunctionOnGridController.h:105-287; ctor .cpp:75-101).  Partitions the grid into
+ * blocks of max_block (<= 128) points and screens every shell against every block
+ * (.cpp:192-255), storing the compacted active-function list per block. */
+xcgpu_status xcgpu_plan_create(xcgpu_ctx* ctx, xcgpu_grid* grid, xcgpu_basis* basis, uint32_t max_block,
+                               double radial_threshold, xcgpu_plan** out);
+typedef struct {
+  uint32_t nblocks, max_block, nbf, max_active;
+  uint64_t npoints;
+  uint64_t sum_active;      /* sum over blocks of the active-function count */
+  double flops_per_spin;    /* sum over blocks of 4 * npts_b * n_b^2 */
+} xcgpu_plan_stats;
+xcgpu_status xcgpu_plan_get_stats(const xcgpu_plan* plan, xcgpu_plan_stats* out);
+/* getBlockOnGridData(b) (.cpp:122-131): dense npts_b x nbf column-major values, 3 such
+ * gradient matrices (x,y,z) when deriv >= 1, 6 Hessian matrices (xx,xy,xz,yy,yz,zz) when
+ * deriv == 2, and negligible[nbf]; host outputs.  deriv > 2 -> XCGPU_ERR_UNSUPPORTED. */
+xcgpu_status xcgpu_block_on_grid(xcgpu_plan* plan, uint32_t block, int deriv, double* values, double* grad,
+                                 double* hess, int32_t* negligible);
+/* active-function list of a block (ascending function indices), returns the count */
+int32_t xcgpu_block_active(const xcgpu_plan* plan, uint32_t block, int32_t* idx);
+void xcgpu_plan_destroy(xcgpu_plan* plan);
+
+/* ---- stages ----------------------------------------------------------------------------
+ * DensityOnGridCalculator::calcDensityAndGradientOnGrid (DensityOnGridCalculator.h:53-128,
+ * MatrixOperatorToGridTransformer.cpp:37-198): rho = rowsum((phi P_b) o phi),
+ * grad rho = 2 rowsum((phi P_b) o grad phi).  grad may be NULL (density only). */
+xcgpu_status xcgpu_density(xcgpu_plan* plan, int nspin, const double* P, double* rho, double* grad, int mem);
+/* FunctionalLibrary::calcData(GRADIENTS, f, ., order 1) (FunctionalLibrary.cpp:40-71,
+ * XCFun.cpp:39-158): epuv (energy per volume), dF/drho and, for GGAs, dF/d(grad rho).
+ * skip_block > 0 applies the reference's block skip (sum |rho| < n * 1e-12 on blocks of
+ * skip_block points, XCFun.cpp:136-140). */
+xcgpu_status xcgpu_functional(xcgpu_ctx* ctx, int func, int nspin, uint64_t npoints, uint32_t skip_block,
+                              const double* rho, const double* grad, double* epuv, double* dfdrho, double* dfdgrad,
+                              int mem);
+int xcgpu_functional_is_gga(int func);
+/* ScalarOperatorToMatrixAdder::addScalarOperatorToMatrix (ScalarOperatorToMatrixAdder.h:56-93,
+ * .cpp:51-113,178-303): F += sum_p w (v phi phi^T) (+ the GGA term with g = dF/d grad rho
+ * when g != NULL).  Adds into F; blocks below block_ave_threshold are skipped. */
+xcgpu_status xcgpu_add_scalar(xcgpu_plan* plan, double block_ave_threshold, int nspin, const double* v,
+                              const double* g, double* F, int mem);
+
+/* ---- whole build: FuncPotential::getMatrix + getEnergy (FuncPotential.cpp:74-110) -----
+ * V (nspin matrices) is overwritten with the XC potential matrix; Exc = sum_p w_p epuv_p;
+ * Nel = sum_p w_p rho_p (total density).  P, V in `mem` space; Exc, Nel host scalars. */
+xcgpu_status xcgpu_vxc(xcgpu_plan* plan, int func, int nspin, int precision, double block_ave_threshold,
+                       const double* P, double* V, double* Exc, double* Nel, int mem);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XCGPU_H */

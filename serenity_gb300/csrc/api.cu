@@ -1,0 +1,717 @@
+// C ABI of the xcgpu library: contexts, device memory under an HBM budget, grids,
+// bases, plans (block partition + screening) and the XC stages / whole build.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "functionals.cuh"
+#include "internal.h"
+
+namespace xcgpu {
+
+DevBuf::~DevBuf() { release(); }
+
+void DevBuf::release() {
+  if (p) {
+    cudaFree(p);
+    if (ctx) ctx->in_use -= bytes;
+  }
+  p = nullptr;
+  bytes = 0;
+}
+
+xcgpu_status DevBuf::alloc(Ctx* c, size_t n) {
+  if (n <= bytes && p) return XCGPU_OK;
+  release();
+  ctx = c;
+  if (n == 0) n = 16;
+  if (c->in_use + n > c->budget)
+    return c->fail(XCGPU_ERR_BUDGET, "device allocation of " + std::to_string(n) + " bytes exceeds the HBM budget (" +
+                                         std::to_string(c->in_use) + " of " + std::to_string(c->budget) + " in use)");
+  cudaError_t e = cudaMalloc(&p, n);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    cudaGetLastError();
+    return c->fail(XCGPU_ERR_NO_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  bytes = n;
+  c->in_use += n;
+  return XCGPU_OK;
+}
+
+template <class T>
+static xcgpu_status upload(Ctx* c, DevBuf& b, const T* src, size_t count) {
+  xcgpu_status st = b.alloc(c, count * sizeof(T));
+  if (st) return st;
+  if (count == 0) return XCGPU_OK;
+  return c->cuda(cudaMemcpyAsync(b.p, src, count * sizeof(T), cudaMemcpyHostToDevice, c->stream), "upload");
+}
+
+static double dfact(int n) {
+  double r = 1.0;
+  for (int k = n; k > 1; k -= 2) r *= k;
+  return r;
+}
+static double factorial(int n) {
+  double r = 1.0;
+  for (int k = 2; k <= n; ++k) r *= k;
+  return r;
+}
+static double choose(int n, int k) {
+  return (k < 0 || k > n) ? 0.0 : factorial(n) / (factorial(k) * factorial(n - k));
+}
+
+// Real solid harmonics as polynomials in the Cartesian monomials x^a y^b z^c (order
+// a = l..0, b = l-a..0), m = -l..l; closed form of Helgaker, Joergensen & Olsen,
+// "Molecular Electronic-Structure Theory", section 6.4.
+std::vector<double> solid_harmonic_matrix(int l) {
+  const int nc = ncart(l);
+  std::vector<double> T((2 * l + 1) * nc, 0.0);
+  auto col = [l](int a, int b) {  // index of (a, b, l-a-b)
+    int k = 0;
+    for (int aa = l; aa > a; --aa) k += l - aa + 1;
+    return k + (l - a - b);
+  };
+  for (int m = -l; m <= l; ++m) {
+    const int am = std::abs(m);
+    const int twice_vm = m < 0 ? 1 : 0;
+    const double N = std::sqrt(2.0 * factorial(l + am) * factorial(l - am) / (m == 0 ? 2.0 : 1.0)) /
+                     (std::pow(2.0, am) * factorial(l));
+    for (int t = 0; t <= (l - am) / 2; ++t)
+      for (int u = 0; u <= t; ++u)
+        for (int tv = twice_vm; tv <= am; tv += 2) {  // 2v runs over vm*2, vm*2+2, ... <= |m|
+          const int sign_exp = t + (tv - twice_vm) / 2;
+          const double C = (sign_exp % 2 ? -1.0 : 1.0) * std::pow(0.25, t) * choose(l, t) * choose(l - t, am + t) *
+                           choose(t, u) * choose(am, tv);
+          const int py = 2 * u + tv;
+          const int px = 2 * t + am - py;
+          T[(m + l) * nc + col(px, py)] += N * C;
+        }
+  }
+  return T;
+}
+
+// Cartesian factors sqrt((2l-1)!! / ((2a-1)!! (2b-1)!! (2c-1)!!)) (Normalization.h:82-87).
+std::vector<double> cartesian_norms(int l) {
+  std::vector<double> out;
+  for (int a = l; a >= 0; --a)
+    for (int b = l - a; b >= 0; --b) {
+      const int c = l - a - b;
+      out.push_back(std::sqrt(dfact(2 * l - 1) / (dfact(2 * a - 1) * dfact(2 * b - 1) * dfact(2 * c - 1))));
+    }
+  return out;
+}
+
+}  // namespace xcgpu
+
+using namespace xcgpu;
+
+#define XC_TRY(expr)                 \
+  do {                               \
+    xcgpu_status _s = (expr);        \
+    if (_s != XCGPU_OK) return _s;   \
+  } while (0)
+
+extern "C" {
+
+xcgpu_status xcgpu_ctx_create(const xcgpu_config* cfg, xcgpu_ctx** out) {
+  if (!out) return XCGPU_ERR_INVALID;
+  *out = nullptr;
+  xcgpu_ctx* c = new xcgpu_ctx();
+  c->device = cfg ? cfg->device : 0;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev <= c->device) {
+    cudaGetLastError();
+    delete c;
+    return XCGPU_ERR_CUDA;
+  }
+  if ((e = cudaSetDevice(c->device)) != cudaSuccess) {
+    delete c;
+    return XCGPU_ERR_CUDA;
+  }
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  c->budget = (cfg && cfg->hbm_budget) ? cfg->hbm_budget : (uint64_t)(0.9 * fr);
+  c->scratch_cap = (cfg && cfg->scratch_bytes) ? cfg->scratch_bytes : std::min<uint64_t>(c->budget / 4, 4ull << 30);
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return XCGPU_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  *out = c;
+  return XCGPU_OK;
+}
+
+void xcgpu_ctx_destroy(xcgpu_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->scratch.release();
+  c->scratch2.release();
+  c->partials.release();
+  c->skip.release();
+  for (auto& pe : c->ev_pending) {
+    cudaEventDestroy(pe.second.first);
+    cudaEventDestroy(pe.second.second);
+  }
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+const char* xcgpu_last_error(const xcgpu_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+xcgpu_status xcgpu_set_stream(xcgpu_ctx* c, void* s) {
+  if (!c) return XCGPU_ERR_INVALID;
+  c->stream = s ? static_cast<cudaStream_t>(s) : c->own_stream;
+  return XCGPU_OK;
+}
+
+xcgpu_status xcgpu_synchronize(xcgpu_ctx* c) {
+  if (!c) return XCGPU_ERR_INVALID;
+  return c->cuda(cudaStreamSynchronize(c->stream), "synchronize");
+}
+
+xcgpu_status xcgpu_set_timing(xcgpu_ctx* c, int enable) {
+  if (!c) return XCGPU_ERR_INVALID;
+  c->timing = enable != 0;
+  return XCGPU_OK;
+}
+
+xcgpu_status xcgpu_get_timing(xcgpu_ctx* c, double* ms, uint64_t* launches) {
+  if (!c) return XCGPU_ERR_INVALID;
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "timing"));
+  for (auto& pe : c->ev_pending) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, pe.second.first, pe.second.second);
+    c->t_ms[pe.first] += t;
+    c->t_count[pe.first] += 1;
+    c->ev_pool.push_back(pe.second.first);
+    c->ev_pool.push_back(pe.second.second);
+  }
+  c->ev_pending.clear();
+  for (int k = 0; k < kClasses; ++k) {
+    if (ms) ms[k] = c->t_ms[k];
+    if (launches) launches[k] = c->t_count[k];
+    c->t_ms[k] = 0;
+    c->t_count[k] = 0;
+  }
+  return XCGPU_OK;
+}
+
+uint64_t xcgpu_bytes_in_use(const xcgpu_ctx* c) { return c ? c->in_use : 0; }
+uint64_t xcgpu_kernel_launches(const xcgpu_ctx* c) { return c ? c->launches : 0; }
+
+/* ---- grid ---- */
+xcgpu_status xcgpu_grid_create(xcgpu_ctx* c, const double* xyz, const double* w, uint64_t n, xcgpu_grid** out) {
+  if (!c || !out || (n && (!xyz || !w))) return c ? c->fail(XCGPU_ERR_INVALID, "grid: null argument") : XCGPU_ERR_INVALID;
+  cudaSetDevice(c->device);
+  auto* g = new xcgpu_grid();
+  g->ctx = c;
+  g->n = (long)n;
+  xcgpu_status st = upload(c, g->xyz, xyz, 3 * n);
+  if (!st) st = upload(c, g->w, w, n);
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "grid upload");
+  if (st) {
+    delete g;
+    return st;
+  }
+  *out = g;
+  return XCGPU_OK;
+}
+
+uint64_t xcgpu_grid_npoints(const xcgpu_grid* g) { return g ? (uint64_t)g->n : 0; }
+
+xcgpu_status xcgpu_grid_copy(const xcgpu_grid* g, double* xyz, double* w) {
+  if (!g) return XCGPU_ERR_INVALID;
+  Ctx* c = g->ctx;
+  if (xyz) XC_TRY(c->cuda(cudaMemcpy(xyz, g->xyz.p, 3 * g->n * sizeof(double), cudaMemcpyDeviceToHost), "grid copy"));
+  if (w) XC_TRY(c->cuda(cudaMemcpy(w, g->w.p, g->n * sizeof(double), cudaMemcpyDeviceToHost), "grid copy"));
+  return XCGPU_OK;
+}
+
+void xcgpu_grid_destroy(xcgpu_grid* g) { delete g; }
+
+/* ---- basis ---- */
+xcgpu_status xcgpu_basis_create(xcgpu_ctx* c, const xcgpu_shell* shells, uint32_t nshell, xcgpu_basis** out) {
+  if (!c || !out || (nshell && !shells)) return c ? c->fail(XCGPU_ERR_INVALID, "basis: null argument") : XCGPU_ERR_INVALID;
+  cudaSetDevice(c->device);
+  auto* B = new xcgpu_basis();
+  B->ctx = c;
+  B->nshell = (int)nshell;
+  const double pi32 = std::pow(M_PI, 1.5);
+  for (uint32_t s = 0; s < nshell; ++s) {
+    const xcgpu_shell& sh = shells[s];
+    if (sh.l < 0 || sh.l > kMaxL) {
+      delete B;
+      return c->fail(XCGPU_ERR_UNSUPPORTED, "Angular momentum too high for transformation spherical harmonics.");
+    }
+    if (sh.nprim <= 0 || !sh.alpha || !sh.coef) {
+      delete B;
+      return c->fail(XCGPU_ERR_INVALID, "basis: shell without primitives");
+    }
+    B->l.push_back(sh.l);
+    B->pure.push_back(sh.pure ? 1 : 0);
+    B->nprim.push_back(sh.nprim);
+    B->prim_off.push_back((int)B->alpha.size());
+    B->first.push_back(B->nbf);
+    for (int k = 0; k < 3; ++k) B->center.push_back(sh.center[k]);
+    // libint2 convention (Shell.cpp:30-47): normalise each primitive for the x^l
+    // component, then scale the contraction to unit self-overlap.
+    const int L = sh.l;
+    std::vector<double> cf(sh.coef, sh.coef + sh.nprim);
+    for (int p = 0; p < sh.nprim; ++p) {
+      const double ta = 2.0 * sh.alpha[p];
+      cf[p] *= std::sqrt(std::pow(2.0, L) * std::pow(ta, L + 1.5) / (pi32 * dfact(2 * L - 1)));
+    }
+    double ov = 0.0;
+    for (int p = 0; p < sh.nprim; ++p)
+      for (int q = 0; q < sh.nprim; ++q)
+        ov += dfact(2 * L - 1) * pi32 * cf[p] * cf[q] / (std::pow(2.0, L) * std::pow(sh.alpha[p] + sh.alpha[q], L + 1.5));
+    for (int p = 0; p < sh.nprim; ++p) {
+      B->alpha.push_back(sh.alpha[p]);
+      B->coef.push_back(cf[p] / std::sqrt(ov));
+    }
+    B->nbf += sh.pure ? 2 * L + 1 : ncart(L);
+    B->maxl = std::max(B->maxl, L);
+  }
+  std::vector<double> trans, cnorm;
+  std::vector<int> toff, coff;
+  for (int l = 0; l <= kMaxL; ++l) {
+    toff.push_back((int)trans.size());
+    coff.push_back((int)cnorm.size());
+    auto T = solid_harmonic_matrix(l);
+    auto N = cartesian_norms(l);
+    trans.insert(trans.end(), T.begin(), T.end());
+    cnorm.insert(cnorm.end(), N.begin(), N.end());
+  }
+  xcgpu_status st = XCGPU_OK;
+  if (!st) st = upload(c, B->d_l, B->l.data(), nshell);
+  if (!st) st = upload(c, B->d_pure, B->pure.data(), nshell);
+  if (!st) st = upload(c, B->d_nprim, B->nprim.data(), nshell);
+  if (!st) st = upload(c, B->d_prim_off, B->prim_off.data(), nshell);
+  if (!st) st = upload(c, B->d_first, B->first.data(), nshell);
+  if (!st) st = upload(c, B->d_center, B->center.data(), B->center.size());
+  if (!st) st = upload(c, B->d_alpha, B->alpha.data(), B->alpha.size());
+  if (!st) st = upload(c, B->d_coef, B->coef.data(), B->coef.size());
+  if (!st) st = upload(c, B->d_trans, trans.data(), trans.size());
+  if (!st) st = upload(c, B->d_cnorm, cnorm.data(), cnorm.size());
+  if (!st) st = upload(c, B->d_toff, toff.data(), toff.size());
+  if (!st) st = upload(c, B->d_coff, coff.data(), coff.size());
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "basis upload");
+  if (st) {
+    delete B;
+    return st;
+  }
+  DevBasis& d = B->dev;
+  d.nshell = B->nshell;
+  d.nbf = B->nbf;
+  d.maxl = B->maxl;
+  d.l = B->d_l.as<int>();
+  d.pure = B->d_pure.as<int>();
+  d.nprim = B->d_nprim.as<int>();
+  d.prim_off = B->d_prim_off.as<int>();
+  d.first = B->d_first.as<int>();
+  d.center = B->d_center.as<double>();
+  d.alpha = B->d_alpha.as<double>();
+  d.coef = B->d_coef.as<double>();
+  d.trans = B->d_trans.as<double>();
+  d.cnorm = B->d_cnorm.as<double>();
+  d.trans_off = B->d_toff.as<int>();
+  d.cnorm_off = B->d_coff.as<int>();
+  *out = B;
+  return XCGPU_OK;
+}
+
+uint32_t xcgpu_basis_nbf(const xcgpu_basis* b) { return b ? (uint32_t)b->nbf : 0; }
+
+xcgpu_status xcgpu_basis_coefs(const xcgpu_basis* b, uint32_t s, double* out) {
+  if (!b || (int)s >= b->nshell || !out) return XCGPU_ERR_INVALID;
+  for (int i = 0; i < b->nprim[s]; ++i) out[i] = b->coef[b->prim_off[s] + i];
+  return XCGPU_OK;
+}
+
+void xcgpu_basis_destroy(xcgpu_basis* b) { delete b; }
+
+/* ---- plan ---- */
+xcgpu_status xcgpu_plan_create(xcgpu_ctx* c, xcgpu_grid* g, xcgpu_basis* B, uint32_t max_block, double thr,
+                               xcgpu_plan** out) {
+  if (!c || !g || !B || !out) return c ? c->fail(XCGPU_ERR_INVALID, "plan: null argument") : XCGPU_ERR_INVALID;
+  if (max_block == 0 || max_block > (uint32_t)kBlockPoints)
+    return c->fail(XCGPU_ERR_UNSUPPORTED, "plan: max_block must be in 1..128");
+  if (g->ctx != c || B->ctx != c) return c->fail(XCGPU_ERR_INVALID, "plan: grid and basis belong to another context");
+  cudaSetDevice(c->device);
+  auto* P = new xcgpu_plan();
+  P->ctx = c;
+  P->grid = g;
+  P->basis = B;
+  P->max_block = (int)max_block;
+  P->radial_threshold = thr;
+  P->nblocks = (int)((g->n + max_block - 1) / max_block);
+  const int nb = P->nblocks, ns = B->nshell;
+  DevBuf flags, nfn;
+  xcgpu_status st = flags.alloc(c, (size_t)nb * ns + 1);
+  if (!st) st = nfn.alloc(c, (size_t)nb * sizeof(int) + 4);
+  if (!st) st = launch_screen(c, B->dev, g->xyz.as<double>(), g->n, P->max_block, nb, thr, flags.as<unsigned char>(),
+                              nfn.as<int>());
+  std::vector<unsigned char> hf((size_t)nb * ns);
+  if (!st && nb)
+    st = c->cuda(cudaMemcpyAsync(hf.data(), flags.p, hf.size(), cudaMemcpyDeviceToHost, c->stream), "plan flags");
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "plan screen");
+  if (st) {
+    delete P;
+    return st;
+  }
+  P->sh_off.assign(1, 0);
+  P->fn_off.assign(1, 0);
+  P->work_off.assign(1, 0);
+  for (int b = 0; b < nb; ++b) {
+    for (int s = 0; s < ns; ++s)
+      if (hf[(size_t)b * ns + s]) {
+        P->sh_list.push_back(s);
+        const int nf = B->pure[s] ? 2 * B->l[s] + 1 : ncart(B->l[s]);
+        for (int f = 0; f < nf; ++f) P->fn_list.push_back(B->first[s] + f);
+      }
+    P->sh_off.push_back((int)P->sh_list.size());
+    P->fn_off.push_back((int)P->fn_list.size());
+    const int nact = P->fn_off[b + 1] - P->fn_off[b];
+    P->max_active = std::max(P->max_active, nact);
+    const long npts = std::min<long>(P->max_block, g->n - (long)b * P->max_block);
+    P->flops += 4.0 * npts * (double)nact * nact;
+    const int nt = (nact + 63) / 64;
+    for (int i = 0; i < nt; ++i)
+      for (int j = i; j < nt; ++j) {
+        P->work.push_back(b);
+        P->work.push_back(i);
+        P->work.push_back(j);
+      }
+    P->work_off.push_back((long)P->work.size() / 3);
+  }
+  st = upload(c, P->d_sh_off, P->sh_off.data(), P->sh_off.size());
+  if (!st) st = upload(c, P->d_sh_list, P->sh_list.data(), P->sh_list.size());
+  if (!st) st = upload(c, P->d_fn_off, P->fn_off.data(), P->fn_off.size());
+  if (!st) st = upload(c, P->d_fn_list, P->fn_list.data(), P->fn_list.size());
+  if (!st) st = upload(c, P->d_work, P->work.data(), P->work.size());
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "plan upload");
+  if (st) {
+    delete P;
+    return st;
+  }
+  DevPlan& d = P->dev;
+  d.nblocks = nb;
+  d.max_block = P->max_block;
+  d.nbf = B->nbf;
+  d.npoints = g->n;
+  d.xyz = g->xyz.as<double>();
+  d.w = g->w.as<double>();
+  d.sh_off = P->d_sh_off.as<int>();
+  d.sh_list = P->d_sh_list.as<int>();
+  d.fn_off = P->d_fn_off.as<int>();
+  d.fn_list = P->d_fn_list.as<int>();
+  d.radial_threshold = thr;
+  d.exponent_threshold = thr > 0 ? -std::log(thr) : HUGE_VAL;
+  *out = P;
+  return XCGPU_OK;
+}
+
+xcgpu_status xcgpu_plan_get_stats(const xcgpu_plan* P, xcgpu_plan_stats* s) {
+  if (!P || !s) return XCGPU_ERR_INVALID;
+  s->nblocks = (uint32_t)P->nblocks;
+  s->max_block = (uint32_t)P->max_block;
+  s->nbf = (uint32_t)P->basis->nbf;
+  s->max_active = (uint32_t)P->max_active;
+  s->npoints = (uint64_t)P->grid->n;
+  s->sum_active = P->fn_list.size();
+  s->flops_per_spin = P->flops;
+  return XCGPU_OK;
+}
+
+int32_t xcgpu_block_active(const xcgpu_plan* P, uint32_t b, int32_t* idx) {
+  if (!P || (int)b >= P->nblocks) return -1;
+  const int n = P->fn_off[b + 1] - P->fn_off[b];
+  if (idx)
+    for (int i = 0; i < n; ++i) idx[i] = P->fn_list[P->fn_off[b] + i];
+  return n;
+}
+
+void xcgpu_plan_destroy(xcgpu_plan* P) { delete P; }
+
+xcgpu_status xcgpu_block_on_grid(xcgpu_plan* P, uint32_t b, int deriv, double* values, double* grad, double* hess,
+                                 int32_t* negligible) {
+  if (!P) return XCGPU_ERR_INVALID;
+  Ctx* c = P->ctx;
+  if (deriv > 2 || deriv < 0)
+    return c->fail(XCGPU_ERR_UNSUPPORTED, "Third derivatives of basis functions on the grid are not implemented!");
+  if ((int)b >= P->nblocks) return c->fail(XCGPU_ERR_INVALID, "block index out of range");
+  cudaSetDevice(c->device);
+  const int nbf = P->basis->nbf;
+  const int npts = (int)std::min<long>(P->max_block, P->grid->n - (long)b * P->max_block);
+  const int ncomp = deriv == 0 ? 1 : deriv == 1 ? 4 : 10;
+  const size_t plane = (size_t)npts * nbf;
+  DevBuf buf;
+  XC_TRY(buf.alloc(c, ncomp * plane * sizeof(double)));
+  XC_TRY(c->cuda(cudaMemsetAsync(buf.p, 0, ncomp * plane * sizeof(double), c->stream), "memset"));
+  XC_TRY(launch_block_values(c, P->basis->dev, P->dev, (int)b, deriv, buf.as<double>(), npts));
+  std::vector<double> h(ncomp * plane);
+  XC_TRY(c->cuda(cudaMemcpyAsync(h.data(), buf.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "copy"));
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "block_on_grid"));
+  if (values) std::memcpy(values, h.data(), plane * sizeof(double));
+  if (grad && deriv >= 1) std::memcpy(grad, h.data() + plane, 3 * plane * sizeof(double));
+  if (hess && deriv >= 2) std::memcpy(hess, h.data() + 4 * plane, 6 * plane * sizeof(double));
+  if (negligible) {
+    for (int i = 0; i < nbf; ++i) negligible[i] = 1;
+    for (int i = P->fn_off[b]; i < P->fn_off[b + 1]; ++i) negligible[P->fn_list[i]] = 0;
+  }
+  return XCGPU_OK;
+}
+
+int xcgpu_functional_is_gga(int func) { return xc::is_gga(func) ? 1 : 0; }
+
+}  // extern "C"
+
+/* ---- stages and the whole build ------------------------------------------------------ */
+namespace xcgpu {
+
+// Chunks of consecutive blocks whose FP64 slabs fit the scratch cap.
+struct Chunks {
+  std::vector<int> bounds;         // chunk k covers blocks [bounds[k], bounds[k+1])
+  std::vector<long> slab_off;      // per block, offset within its chunk (doubles)
+  long max_chunk_doubles = 0;
+};
+
+static Chunks make_chunks(const xcgpu_plan* P, uint64_t cap_bytes) {
+  Chunks ch;
+  const long cap = std::max<long>((long)(cap_bytes / sizeof(double)), 4L * kBlockPoints * std::max(P->max_active, 1));
+  ch.bounds.push_back(0);
+  long cur = 0;
+  for (int b = 0; b < P->nblocks; ++b) {
+    const long need = 4L * kBlockPoints * (P->fn_off[b + 1] - P->fn_off[b]);
+    if (cur + need > cap && cur > 0) {
+      ch.bounds.push_back(b);
+      ch.max_chunk_doubles = std::max(ch.max_chunk_doubles, cur);
+      cur = 0;
+    }
+    ch.slab_off.push_back(cur);
+    cur += need;
+  }
+  ch.max_chunk_doubles = std::max(ch.max_chunk_doubles, cur);
+  ch.bounds.push_back(P->nblocks);
+  return ch;
+}
+
+struct PlanWork {
+  DevBuf slab_off, P, V, rho, grad, epuv, dfdrho, dfdgrad, askip, sums;
+};
+
+static xcgpu_status stage_density(xcgpu_plan* P, const Chunks& ch, DevBuf& d_slab, int nspin, const double* dP,
+                                  double* rho, double* grad) {
+  Ctx* c = P->ctx;
+  XC_TRY(c->scratch.alloc(c, std::max<long>(ch.max_chunk_doubles, 1) * sizeof(double)));
+  for (size_t k = 0; k + 1 < ch.bounds.size(); ++k) {
+    const int b0 = ch.bounds[k], b1 = ch.bounds[k + 1];
+    const long* so = d_slab.as<long>() + b0;
+    XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, c->scratch.as<double>(), 1));
+    XC_TRY(fp64_density_chunk(c, P->dev, b0, b1, so, c->scratch.as<double>(), nspin, dP, rho, grad));
+  }
+  return XCGPU_OK;
+}
+
+static xcgpu_status stage_adder(xcgpu_plan* P, const Chunks& ch, DevBuf& d_slab, int nspin, const double* v,
+                                const double* g, double thr, DevBuf& skip, double* F) {
+  Ctx* c = P->ctx;
+  XC_TRY(skip.alloc(c, (size_t)nspin * P->nblocks + 1));
+  XC_TRY(launch_block_skip_flags(c, P->dev, nspin, v, g, thr, skip.as<unsigned char>()));
+  XC_TRY(c->scratch.alloc(c, std::max<long>(ch.max_chunk_doubles, 1) * sizeof(double)));
+  for (size_t k = 0; k + 1 < ch.bounds.size(); ++k) {
+    const int b0 = ch.bounds[k], b1 = ch.bounds[k + 1];
+    const long* so = d_slab.as<long>() + b0;
+    XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, c->scratch.as<double>(), 1));
+    XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, so,
+                            c->scratch.as<double>(), nspin, v, g, skip.as<unsigned char>(), F));
+  }
+  return XCGPU_OK;
+}
+
+static xcgpu_status prep_chunks(xcgpu_plan* P, Chunks& ch, DevBuf& d_slab) {
+  Ctx* c = P->ctx;
+  ch = make_chunks(P, c->scratch_cap);
+  XC_TRY(upload(c, d_slab, ch.slab_off.data(), ch.slab_off.size()));
+  return XCGPU_OK;
+}
+
+template <class T>
+static xcgpu_status to_device(Ctx* c, DevBuf& tmp, const T* src, size_t count, int mem, const T** dst) {
+  if (mem == XCGPU_MEM_DEVICE) {
+    *dst = src;
+    return XCGPU_OK;
+  }
+  XC_TRY(upload(c, tmp, src, count));
+  *dst = tmp.as<T>();
+  return XCGPU_OK;
+}
+
+}  // namespace xcgpu
+
+extern "C" {
+
+xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* rho, double* grad, int mem) {
+  if (!P) return XCGPU_ERR_INVALID;
+  Ctx* c = P->ctx;
+  if ((nspin != 1 && nspin != 2) || !Pm || !rho) return c->fail(XCGPU_ERR_INVALID, "density: bad arguments");
+  cudaSetDevice(c->device);
+  const long n = P->grid->n;
+  const int nbf = P->basis->nbf;
+  Chunks ch;
+  DevBuf d_slab, dPm, drho, dgrad;
+  XC_TRY(prep_chunks(P, ch, d_slab));
+  const double* Pd = nullptr;
+  XC_TRY(to_device(c, dPm, Pm, (size_t)nspin * nbf * nbf, mem, &Pd));
+  double* r = rho;
+  double* gr = grad;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(drho.alloc(c, (size_t)nspin * n * sizeof(double)));
+    r = drho.as<double>();
+    if (grad) {
+      XC_TRY(dgrad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+      gr = dgrad.as<double>();
+    }
+  }
+  XC_TRY(c->cuda(cudaMemsetAsync(r, 0, (size_t)nspin * n * sizeof(double), c->stream), "memset rho"));
+  XC_TRY(stage_density(P, ch, d_slab, nspin, Pd, r, gr));
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(c->cuda(cudaMemcpyAsync(rho, r, (size_t)nspin * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "rho"));
+    if (grad)
+      XC_TRY(c->cuda(cudaMemcpyAsync(grad, gr, (size_t)nspin * 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                     "grad"));
+  }
+  return c->cuda(cudaStreamSynchronize(c->stream), "density");
+}
+
+xcgpu_status xcgpu_functional(xcgpu_ctx* c, int func, int nspin, uint64_t n, uint32_t skip_block, const double* rho,
+                              const double* grad, double* epuv, double* dfdrho, double* dfdgrad, int mem) {
+  if (!c) return XCGPU_ERR_INVALID;
+  if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "unknown functional");
+  const bool gga = xc::is_gga(func);
+  if ((nspin != 1 && nspin != 2) || !rho || !epuv || !dfdrho || (gga && (!grad || !dfdgrad)))
+    return c->fail(XCGPU_ERR_INVALID, "functional: bad arguments");
+  cudaSetDevice(c->device);
+  DevBuf a, b, o1, o2, o3;
+  const double *dr = rho, *dg = grad;
+  double *e = epuv, *v = dfdrho, *vg = dfdgrad;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(upload(c, a, rho, (size_t)nspin * n));
+    dr = a.as<double>();
+    if (gga) {
+      XC_TRY(upload(c, b, grad, (size_t)nspin * 3 * n));
+      dg = b.as<double>();
+    }
+    XC_TRY(o1.alloc(c, n * sizeof(double)));
+    XC_TRY(o2.alloc(c, (size_t)nspin * n * sizeof(double)));
+    e = o1.as<double>();
+    v = o2.as<double>();
+    if (gga) {
+      XC_TRY(o3.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+      vg = o3.as<double>();
+    }
+  }
+  XC_TRY(launch_functional(c, func, nspin, (long)n, (int)skip_block, dr, gga ? dg : nullptr, e, v, gga ? vg : nullptr,
+                           nullptr, nullptr, nullptr));
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(c->cuda(cudaMemcpyAsync(epuv, e, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "epuv"));
+    XC_TRY(c->cuda(cudaMemcpyAsync(dfdrho, v, (size_t)nspin * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                   "dfdrho"));
+    if (gga)
+      XC_TRY(c->cuda(
+          cudaMemcpyAsync(dfdgrad, vg, (size_t)nspin * 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+          "dfdgrad"));
+  }
+  return c->cuda(cudaStreamSynchronize(c->stream), "functional");
+}
+
+xcgpu_status xcgpu_add_scalar(xcgpu_plan* P, double thr, int nspin, const double* v, const double* g, double* F,
+                              int mem) {
+  if (!P) return XCGPU_ERR_INVALID;
+  Ctx* c = P->ctx;
+  if ((nspin != 1 && nspin != 2) || !v || !F) return c->fail(XCGPU_ERR_INVALID, "add_scalar: bad arguments");
+  cudaSetDevice(c->device);
+  const long n = P->grid->n;
+  const int nbf = P->basis->nbf;
+  Chunks ch;
+  DevBuf d_slab, dv, dg, dF, skip;
+  XC_TRY(prep_chunks(P, ch, d_slab));
+  const double *vd = nullptr, *gd = nullptr;
+  XC_TRY(to_device(c, dv, v, (size_t)nspin * n, mem, &vd));
+  if (g) XC_TRY(to_device(c, dg, g, (size_t)nspin * 3 * n, mem, &gd));
+  double* Fd = F;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(upload(c, dF, F, (size_t)nspin * nbf * nbf));
+    Fd = dF.as<double>();
+  }
+  XC_TRY(stage_adder(P, ch, d_slab, nspin, vd, gd, thr, skip, Fd));
+  if (mem == XCGPU_MEM_HOST)
+    XC_TRY(c->cuda(cudaMemcpyAsync(F, Fd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                   "F"));
+  return c->cuda(cudaStreamSynchronize(c->stream), "add_scalar");
+}
+
+xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double thr, const double* Pm, double* V,
+                       double* Exc, double* Nel, int mem) {
+  if (!P) return XCGPU_ERR_INVALID;
+  Ctx* c = P->ctx;
+  if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "unknown functional");
+  if ((nspin != 1 && nspin != 2) || !Pm || !V) return c->fail(XCGPU_ERR_INVALID, "vxc: bad arguments");
+  if (precision != XCGPU_PREC_FP64)
+    return c->fail(XCGPU_ERR_UNSUPPORTED, "vxc: requested precision is not available in this build");
+  cudaSetDevice(c->device);
+  const bool gga = xc::is_gga(func);
+  const long n = P->grid->n;
+  const int nbf = P->basis->nbf;
+  Chunks ch;
+  DevBuf d_slab, dPm, dV, rho, grad, epuv, dfdrho, dfdgrad, partials, sums, skip;
+  XC_TRY(prep_chunks(P, ch, d_slab));
+  const double* Pd = nullptr;
+  XC_TRY(to_device(c, dPm, Pm, (size_t)nspin * nbf * nbf, mem, &Pd));
+  double* Vd = V;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(dV.alloc(c, (size_t)nspin * nbf * nbf * sizeof(double)));
+    Vd = dV.as<double>();
+  }
+  XC_TRY(rho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  XC_TRY(epuv.alloc(c, (size_t)n * sizeof(double)));
+  XC_TRY(dfdrho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  if (gga) {
+    XC_TRY(grad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+    XC_TRY(dfdgrad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+  }
+  const long nparts_max = (n + 127) / 128;
+  XC_TRY(partials.alloc(c, 2 * nparts_max * sizeof(double) + 16));
+  XC_TRY(sums.alloc(c, 2 * sizeof(double)));
+  // 1. rho, grad rho
+  XC_TRY(stage_density(P, ch, d_slab, nspin, Pd, rho.as<double>(), gga ? grad.as<double>() : nullptr));
+  // 2. functional + grid sums
+  int nparts = 0;
+  XC_TRY(launch_functional(c, func, nspin, n, kSkipBlock, rho.as<double>(), gga ? grad.as<double>() : nullptr,
+                           epuv.as<double>(), dfdrho.as<double>(), gga ? dfdgrad.as<double>() : nullptr,
+                           P->dev.w, partials.as<double>(), &nparts));
+  if (nparts) XC_TRY(launch_sum_partials(c, partials.as<double>(), nparts, 2, sums.as<double>()));
+  else XC_TRY(c->cuda(cudaMemsetAsync(sums.p, 0, 2 * sizeof(double), c->stream), "memset sums"));
+  // 3. Vxc
+  XC_TRY(c->cuda(cudaMemsetAsync(Vd, 0, (size_t)nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
+  XC_TRY(stage_adder(P, ch, d_slab, nspin, dfdrho.as<double>(), gga ? dfdgrad.as<double>() : nullptr, thr, skip, Vd));
+  double hs[2] = {0, 0};
+  XC_TRY(c->cuda(cudaMemcpyAsync(hs, sums.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "sums"));
+  if (mem == XCGPU_MEM_HOST)
+    XC_TRY(c->cuda(cudaMemcpyAsync(V, Vd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                   "V"));
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "vxc"));
+  if (Exc) *Exc = hs[0];
+  if (Nel) *Nel = hs[1];
+  return XCGPU_OK;
+}
+
+}  // extern "C"

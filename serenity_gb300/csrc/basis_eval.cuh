@@ -1,0 +1,155 @@
+// Contracted Gaussian shells on a grid point: radial part, Cartesian monomials and
+// the transform to real solid harmonics, with gradients (and Hessians).
+//
+// Follows BasisFunctionOnGridController.cpp:259-1097: per point and shell the
+// radial sum R = sum_i c_i exp(-a_i r^2) skips primitives with a_i r^2 beyond
+// -ln(threshold) (:298-307); if |R| < threshold every function of the shell is
+// zero at this point (:312-329); Cartesian functions run (l,0,0) ... (0,0,l)
+// (:359-362); spherical ones are real solid harmonics m = -l..l (:455-1062);
+// gradients use R' = -2 sum a c exp(.) (:1068-1080).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace xcgpu {
+
+__host__ __device__ __forceinline__ int ncart_d(int l) { return (l + 1) * (l + 2) / 2; }
+
+template <class R> __device__ __forceinline__ R dexp(R x);
+template <> __device__ __forceinline__ double dexp<double>(double x) { return exp(x); }
+template <> __device__ __forceinline__ float dexp<float>(float x) { return __expf(x); }
+
+// radial part of shell s at squared distance r2; returns false if negligible
+template <class R, int DERIV>
+__device__ __forceinline__ bool shell_radial(const double* __restrict__ alpha, const double* __restrict__ coef, int np,
+                                             R r2, R expthr, R thr, R& Rv, R& dR, R& ddR) {
+  Rv = R(0);
+  dR = R(0);
+  ddR = R(0);
+  for (int i = 0; i < np; ++i) {
+    const R a = (R)__ldg(alpha + i);
+    const R t = a * r2;
+    if (t < expthr) {
+      const R e = (R)__ldg(coef + i) * dexp<R>(-t);
+      Rv += e;
+      if (DERIV >= 1) dR -= R(2) * a * e;
+      if (DERIV >= 2) ddR += R(4) * a * a * e;
+    }
+  }
+  return fabs(Rv) >= thr;
+}
+
+// Emit(f, value, gx, gy, gz, h) for the nfunc functions of an l = L shell.
+// T: solid-harmonic matrix (2L+1) x ncart(L) (pure) ; cn: Cartesian factors (ncart(L)).
+template <class R, int L, int DERIV, class Emit>
+__device__ __forceinline__ void shell_functions(R x, R y, R z, R Rv, R dR, R ddR, bool pure,
+                                                const double* __restrict__ T, const double* __restrict__ cn,
+                                                Emit&& emit) {
+  constexpr int NC = (L + 1) * (L + 2) / 2;
+  constexpr int NS = 2 * L + 1;
+  R px[L + 3], py[L + 3], pz[L + 3];
+  px[0] = py[0] = pz[0] = R(1);
+#pragma unroll
+  for (int k = 1; k < L + 3; ++k) {
+    px[k] = px[k - 1] * x;
+    py[k] = py[k - 1] * y;
+    pz[k] = pz[k - 1] * z;
+  }
+  R sv[NS], sg[DERIV >= 1 ? 3 * NS : 1], sh[DERIV >= 2 ? 6 * NS : 1];
+  if (pure) {
+#pragma unroll
+    for (int m = 0; m < NS; ++m) {
+      sv[m] = R(0);
+      if (DERIV >= 1) sg[3 * m] = sg[3 * m + 1] = sg[3 * m + 2] = R(0);
+      if (DERIV >= 2)
+#pragma unroll
+        for (int h = 0; h < 6; ++h) sh[6 * m + h] = R(0);
+    }
+  }
+  int k = 0;
+#pragma unroll
+  for (int a = L; a >= 0; --a) {
+#pragma unroll
+    for (int b = L - a; b >= 0; --b, ++k) {
+      const int c = L - a - b;
+      const R mono = px[a] * py[b] * pz[c];
+      const R v = mono * Rv;
+      R g[3] = {R(0), R(0), R(0)};
+      R hh[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
+      if (DERIV >= 1) {
+        const R dmx = a > 0 ? R(a) * px[a > 0 ? a - 1 : 0] * py[b] * pz[c] : R(0);
+        const R dmy = b > 0 ? R(b) * px[a] * py[b > 0 ? b - 1 : 0] * pz[c] : R(0);
+        const R dmz = c > 0 ? R(c) * px[a] * py[b] * pz[c > 0 ? c - 1 : 0] : R(0);
+        g[0] = dmx * Rv + mono * dR * x;
+        g[1] = dmy * Rv + mono * dR * y;
+        g[2] = dmz * Rv + mono * dR * z;
+        if (DERIV >= 2) {
+          const R r[3] = {x, y, z};
+          const R dm[3] = {dmx, dmy, dmz};
+          const int e[3] = {a, b, c};
+          const int hi[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+#pragma unroll
+          for (int q = 0; q < 6; ++q) {
+            const int i = hi[q][0], j = hi[q][1];
+            int f[3] = {e[0], e[1], e[2]};
+            R coefm = R(f[i]);
+            f[i] -= 1;
+            coefm *= R(f[j]);
+            f[j] -= 1;
+            R d2 = R(0);
+            if (f[0] >= 0 && f[1] >= 0 && f[2] >= 0 && coefm != R(0)) d2 = coefm * px[f[0]] * py[f[1]] * pz[f[2]];
+            hh[q] = d2 * Rv + dm[i] * dR * r[j] + dm[j] * dR * r[i] + mono * (ddR * r[i] * r[j] + (i == j ? dR : R(0)));
+          }
+        }
+      }
+      if (pure) {
+#pragma unroll
+        for (int m = 0; m < NS; ++m) {
+          const R t = (R)__ldg(T + m * NC + k);
+          sv[m] += t * v;
+          if (DERIV >= 1) {
+            sg[3 * m] += t * g[0];
+            sg[3 * m + 1] += t * g[1];
+            sg[3 * m + 2] += t * g[2];
+          }
+          if (DERIV >= 2)
+#pragma unroll
+            for (int q = 0; q < 6; ++q) sh[6 * m + q] += t * hh[q];
+        }
+      } else {
+        const R t = (R)__ldg(cn + k);
+        R ht[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) ht[q] = t * hh[q];
+        emit(k, t * v, t * g[0], t * g[1], t * g[2], ht);
+      }
+    }
+  }
+  if (pure) {
+#pragma unroll
+    for (int m = 0; m < NS; ++m) {
+      R ht[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) ht[q] = DERIV >= 2 ? sh[6 * m + q] : R(0);
+      emit(m, sv[m], DERIV >= 1 ? sg[3 * m] : R(0), DERIV >= 1 ? sg[3 * m + 1] : R(0),
+           DERIV >= 1 ? sg[3 * m + 2] : R(0), ht);
+    }
+  }
+}
+
+// dispatch on l at run time
+template <class R, int DERIV, class Emit>
+__device__ __forceinline__ void shell_functions_l(int l, R x, R y, R z, R Rv, R dR, R ddR, bool pure,
+                                                  const double* T, const double* cn, Emit&& emit) {
+  switch (l) {
+    case 0: shell_functions<R, 0, DERIV>(x, y, z, Rv, dR, ddR, pure, T, cn, emit); break;
+    case 1: shell_functions<R, 1, DERIV>(x, y, z, Rv, dR, ddR, pure, T, cn, emit); break;
+    case 2: shell_functions<R, 2, DERIV>(x, y, z, Rv, dR, ddR, pure, T, cn, emit); break;
+    case 3: shell_functions<R, 3, DERIV>(x, y, z, Rv, dR, ddR, pure, T, cn, emit); break;
+    case 4: shell_functions<R, 4, DERIV>(x, y, z, Rv, dR, ddR, pure, T, cn, emit); break;
+    case 5: shell_functions<R, 5, DERIV>(x, y, z, Rv, dR, ddR, pure, T, cn, emit); break;
+    case 6: shell_functions<R, 6, DERIV>(x, y, z, Rv, dR, ddR, pure, T, cn, emit); break;
+    default: break;
+  }
+}
+
+}  // namespace xcgpu

@@ -1,0 +1,189 @@
+// Internal declarations of the xcgpu library (GB300 / sm_103a XC integration).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/xcgpu.h"
+
+namespace xcgpu {
+
+constexpr int kMaxL = 6;              // AM_MAX (Constants.h:31)
+constexpr int kBlockPoints = 128;     // points per block handled by one CTA
+constexpr int kSkipBlock = 128;       // FunctionalLibrary(128) block (FuncPotential.cpp:86)
+constexpr double kDensTiny = 1e-14;   // point cut-off of the functional
+
+inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+// Device-side basis description (struct of arrays, all device pointers).
+struct DevBasis {
+  int nshell = 0, nbf = 0, maxl = 0;
+  const int* l = nullptr;          // [nshell]
+  const int* pure = nullptr;       // [nshell]
+  const int* nprim = nullptr;      // [nshell]
+  const int* prim_off = nullptr;   // [nshell]
+  const int* first = nullptr;      // [nshell] first function index
+  const double* center = nullptr;  // [3*nshell]
+  const double* alpha = nullptr;   // [nprim total]
+  const double* coef = nullptr;    // [nprim total] normalised
+  const double* trans = nullptr;   // transform tables: per l, (2l+1) x ncart(l) solid harmonics
+  const double* cnorm = nullptr;   // per l, ncart(l) Cartesian factors
+  const int* trans_off = nullptr;  // [kMaxL+1] offsets into trans
+  const int* cnorm_off = nullptr;  // [kMaxL+1] offsets into cnorm
+};
+
+// Device-side block table of a plan.
+struct DevPlan {
+  int nblocks = 0, max_block = 0, nbf = 0;
+  long npoints = 0;
+  const double* xyz = nullptr;     // [3*npoints]
+  const double* w = nullptr;       // [npoints]
+  const int* sh_off = nullptr;     // [nblocks+1] active shells of block b: sh_list[sh_off[b] .. sh_off[b+1])
+  const int* sh_list = nullptr;
+  const int* fn_off = nullptr;     // [nblocks+1] active functions of block b
+  const int* fn_list = nullptr;
+  double radial_threshold = 1e-9, exponent_threshold = 0.0;
+};
+
+struct Ctx;
+
+// Simple owning device buffer that books its size against the context budget.
+struct DevBuf {
+  Ctx* ctx = nullptr;
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf();
+  xcgpu_status alloc(Ctx* c, size_t n);  // no-op if already >= n
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+enum KernelClass { kEval = 0, kDensity = 1, kFunctional = 2, kAdder = 3, kOther = 4, kClasses = 5 };
+
+struct Ctx {
+  int device = 0;
+  // per-kernel timing (xcgpu_set_timing)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+  double t_ms[kClasses] = {0, 0, 0, 0, 0};
+  uint64_t t_count[kClasses] = {0, 0, 0, 0, 0};
+  cudaEvent_t take_event() {
+    if (ev_pool.empty()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = ev_pool.back();
+    ev_pool.pop_back();
+    return e;
+  }
+  uint64_t budget = 0, in_use = 0, scratch_cap = 0;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  uint64_t launches = 0;
+  std::string err;
+  int sm_count = 0;
+  // reusable scratch
+  DevBuf scratch, scratch2, partials, skip;
+  xcgpu_status fail(xcgpu_status s, const std::string& msg) {
+    err = msg;
+    return s;
+  }
+  xcgpu_status cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return XCGPU_OK;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return XCGPU_ERR_CUDA;
+  }
+  xcgpu_status check_launch(const char* what) {
+    ++launches;
+    return cuda(cudaGetLastError(), what);
+  }
+};
+
+// Brackets the kernel launches of one class with events when timing is enabled.
+struct KernelTimer {
+  Ctx* c;
+  int cls;
+  cudaEvent_t a = nullptr;
+  KernelTimer(Ctx* ctx, int k) : c(ctx), cls(k) {
+    if (c->timing) {
+      a = c->take_event();
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~KernelTimer() {
+    if (c->timing) {
+      cudaEvent_t b = c->take_event();
+      cudaEventRecord(b, c->stream);
+      c->ev_pending.push_back({cls, {a, b}});
+    }
+  }
+};
+
+}  // namespace xcgpu
+
+struct xcgpu_ctx : xcgpu::Ctx {};
+
+struct xcgpu_grid {
+  xcgpu::Ctx* ctx = nullptr;
+  long n = 0;
+  xcgpu::DevBuf xyz, w;
+};
+
+struct xcgpu_basis {
+  xcgpu::Ctx* ctx = nullptr;
+  int nshell = 0, nbf = 0, maxl = 0;
+  std::vector<int> l, pure, nprim, prim_off, first;
+  std::vector<double> center, alpha, coef;
+  xcgpu::DevBuf d_l, d_pure, d_nprim, d_prim_off, d_first, d_center, d_alpha, d_coef, d_trans, d_cnorm, d_toff, d_coff;
+  xcgpu::DevBasis dev;
+};
+
+struct xcgpu_plan {
+  xcgpu::Ctx* ctx = nullptr;
+  xcgpu_grid* grid = nullptr;
+  xcgpu_basis* basis = nullptr;
+  int max_block = 128, nblocks = 0;
+  double radial_threshold = 1e-9;
+  std::vector<int> sh_off, sh_list, fn_off, fn_list;  // host copies
+  int max_active = 0;
+  double flops = 0.0;
+  xcgpu::DevBuf d_sh_off, d_sh_list, d_fn_off, d_fn_list;
+  // adder tile work list (block, tile_i, tile_j) for 64-wide tiles, upper triangle
+  std::vector<int> work;  // 3 ints per item, sorted by block
+  std::vector<long> work_off;  // [nblocks+1]
+  xcgpu::DevBuf d_work;
+  xcgpu::DevPlan dev;
+};
+
+namespace xcgpu {
+
+// host helpers implemented in the .cu files
+std::vector<double> solid_harmonic_matrix(int l);
+std::vector<double> cartesian_norms(int l);
+
+// kernels (launchers); all return a status and record errors on ctx
+xcgpu_status launch_screen(Ctx* c, const DevBasis& B, const double* xyz, long npoints, int max_block, int nblocks,
+                           double thr, unsigned char* flags /*nblocks*nshell*/, int* nfn /*nblocks*/);
+xcgpu_status launch_block_values(Ctx* c, const DevBasis& B, const DevPlan& P, int block, int deriv, double* out,
+                                 int ld /*npts per function*/);
+xcgpu_status fp64_eval_chunk(Ctx* c, const DevBasis& B, const DevPlan& P, int b0, int b1, const long* slab_off,
+                             double* scratch, int deriv);
+xcgpu_status fp64_density_chunk(Ctx* c, const DevPlan& P, int b0, int b1, const long* slab_off, const double* scratch,
+                                int nspin, const double* Pm, double* rho, double* grad);
+xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_block, const double* rho,
+                               const double* grad, double* epuv, double* dfdrho, double* dfdgrad, const double* w,
+                               double* partials /*2*nparts or null*/, int* nparts);
+xcgpu_status launch_block_skip_flags(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
+                                     double thr, unsigned char* skip /*nspin*nblocks*/);
+xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0, long w1, int chunk_b0,
+                              const long* slab_off, const double* scratch, int nspin, const double* v,
+                              const double* g, const unsigned char* skip, double* F);
+xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out /*device*/);
+
+}  // namespace xcgpu

@@ -1,0 +1,330 @@
+"""Python binding of the xcgpu C ABI (``include/xcgpu.h``) through ctypes.
+
+The GPU library is the only implementation: if ``libxcgpu.so`` cannot be loaded,
+or no CUDA device is present, every constructor raises.  There is no CPU
+fallback.  Array arguments are numpy arrays (host memory, ``XCGPU_MEM_HOST``) or
+any object exposing ``data_ptr()`` on the GPU (``XCGPU_MEM_DEVICE``, e.g. a torch
+CUDA tensor).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+MEM_HOST, MEM_DEVICE = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+FUNC = {"LDA": 1, "PBE": 2, "BLYP": 3, "SLATER": 16, "VWN5": 17, "PBEX": 18, "PBEC": 19, "B88": 20, "LYP": 21,
+        "PW92": 22}
+STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NO_MEMORY", 4: "BUDGET", 5: "UNSUPPORTED", 6: "TIMEOUT", 7: "IO"}
+
+
+class XcgpuError(RuntimeError):
+    """Raised for a non-OK status (the reference throws SerenityError at this boundary)."""
+
+    def __init__(self, status, message):
+        super().__init__("xcgpu %s: %s" % (STATUS.get(status, status), message))
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget", ctypes.c_uint64), ("scratch_bytes", ctypes.c_uint64)]
+
+
+class Shell(ctypes.Structure):
+    _fields_ = [("l", ctypes.c_int32), ("pure", ctypes.c_int32), ("nprim", ctypes.c_int32),
+                ("center", ctypes.c_double * 3), ("alpha", ctypes.POINTER(ctypes.c_double)),
+                ("coef", ctypes.POINTER(ctypes.c_double))]
+
+
+class PlanStats(ctypes.Structure):
+    _fields_ = [("nblocks", ctypes.c_uint32), ("max_block", ctypes.c_uint32), ("nbf", ctypes.c_uint32),
+                ("max_active", ctypes.c_uint32), ("npoints", ctypes.c_uint64), ("sum_active", ctypes.c_uint64),
+                ("flops_per_spin", ctypes.c_double)]
+
+
+_lib = None
+vp = ctypes.c_void_p
+dp = ctypes.POINTER(ctypes.c_double)
+
+
+def library(build_if_needed=True):
+    """Load libxcgpu.so (building it first if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_needed:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise XcgpuError(2, "libxcgpu.so not built (%s)" % _build.LIB)
+    L = ctypes.CDLL(_build.LIB)
+    S = ctypes.c_int
+    L.xcgpu_ctx_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
+    L.xcgpu_ctx_destroy.argtypes = [vp]
+    L.xcgpu_last_error.argtypes = [vp]
+    L.xcgpu_last_error.restype = ctypes.c_char_p
+    L.xcgpu_set_stream.argtypes = [vp, vp]
+    L.xcgpu_synchronize.argtypes = [vp]
+    L.xcgpu_bytes_in_use.argtypes = [vp]
+    L.xcgpu_bytes_in_use.restype = ctypes.c_uint64
+    L.xcgpu_kernel_launches.argtypes = [vp]
+    L.xcgpu_kernel_launches.restype = ctypes.c_uint64
+    L.xcgpu_grid_create.argtypes = [vp, vp, vp, ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.xcgpu_grid_build.argtypes = [vp, S, vp, vp, S, S, S, ctypes.c_double, S, S, ctypes.c_char_p, ctypes.POINTER(vp)]
+    L.xcgpu_grid_npoints.argtypes = [vp]
+    L.xcgpu_grid_npoints.restype = ctypes.c_uint64
+    L.xcgpu_grid_copy.argtypes = [vp, vp, vp]
+    L.xcgpu_grid_destroy.argtypes = [vp]
+    L.xcgpu_basis_create.argtypes = [vp, ctypes.POINTER(Shell), ctypes.c_uint32, ctypes.POINTER(vp)]
+    L.xcgpu_basis_nbf.argtypes = [vp]
+    L.xcgpu_basis_nbf.restype = ctypes.c_uint32
+    L.xcgpu_basis_coefs.argtypes = [vp, ctypes.c_uint32, vp]
+    L.xcgpu_basis_destroy.argtypes = [vp]
+    L.xcgpu_plan_create.argtypes = [vp, vp, vp, ctypes.c_uint32, ctypes.c_double, ctypes.POINTER(vp)]
+    L.xcgpu_plan_get_stats.argtypes = [vp, ctypes.POINTER(PlanStats)]
+    L.xcgpu_block_on_grid.argtypes = [vp, ctypes.c_uint32, S, vp, vp, vp, vp]
+    L.xcgpu_block_active.argtypes = [vp, ctypes.c_uint32, vp]
+    L.xcgpu_block_active.restype = ctypes.c_int32
+    L.xcgpu_plan_destroy.argtypes = [vp]
+    L.xcgpu_density.argtypes = [vp, S, vp, vp, vp, S]
+    L.xcgpu_functional.argtypes = [vp, S, S, ctypes.c_uint64, ctypes.c_uint32, vp, vp, vp, vp, vp, S]
+    L.xcgpu_functional_is_gga.argtypes = [S]
+    L.xcgpu_add_scalar.argtypes = [vp, ctypes.c_double, S, vp, vp, vp, S]
+    L.xcgpu_vxc.argtypes = [vp, S, S, S, ctypes.c_double, vp, vp, dp, dp, S]
+    for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
+                 "xcgpu_grid_copy", "xcgpu_basis_create", "xcgpu_basis_coefs", "xcgpu_plan_create",
+                 "xcgpu_plan_get_stats", "xcgpu_block_on_grid", "xcgpu_density", "xcgpu_functional",
+                 "xcgpu_add_scalar", "xcgpu_vxc"]:
+        getattr(L, name).restype = S
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _mem(a):
+    return MEM_DEVICE if hasattr(a, "data_ptr") else MEM_HOST
+
+
+def _f64(a):
+    if hasattr(a, "data_ptr"):
+        return a
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """One GPU, one stream, an HBM budget (bytes; 0 = 90% of free memory)."""
+
+    def __init__(self, device=0, hbm_budget=0, scratch_bytes=0):
+        L = library()
+        h = vp()
+        cfg = Config(device, hbm_budget, scratch_bytes)
+        st = L.xcgpu_ctx_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != 0:
+            raise XcgpuError(st, "cannot create a context on CUDA device %d (is a GPU present?)" % device)
+        self.h = h
+        self.L = L
+
+    def check(self, st):
+        if st != 0:
+            raise XcgpuError(st, self.L.xcgpu_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.xcgpu_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        self.check(self.L.xcgpu_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def synchronize(self):
+        self.check(self.L.xcgpu_synchronize(self.h))
+
+    @property
+    def bytes_in_use(self):
+        return int(self.L.xcgpu_bytes_in_use(self.h))
+
+    @property
+    def kernel_launches(self):
+        return int(self.L.xcgpu_kernel_launches(self.h))
+
+    def functional(self, func, rho, grad=None, skip_block=128):
+        """FunctionalLibrary::calcData(GRADIENTS, ., order 1) on host arrays
+        rho [nspin, n], grad [nspin, 3, n] -> (epuv, dfdrho, dfdgrad)."""
+        fid = FUNC[func] if isinstance(func, str) else int(func)
+        rho = _f64(rho)
+        nspin, n = rho.shape
+        gga = bool(self.L.xcgpu_functional_is_gga(fid))
+        g = _f64(grad) if gga else None
+        epuv = np.zeros(n)
+        dr = np.zeros((nspin, n))
+        dg = np.zeros((nspin, 3, n)) if gga else None
+        self.check(self.L.xcgpu_functional(self.h, fid, nspin, n, skip_block, _ptr(rho), _ptr(g), _ptr(epuv), _ptr(dr),
+                                           _ptr(dg), MEM_HOST))
+        return epuv, dr, dg
+
+
+class Grid:
+    def __init__(self, ctx, xyz=None, w=None, handle=None):
+        self.ctx = ctx
+        if handle is None:
+            xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+            w = np.ascontiguousarray(w, dtype=np.float64)
+            h = vp()
+            ctx.check(ctx.L.xcgpu_grid_create(ctx.h, _ptr(xyz), _ptr(w), w.size, ctypes.byref(h)))
+            handle = h
+        self.h = handle
+        self.n = int(ctx.L.xcgpu_grid_npoints(self.h))
+
+    @staticmethod
+    def build(ctx, Z, xyz_bohr, n_rad=0, n_ang=0, accuracy=0, weight_threshold=1e-14, smoothing=3, sort=True,
+              lebedev_table=None):
+        from .basis import LEBEDEV_TABLE
+        Z = np.ascontiguousarray(Z, dtype=np.int32)
+        xyz = np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1)
+        h = vp()
+        ctx.check(ctx.L.xcgpu_grid_build(ctx.h, len(Z), _ptr(Z), _ptr(xyz), n_rad, n_ang, accuracy, weight_threshold,
+                                         smoothing, int(sort), (lebedev_table or LEBEDEV_TABLE).encode(),
+                                         ctypes.byref(h)))
+        return Grid(ctx, handle=h)
+
+    def points(self):
+        xyz = np.zeros(3 * self.n)
+        w = np.zeros(self.n)
+        self.ctx.check(self.ctx.L.xcgpu_grid_copy(self.h, _ptr(xyz), _ptr(w)))
+        return xyz.reshape(-1, 3), w
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx.L.xcgpu_grid_destroy(self.h)
+            self.h = None
+
+
+class Basis:
+    def __init__(self, ctx, shells):
+        self.ctx = ctx
+        self.shells = shells
+        arr = (Shell * shells.nshell)()
+        self._keep = []
+        off = 0
+        for i in range(shells.nshell):
+            n = int(shells.nprim[i])
+            a = np.ascontiguousarray(shells.alpha[off:off + n])
+            c = np.ascontiguousarray(shells.coef[off:off + n])
+            self._keep += [a, c]
+            arr[i].l = int(shells.l[i])
+            arr[i].pure = int(shells.pure[i])
+            arr[i].nprim = n
+            for k in range(3):
+                arr[i].center[k] = float(shells.centers[3 * i + k])
+            arr[i].alpha = a.ctypes.data_as(dp)
+            arr[i].coef = c.ctypes.data_as(dp)
+            off += n
+        h = vp()
+        ctx.check(ctx.L.xcgpu_basis_create(ctx.h, arr, shells.nshell, ctypes.byref(h)))
+        self.h = h
+        self.nbf = int(ctx.L.xcgpu_basis_nbf(h))
+
+    def coefs(self, s):
+        out = np.zeros(int(self.shells.nprim[s]))
+        self.ctx.check(self.ctx.L.xcgpu_basis_coefs(self.h, s, _ptr(out)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx.L.xcgpu_basis_destroy(self.h)
+            self.h = None
+
+
+class Plan:
+    """BasisFunctionOnGridController: blocks of max_block points, per-block screening."""
+
+    def __init__(self, ctx, grid, basis, max_block=128, radial_threshold=1e-9):
+        self.ctx, self.grid, self.basis = ctx, grid, basis
+        h = vp()
+        ctx.check(ctx.L.xcgpu_plan_create(ctx.h, grid.h, basis.h, max_block, radial_threshold, ctypes.byref(h)))
+        self.h = h
+        self.max_block = max_block
+        self.nbf = basis.nbf
+
+    def stats(self):
+        s = PlanStats()
+        self.ctx.check(self.ctx.L.xcgpu_plan_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in PlanStats._fields_}
+
+    def block_on_grid(self, block, deriv=1):
+        n = min(self.max_block, self.grid.n - block * self.max_block)
+        v = np.zeros(n * self.nbf)
+        g = np.zeros(3 * n * self.nbf) if deriv >= 1 else None
+        hh = np.zeros(6 * n * self.nbf) if deriv >= 2 else None
+        neg = np.zeros(self.nbf, dtype=np.int32)
+        self.ctx.check(self.ctx.L.xcgpu_block_on_grid(self.h, block, deriv, _ptr(v), _ptr(g), _ptr(hh), _ptr(neg)))
+        out = {"values": v.reshape(self.nbf, n).T, "negligible": neg}
+        if deriv >= 1:
+            out["grad"] = g.reshape(3, self.nbf, n).transpose(0, 2, 1)
+        if deriv >= 2:
+            out["hess"] = hh.reshape(6, self.nbf, n).transpose(0, 2, 1)
+        return out
+
+    def active(self, block):
+        n = self.ctx.L.xcgpu_block_active(self.h, block, None)
+        idx = np.zeros(max(n, 1), dtype=np.int32)
+        self.ctx.L.xcgpu_block_active(self.h, block, _ptr(idx))
+        return idx[:n]
+
+    def density(self, P, grad=True):
+        """rho [nspin, n], grad [nspin, 3, n] for P [nbf, nbf] or [nspin, nbf, nbf] (symmetric)."""
+        P = np.asarray(P, dtype=np.float64)
+        nspin = 1 if P.ndim == 2 else P.shape[0]
+        Pc = np.ascontiguousarray(np.stack([m.T for m in P.reshape(nspin, self.nbf, self.nbf)]))
+        rho = np.zeros((nspin, self.grid.n))
+        g = np.zeros((nspin, 3, self.grid.n)) if grad else None
+        self.ctx.check(self.ctx.L.xcgpu_density(self.h, nspin, _ptr(Pc), _ptr(rho), _ptr(g), MEM_HOST))
+        return rho, g
+
+    def add_scalar(self, v, g=None, F=None, block_ave_threshold=1e-11):
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        nspin = v.size // self.grid.n
+        gg = None if g is None else np.ascontiguousarray(g, dtype=np.float64).reshape(-1)
+        Fc = np.zeros((nspin, self.nbf, self.nbf)) if F is None else np.ascontiguousarray(
+            np.stack([m.T for m in np.asarray(F, dtype=np.float64).reshape(nspin, self.nbf, self.nbf)]))
+        self.ctx.check(self.ctx.L.xcgpu_add_scalar(self.h, block_ave_threshold, nspin, _ptr(v), _ptr(gg), _ptr(Fc),
+                                                   MEM_HOST))
+        return Fc.transpose(0, 2, 1)
+
+    def vxc(self, func, P, precision=PREC_FP64, block_ave_threshold=1e-11, out=None):
+        """Whole build; P host array [nbf,nbf] / [nspin,nbf,nbf] or a device tensor
+        (column-major per spin).  Returns (V, Exc, Nel)."""
+        fid = FUNC[func] if isinstance(func, str) else int(func)
+        exc, nel = ctypes.c_double(), ctypes.c_double()
+        if hasattr(P, "data_ptr"):
+            nspin = P.numel() // (self.nbf * self.nbf)
+            V = out
+            self.ctx.check(self.ctx.L.xcgpu_vxc(self.h, fid, nspin, precision, block_ave_threshold, _ptr(P), _ptr(V),
+                                                ctypes.byref(exc), ctypes.byref(nel), MEM_DEVICE))
+            return V, exc.value, nel.value
+        P = np.asarray(P, dtype=np.float64)
+        nspin = 1 if P.ndim == 2 else P.shape[0]
+        Pc = np.ascontiguousarray(np.stack([m.T for m in P.reshape(nspin, self.nbf, self.nbf)]))
+        V = np.zeros((nspin, self.nbf, self.nbf))
+        self.ctx.check(self.ctx.L.xcgpu_vxc(self.h, fid, nspin, precision, block_ave_threshold, _ptr(Pc), _ptr(V),
+                                            ctypes.byref(exc), ctypes.byref(nel), MEM_HOST))
+        return V.transpose(0, 2, 1), exc.value, nel.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx.L.xcgpu_plan_destroy(self.h)
+            self.h = None

@@ -1,0 +1,174 @@
+"""GPU parity: the xcgpu C ABI (FP64 drop-in precision) against the reference's
+golden vectors and against the oracle on the same inputs.
+
+Tolerances: the reference's own where a golden vector exists (1e-8 basis values,
+5e-8 density, 1e-8 adder, 1e-6 Fock matrix); 1e-10 absolute / 1e-12 relative
+against the oracle (FP64 on both sides, different summation orders)."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from serenity_gb300 import workload as wl
+from serenity_gb300.basis import ANGSTROM_TO_BOHR, Shells, atomic_number
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from serenity_gb300 import xcgpu
+    return xcgpu.Context()
+
+
+def _plan(ctx, shells, pts, w, max_block, thr):
+    from serenity_gb300 import xcgpu
+    g = xcgpu.Grid(ctx, pts, w)
+    b = xcgpu.Basis(ctx, shells)
+    return xcgpu.Plan(ctx, g, b, max_block, thr)
+
+
+def test_block_on_grid_golden(ctx, golden):
+    g = golden("bf_small_mixed_tiny.json")
+    pts = np.array(g["points"])
+    P = _plan(ctx, Shells(g["shells"]), pts, np.ones(len(pts)), g["max_block_size"], g["radial_threshold"])
+    out = P.block_on_grid(0, deriv=2)
+    e, tol = g["expected"], g["tolerance"]
+    np.testing.assert_allclose(out["values"], e["values"], rtol=0, atol=tol)
+    for i, c in enumerate("xyz"):
+        np.testing.assert_allclose(out["grad"][i], e[c], rtol=0, atol=tol)
+    for i, c in enumerate(["xx", "xy", "xz", "yy", "yz", "zz"]):
+        np.testing.assert_allclose(out["hess"][i], e[c], rtol=0, atol=tol)
+    ref = po.Basis(Shells(g["shells"])).block(pts, g["radial_threshold"], deriv=2)
+    np.testing.assert_allclose(out["values"], ref["values"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(out["hess"], ref["hess"], rtol=1e-13, atol=1e-14)
+    assert (out["negligible"] == ref["negligible"]).all()
+
+
+def test_density_golden(ctx, golden):
+    d = golden("density_tiny.json")
+    pts = np.array(d["points"])
+    P = _plan(ctx, Shells(d["shells"]), pts, np.ones(len(pts)), d["max_block_size"], d["radial_threshold"])
+    rho, grad = P.density(np.array(d["P"]))
+    np.testing.assert_allclose(rho[0], d["rho"], rtol=0, atol=d["tolerance"])
+    np.testing.assert_allclose(grad[0], d["grad"], rtol=0, atol=d["tolerance"])
+
+
+def test_adder_golden(ctx, golden):
+    a = golden("adder_very_small.json")
+    pts = np.array(a["points"])
+    P = _plan(ctx, Shells(a["shells"]), pts, np.array(a["weights"]), a["max_block_size"], a["radial_threshold"])
+    F = P.add_scalar(np.array(a["potential"]), np.array(a["gradient_potential"]),
+                     block_ave_threshold=a["block_ave_threshold"])
+    np.testing.assert_allclose(F[0], a["F"], rtol=0, atol=a["tolerance"])
+
+
+def _h2(golden):
+    d = golden("funcpot_h2.json")
+    sym = [a[0] for a in d["atoms_angstrom"]]
+    xyz = np.array([a[1:] for a in d["atoms_angstrom"]]) * ANGSTROM_TO_BOHR
+    return d, sym, xyz
+
+
+def test_grid_builder_matches_oracle(ctx, golden):
+    from serenity_gb300 import xcgpu
+    d, sym, xyz = _h2(golden)
+    Z = [atomic_number(s) for s in sym]
+    gs = d["grid_settings"]
+    g = xcgpu.Grid.build(ctx, Z, xyz, accuracy=int(gs["ACCURACY"]), weight_threshold=float(gs["WEIGHTTHRESHOLD"]),
+                         smoothing=int(gs["SMOOTHING"]))
+    pts, w = g.points()
+    rp, rw = po.becke_grid(Z, xyz, accuracy=int(gs["ACCURACY"]), weight_threshold=float(gs["WEIGHTTHRESHOLD"]),
+                           smoothing=int(gs["SMOOTHING"]))
+    assert pts.shape == rp.shape
+    np.testing.assert_allclose(pts, rp, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(w, rw, rtol=1e-12, atol=1e-15)
+    # water tetramer, explicit 50 x 194 unpruned grid
+    w0 = wl.config(0)
+    g = xcgpu.Grid.build(ctx, w0.Z, w0.coords, n_rad=50, n_ang=194)
+    pts, w = g.points()
+    rp, rw = po.becke_grid(w0.Z, w0.coords, n_rad=50, n_ang=194)
+    np.testing.assert_allclose(pts, rp, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(w, rw, rtol=1e-11, atol=1e-14)
+
+
+@pytest.mark.parametrize("unrestricted", [False, True])
+def test_h2_lda_fock_matrix(ctx, golden, unrestricted):
+    from serenity_gb300 import xcgpu
+    d, sym, xyz = _h2(golden)
+    gs = d["grid_settings"]
+    g = xcgpu.Grid.build(ctx, [atomic_number(s) for s in sym], xyz, accuracy=int(gs["ACCURACY"]),
+                         weight_threshold=float(gs["WEIGHTTHRESHOLD"]), smoothing=int(gs["SMOOTHING"]))
+    b = xcgpu.Basis(ctx, Shells.for_atoms(sym, xyz, d["basis"], spherical=d["spherical"]))
+    plan = xcgpu.Plan(ctx, g, b, int(gs["BLOCKSIZE"]), float(gs["BASFUNCRADIALTHRESHOLD"]))
+    Pm = np.stack([d["Pa"], d["Pb"]]) if unrestricted else np.array(d["P"])
+    V, exc, nel = plan.vxc("LDA", Pm, block_ave_threshold=float(gs["BLOCKAVETHRESHOLD"]))
+    F = np.array(d["F"]["LDA_UNRES" if unrestricted else "LDA"])
+    for s in range(V.shape[0]):
+        np.testing.assert_allclose(V[s], F, rtol=0, atol=d["tolerance"])
+    assert abs(nel - 2.0) < 1e-5
+
+
+def _random_points(n, nspin, seed):
+    rng = np.random.default_rng(seed)
+    rho = 10.0 ** rng.uniform(-9, 2.5, size=(nspin, n))
+    if nspin == 2:
+        rho[1] *= rng.uniform(0.0, 2.0, size=n)
+    grad = rng.standard_normal((nspin, 3, n)) * rho[:, None, :] * 10.0 ** rng.uniform(-1, 1.5, size=(nspin, 1, n))
+    return rho, grad
+
+
+@pytest.mark.parametrize("func", ["SLATER", "VWN5", "PW92", "PBEX", "PBEC", "B88", "LYP", "LDA", "PBE", "BLYP"])
+@pytest.mark.parametrize("nspin", [1, 2])
+def test_functional_vs_oracle(ctx, func, nspin):
+    rho, grad = _random_points(4000, nspin, 7 + nspin)
+    e, vr, vg = ctx.functional(func, rho, grad, skip_block=0)
+    re, rvr, rvg = po.functional(func, rho, grad)
+    scale = np.abs(re).max()
+    np.testing.assert_allclose(e, re, rtol=1e-11, atol=1e-13 * scale)
+    np.testing.assert_allclose(vr, rvr, rtol=1e-10, atol=1e-13 * np.abs(rvr).max())
+    if rvg is not None:
+        np.testing.assert_allclose(vg, rvg, rtol=1e-9, atol=1e-12 * np.abs(rvg).max())
+
+
+def _small_case(func, unrestricted, seed=3):
+    sym, xyz = wl.water_cluster(4, seed, jitter=0.2, dims=(2, 2, 1))
+    w = wl.Workload(sym, xyz, "DEF2-SVP", func, (20, 19) if unrestricted else 20, 30, 110, seed)
+    pts, wts = po.becke_grid(w.Z, w.coords, n_rad=30, n_ang=110)
+    return w, pts, wts
+
+
+@pytest.mark.parametrize("func,unrestricted", [("LDA", False), ("PBE", False), ("BLYP", False), ("PBE", True),
+                                               ("LDA", True)])
+def test_vxc_vs_oracle_water_tetramer(ctx, func, unrestricted):
+    from serenity_gb300 import xcgpu
+    w, pts, wts = _small_case(func, unrestricted)
+    P = w.density()
+    plan = _plan(ctx, w.shells, pts, wts, 128, 1e-9)
+    V, exc, nel = plan.vxc(func, P)
+    rV, rexc, rnel = po.Basis(w.shells).vxc(pts, wts, func, P)
+    assert abs(exc - rexc) < 1e-10 * max(1.0, abs(rexc))
+    assert abs(nel - rnel) < 1e-10 * rnel
+    np.testing.assert_allclose(V, rV, rtol=0, atol=1e-11)
+    assert plan.ctx.kernel_launches > 0
+    assert isinstance(plan, xcgpu.Plan)
+
+
+def test_stages_vs_oracle_ragged_blocks(ctx):
+    """Blocks of 37 points (ragged last block), density and adder stages separately."""
+    w, pts, wts = _small_case("PBE", False)
+    P = w.density()
+    plan = _plan(ctx, w.shells, pts, wts, 37, 1e-9)
+    ob = po.Basis(w.shells)
+    rho, grad = plan.density(P)
+    rrho, rgrad = ob.density(pts, P, max_block=37)
+    np.testing.assert_allclose(rho, rrho, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(grad, rgrad, rtol=1e-11, atol=1e-13)
+    rng = np.random.default_rng(1)
+    v = rng.standard_normal(len(wts))
+    g = rng.standard_normal((1, 3, len(wts)))
+    F = plan.add_scalar(v, g)
+    rF = ob.add_scalar(pts, wts, v, g, max_block=37)
+    np.testing.assert_allclose(F, rF, rtol=0, atol=1e-11)
+    F = plan.add_scalar(v)
+    rF = ob.add_scalar(pts, wts, v, None, max_block=37)
+    np.testing.assert_allclose(F, rF, rtol=0, atol=1e-11)
