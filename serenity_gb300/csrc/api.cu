@@ -477,70 +477,63 @@ int xcgpu_functional_is_gga(int func) { return xc::is_gga(func) ? 1 : 0; }
 /* ---- stages and the whole build ------------------------------------------------------ */
 namespace xcgpu {
 
-// Chunks of consecutive blocks whose FP64 slabs fit the scratch cap.
+// Chunks of consecutive blocks whose FP64 slabs fit the scratch cap; computed
+// once per plan (slab offsets resident on the device).
 struct Chunks {
-  std::vector<int> bounds;         // chunk k covers blocks [bounds[k], bounds[k+1])
-  std::vector<long> slab_off;      // per block, offset within its chunk (doubles)
+  std::vector<int> bounds;  // chunk k covers blocks [bounds[k], bounds[k+1])
   long max_chunk_doubles = 0;
 };
 
-static Chunks make_chunks(const xcgpu_plan* P, uint64_t cap_bytes) {
-  Chunks ch;
-  const long cap = std::max<long>((long)(cap_bytes / sizeof(double)), 4L * kBlockPoints * std::max(P->max_active, 1));
-  ch.bounds.push_back(0);
-  long cur = 0;
+static xcgpu_status prep_chunks(xcgpu_plan* P) {
+  if (P->chunks_ready) return XCGPU_OK;
+  Ctx* c = P->ctx;
+  const long cap = std::max<long>((long)(c->scratch_cap / sizeof(double)), 4L * kBlockPoints * std::max(P->max_active, 1));
+  std::vector<long> slab_off;
+  P->chunk_bounds.assign(1, 0);
+  long cur = 0, mx = 0;
   for (int b = 0; b < P->nblocks; ++b) {
     const long need = 4L * kBlockPoints * (P->fn_off[b + 1] - P->fn_off[b]);
     if (cur + need > cap && cur > 0) {
-      ch.bounds.push_back(b);
-      ch.max_chunk_doubles = std::max(ch.max_chunk_doubles, cur);
+      P->chunk_bounds.push_back(b);
+      mx = std::max(mx, cur);
       cur = 0;
     }
-    ch.slab_off.push_back(cur);
+    slab_off.push_back(cur);
     cur += need;
   }
-  ch.max_chunk_doubles = std::max(ch.max_chunk_doubles, cur);
-  ch.bounds.push_back(P->nblocks);
-  return ch;
+  P->chunk_max_doubles = std::max(mx, cur);
+  P->chunk_bounds.push_back(P->nblocks);
+  XC_TRY(upload(c, P->w_slab, slab_off.data(), slab_off.size()));
+  P->chunks_ready = true;
+  return XCGPU_OK;
 }
 
-struct PlanWork {
-  DevBuf slab_off, P, V, rho, grad, epuv, dfdrho, dfdgrad, askip, sums;
-};
-
-static xcgpu_status stage_density(xcgpu_plan* P, const Chunks& ch, DevBuf& d_slab, int nspin, const double* dP,
-                                  double* rho, double* grad) {
+static xcgpu_status stage_density(xcgpu_plan* P, int nspin, const double* dP, double* rho, double* grad) {
   Ctx* c = P->ctx;
-  XC_TRY(c->scratch.alloc(c, std::max<long>(ch.max_chunk_doubles, 1) * sizeof(double)));
-  for (size_t k = 0; k + 1 < ch.bounds.size(); ++k) {
-    const int b0 = ch.bounds[k], b1 = ch.bounds[k + 1];
-    const long* so = d_slab.as<long>() + b0;
+  XC_TRY(prep_chunks(P));
+  XC_TRY(c->scratch.alloc(c, std::max<long>(P->chunk_max_doubles, 1) * sizeof(double)));
+  for (size_t k = 0; k + 1 < P->chunk_bounds.size(); ++k) {
+    const int b0 = P->chunk_bounds[k], b1 = P->chunk_bounds[k + 1];
+    const long* so = P->w_slab.as<long>() + b0;
     XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, c->scratch.as<double>(), 1));
     XC_TRY(fp64_density_chunk(c, P->dev, b0, b1, so, c->scratch.as<double>(), nspin, dP, rho, grad));
   }
   return XCGPU_OK;
 }
 
-static xcgpu_status stage_adder(xcgpu_plan* P, const Chunks& ch, DevBuf& d_slab, int nspin, const double* v,
-                                const double* g, double thr, DevBuf& skip, double* F) {
+static xcgpu_status stage_adder(xcgpu_plan* P, int nspin, const double* v, const double* g, double thr, double* F) {
   Ctx* c = P->ctx;
-  XC_TRY(skip.alloc(c, (size_t)nspin * P->nblocks + 1));
-  XC_TRY(launch_block_skip_flags(c, P->dev, nspin, v, g, thr, skip.as<unsigned char>()));
-  XC_TRY(c->scratch.alloc(c, std::max<long>(ch.max_chunk_doubles, 1) * sizeof(double)));
-  for (size_t k = 0; k + 1 < ch.bounds.size(); ++k) {
-    const int b0 = ch.bounds[k], b1 = ch.bounds[k + 1];
-    const long* so = d_slab.as<long>() + b0;
+  XC_TRY(prep_chunks(P));
+  XC_TRY(P->w_skip.alloc(c, (size_t)nspin * P->nblocks + 1));
+  XC_TRY(launch_block_skip_flags(c, P->dev, nspin, v, g, thr, P->w_skip.as<unsigned char>()));
+  XC_TRY(c->scratch.alloc(c, std::max<long>(P->chunk_max_doubles, 1) * sizeof(double)));
+  for (size_t k = 0; k + 1 < P->chunk_bounds.size(); ++k) {
+    const int b0 = P->chunk_bounds[k], b1 = P->chunk_bounds[k + 1];
+    const long* so = P->w_slab.as<long>() + b0;
     XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, c->scratch.as<double>(), 1));
     XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, so,
-                            c->scratch.as<double>(), nspin, v, g, skip.as<unsigned char>(), F));
+                            c->scratch.as<double>(), nspin, v, g, P->w_skip.as<unsigned char>(), F));
   }
-  return XCGPU_OK;
-}
-
-static xcgpu_status prep_chunks(xcgpu_plan* P, Chunks& ch, DevBuf& d_slab) {
-  Ctx* c = P->ctx;
-  ch = make_chunks(P, c->scratch_cap);
-  XC_TRY(upload(c, d_slab, ch.slab_off.data(), ch.slab_off.size()));
   return XCGPU_OK;
 }
 
@@ -566,9 +559,7 @@ xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* r
   cudaSetDevice(c->device);
   const long n = P->grid->n;
   const int nbf = P->basis->nbf;
-  Chunks ch;
-  DevBuf d_slab, dPm, drho, dgrad;
-  XC_TRY(prep_chunks(P, ch, d_slab));
+  DevBuf dPm, drho, dgrad;
   const double* Pd = nullptr;
   XC_TRY(to_device(c, dPm, Pm, (size_t)nspin * nbf * nbf, mem, &Pd));
   double* r = rho;
@@ -582,7 +573,7 @@ xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* r
     }
   }
   XC_TRY(c->cuda(cudaMemsetAsync(r, 0, (size_t)nspin * n * sizeof(double), c->stream), "memset rho"));
-  XC_TRY(stage_density(P, ch, d_slab, nspin, Pd, r, gr));
+  XC_TRY(stage_density(P, nspin, Pd, r, gr));
   if (mem == XCGPU_MEM_HOST) {
     XC_TRY(c->cuda(cudaMemcpyAsync(rho, r, (size_t)nspin * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "rho"));
     if (grad)
@@ -641,9 +632,7 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* P, double thr, int nspin, const double
   cudaSetDevice(c->device);
   const long n = P->grid->n;
   const int nbf = P->basis->nbf;
-  Chunks ch;
-  DevBuf d_slab, dv, dg, dF, skip;
-  XC_TRY(prep_chunks(P, ch, d_slab));
+  DevBuf dv, dg, dF;
   const double *vd = nullptr, *gd = nullptr;
   XC_TRY(to_device(c, dv, v, (size_t)nspin * n, mem, &vd));
   if (g) XC_TRY(to_device(c, dg, g, (size_t)nspin * 3 * n, mem, &gd));
@@ -652,7 +641,7 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* P, double thr, int nspin, const double
     XC_TRY(upload(c, dF, F, (size_t)nspin * nbf * nbf));
     Fd = dF.as<double>();
   }
-  XC_TRY(stage_adder(P, ch, d_slab, nspin, vd, gd, thr, skip, Fd));
+  XC_TRY(stage_adder(P, nspin, vd, gd, thr, Fd));
   if (mem == XCGPU_MEM_HOST)
     XC_TRY(c->cuda(cudaMemcpyAsync(F, Fd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
                    "F"));
@@ -671,40 +660,42 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
   const bool gga = xc::is_gga(func);
   const long n = P->grid->n;
   const int nbf = P->basis->nbf;
-  Chunks ch;
-  DevBuf d_slab, dPm, dV, rho, grad, epuv, dfdrho, dfdgrad, partials, sums, skip;
-  XC_TRY(prep_chunks(P, ch, d_slab));
-  const double* Pd = nullptr;
-  XC_TRY(to_device(c, dPm, Pm, (size_t)nspin * nbf * nbf, mem, &Pd));
+  const double* Pd = Pm;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(upload(c, P->w_P, Pm, (size_t)nspin * nbf * nbf));
+    Pd = P->w_P.as<double>();
+  }
   double* Vd = V;
   if (mem == XCGPU_MEM_HOST) {
-    XC_TRY(dV.alloc(c, (size_t)nspin * nbf * nbf * sizeof(double)));
-    Vd = dV.as<double>();
+    XC_TRY(P->w_V.alloc(c, (size_t)nspin * nbf * nbf * sizeof(double)));
+    Vd = P->w_V.as<double>();
   }
-  XC_TRY(rho.alloc(c, (size_t)nspin * n * sizeof(double)));
-  XC_TRY(epuv.alloc(c, (size_t)n * sizeof(double)));
-  XC_TRY(dfdrho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  XC_TRY(P->w_rho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  XC_TRY(P->w_epuv.alloc(c, (size_t)n * sizeof(double)));
+  XC_TRY(P->w_dfdrho.alloc(c, (size_t)nspin * n * sizeof(double)));
   if (gga) {
-    XC_TRY(grad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
-    XC_TRY(dfdgrad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+    XC_TRY(P->w_grad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+    XC_TRY(P->w_dfdgrad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
   }
   const long nparts_max = (n + 127) / 128;
-  XC_TRY(partials.alloc(c, 2 * nparts_max * sizeof(double) + 16));
-  XC_TRY(sums.alloc(c, 2 * sizeof(double)));
+  XC_TRY(P->w_partials.alloc(c, 2 * nparts_max * sizeof(double) + 16));
+  XC_TRY(P->w_sums.alloc(c, 2 * sizeof(double)));
+  double* rho = P->w_rho.as<double>();
+  double* grad = gga ? P->w_grad.as<double>() : nullptr;
+  double* dfdgrad = gga ? P->w_dfdgrad.as<double>() : nullptr;
   // 1. rho, grad rho
-  XC_TRY(stage_density(P, ch, d_slab, nspin, Pd, rho.as<double>(), gga ? grad.as<double>() : nullptr));
+  XC_TRY(stage_density(P, nspin, Pd, rho, grad));
   // 2. functional + grid sums
   int nparts = 0;
-  XC_TRY(launch_functional(c, func, nspin, n, kSkipBlock, rho.as<double>(), gga ? grad.as<double>() : nullptr,
-                           epuv.as<double>(), dfdrho.as<double>(), gga ? dfdgrad.as<double>() : nullptr,
-                           P->dev.w, partials.as<double>(), &nparts));
-  if (nparts) XC_TRY(launch_sum_partials(c, partials.as<double>(), nparts, 2, sums.as<double>()));
-  else XC_TRY(c->cuda(cudaMemsetAsync(sums.p, 0, 2 * sizeof(double), c->stream), "memset sums"));
+  XC_TRY(launch_functional(c, func, nspin, n, kSkipBlock, rho, grad, P->w_epuv.as<double>(),
+                           P->w_dfdrho.as<double>(), dfdgrad, P->dev.w, P->w_partials.as<double>(), &nparts));
+  if (nparts) XC_TRY(launch_sum_partials(c, P->w_partials.as<double>(), nparts, 2, P->w_sums.as<double>()));
+  else XC_TRY(c->cuda(cudaMemsetAsync(P->w_sums.p, 0, 2 * sizeof(double), c->stream), "memset sums"));
   // 3. Vxc
   XC_TRY(c->cuda(cudaMemsetAsync(Vd, 0, (size_t)nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
-  XC_TRY(stage_adder(P, ch, d_slab, nspin, dfdrho.as<double>(), gga ? dfdgrad.as<double>() : nullptr, thr, skip, Vd));
+  XC_TRY(stage_adder(P, nspin, P->w_dfdrho.as<double>(), dfdgrad, thr, Vd));
   double hs[2] = {0, 0};
-  XC_TRY(c->cuda(cudaMemcpyAsync(hs, sums.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "sums"));
+  XC_TRY(c->cuda(cudaMemcpyAsync(hs, P->w_sums.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "sums"));
   if (mem == XCGPU_MEM_HOST)
     XC_TRY(c->cuda(cudaMemcpyAsync(V, Vd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
                    "V"));

@@ -159,6 +159,11 @@ struct xcgpu_plan {
   std::vector<long> work_off;  // [nblocks+1]
   xcgpu::DevBuf d_work;
   xcgpu::DevPlan dev;
+  // resident work buffers of the build (kept across calls: no allocation per build)
+  bool chunks_ready = false;
+  std::vector<int> chunk_bounds;
+  long chunk_max_doubles = 0;
+  xcgpu::DevBuf w_slab, w_P, w_V, w_rho, w_grad, w_epuv, w_dfdrho, w_dfdgrad, w_partials, w_sums, w_skip, w_aux;
 };
 
 namespace xcgpu {
