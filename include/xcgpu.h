@@ -155,8 +155,10 @@ void xcgpu_plan_destroy(xcgpu_plan* plan);
 /* ---- stages ----------------------------------------------------------------------------
  * DensityOnGridCalculator::calcDensityAndGradientOnGrid (DensityOnGridCalculator.h:53-128,
  * MatrixOperatorToGridTransformer.cpp:37-198): rho = rowsum((phi P_b) o phi),
- * grad rho = 2 rowsum((phi P_b) o grad phi).  grad may be NULL (density only). */
-xcgpu_status xcgpu_density(xcgpu_plan* plan, int nspin, const double* P, double* rho, double* grad, int mem);
+ * grad rho = 2 rowsum((phi P_b) o grad phi).  grad may be NULL (density only).
+ * precision: XCGPU_PREC_FP64 (the drop-in) or XCGPU_PREC_MIXED (3xTF32 tensor cores). */
+xcgpu_status xcgpu_density(xcgpu_plan* plan, int nspin, const double* P, double* rho, double* grad, int precision,
+                           int mem);
 /* FunctionalLibrary::calcData(GRADIENTS, f, ., order 1) (FunctionalLibrary.cpp:40-71,
  * XCFun.cpp:39-158): epuv (energy per volume), dF/drho and, for GGAs, dF/d(grad rho).
  * skip_block > 0 applies the reference's block skip (sum |rho| < n * 1e-12 on blocks of
@@ -169,7 +171,7 @@ int xcgpu_functional_is_gga(int func);
  * .cpp:51-113,178-303): F += sum_p w (v phi phi^T) (+ the GGA term with g = dF/d grad rho
  * when g != NULL).  Adds into F; blocks below block_ave_threshold are skipped. */
 xcgpu_status xcgpu_add_scalar(xcgpu_plan* plan, double block_ave_threshold, int nspin, const double* v,
-                              const double* g, double* F, int mem);
+                              const double* g, double* F, int precision, int mem);
 
 /* ---- whole build: FuncPotential::getMatrix + getEnergy (FuncPotential.cpp:74-110) -----
  * V (nspin matrices) is overwritten with the XC potential matrix; Exc = sum_p w_p epuv_p;

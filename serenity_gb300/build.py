@@ -33,8 +33,8 @@ def up_to_date():
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
-def _compile(src, extra):
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(src, extra, build_dir=BUILD):
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     cmd = [NVCC] + ARCH + FLAGS + extra + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -42,24 +42,28 @@ def _compile(src, extra):
     return obj, r.stderr
 
 
-def build(force=False, verbose=False, extra=()):
-    if not force and up_to_date():
+def build(force=False, verbose=False, extra=(), out=None):
+    """Compile and link; `out` (a path) builds a variant library elsewhere with the
+    extra nvcc flags (e.g. -D switches) instead of the default in-tree library."""
+    lib = out or LIB
+    if not force and out is None and up_to_date():
         return LIB
-    os.makedirs(BUILD, exist_ok=True)
+    build_dir = os.path.join(os.path.dirname(lib), "obj_" + os.path.basename(lib)) if out else BUILD
+    os.makedirs(build_dir, exist_ok=True)
     with concurrent.futures.ThreadPoolExecutor(max_workers=8) as ex:
-        results = list(ex.map(lambda s: _compile(s, list(extra)), sources()))
+        results = list(ex.map(lambda s: _compile(s, list(extra), build_dir), sources()))
     if verbose:
         for obj, err in results:
             if err.strip():
                 sys.stderr.write(err)
     objs = [o for o, _ in results]
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [NVCC] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", tmp] + objs + ["-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

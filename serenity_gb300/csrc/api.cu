@@ -552,7 +552,8 @@ static xcgpu_status to_device(Ctx* c, DevBuf& tmp, const T* src, size_t count, i
 
 extern "C" {
 
-xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* rho, double* grad, int mem) {
+xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* rho, double* grad, int precision,
+                           int mem) {
   if (!P) return XCGPU_ERR_INVALID;
   Ctx* c = P->ctx;
   if ((nspin != 1 && nspin != 2) || !Pm || !rho) return c->fail(XCGPU_ERR_INVALID, "density: bad arguments");
@@ -573,7 +574,13 @@ xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* r
     }
   }
   XC_TRY(c->cuda(cudaMemsetAsync(r, 0, (size_t)nspin * n * sizeof(double), c->stream), "memset rho"));
-  XC_TRY(stage_density(P, nspin, Pd, r, gr));
+  if (precision == XCGPU_PREC_MIXED) {
+    XC_TRY(P->w_aux.alloc(c, 4 * sizeof(int)));
+    XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
+    XC_TRY(mixed_density(c, P->basis->dev, P->dev, nspin, Pd, r, gr, P->w_aux.as<int>(), P->w_aux.as<int>() + 2));
+  } else {
+    XC_TRY(stage_density(P, nspin, Pd, r, gr));
+  }
   if (mem == XCGPU_MEM_HOST) {
     XC_TRY(c->cuda(cudaMemcpyAsync(rho, r, (size_t)nspin * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "rho"));
     if (grad)
@@ -625,7 +632,7 @@ xcgpu_status xcgpu_functional(xcgpu_ctx* c, int func, int nspin, uint64_t n, uin
 }
 
 xcgpu_status xcgpu_add_scalar(xcgpu_plan* P, double thr, int nspin, const double* v, const double* g, double* F,
-                              int mem) {
+                              int precision, int mem) {
   if (!P) return XCGPU_ERR_INVALID;
   Ctx* c = P->ctx;
   if ((nspin != 1 && nspin != 2) || !v || !F) return c->fail(XCGPU_ERR_INVALID, "add_scalar: bad arguments");
@@ -641,7 +648,21 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* P, double thr, int nspin, const double
     XC_TRY(upload(c, dF, F, (size_t)nspin * nbf * nbf));
     Fd = dF.as<double>();
   }
-  XC_TRY(stage_adder(P, nspin, vd, gd, thr, Fd));
+  if (precision == XCGPU_PREC_MIXED) {
+    // the mixed adder accumulates into a zeroed matrix and symmetrises it; add that to F
+    DevBuf tmpF;
+    XC_TRY(tmpF.alloc(c, (size_t)nspin * nbf * nbf * sizeof(double)));
+    XC_TRY(c->cuda(cudaMemsetAsync(tmpF.p, 0, (size_t)nspin * nbf * nbf * sizeof(double), c->stream), "memset"));
+    XC_TRY(P->w_aux.alloc(c, 4 * sizeof(int)));
+    XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
+    XC_TRY(P->w_skip.alloc(c, (size_t)nspin * P->nblocks + 1));
+    XC_TRY(launch_block_skip_flags(c, P->dev, nspin, vd, gd, thr, P->w_skip.as<unsigned char>()));
+    XC_TRY(mixed_adder(c, P->basis->dev, P->dev, nspin, vd, gd, P->w_skip.as<unsigned char>(), tmpF.as<double>(),
+                       P->w_aux.as<int>() + 1, P->w_aux.as<int>() + 2));
+    XC_TRY(launch_axpy(c, (long)nspin * nbf * nbf, tmpF.as<double>(), Fd));
+  } else {
+    XC_TRY(stage_adder(P, nspin, vd, gd, thr, Fd));
+  }
   if (mem == XCGPU_MEM_HOST)
     XC_TRY(c->cuda(cudaMemcpyAsync(F, Fd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
                    "F"));
@@ -654,8 +675,9 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
   Ctx* c = P->ctx;
   if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "unknown functional");
   if ((nspin != 1 && nspin != 2) || !Pm || !V) return c->fail(XCGPU_ERR_INVALID, "vxc: bad arguments");
-  if (precision != XCGPU_PREC_FP64)
-    return c->fail(XCGPU_ERR_UNSUPPORTED, "vxc: requested precision is not available in this build");
+  if (precision != XCGPU_PREC_FP64 && precision != XCGPU_PREC_MIXED)
+    return c->fail(XCGPU_ERR_INVALID, "vxc: unknown precision");
+  const bool mixed = precision == XCGPU_PREC_MIXED;
   cudaSetDevice(c->device);
   const bool gga = xc::is_gga(func);
   const long n = P->grid->n;
@@ -683,8 +705,13 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
   double* rho = P->w_rho.as<double>();
   double* grad = gga ? P->w_grad.as<double>() : nullptr;
   double* dfdgrad = gga ? P->w_dfdgrad.as<double>() : nullptr;
+  XC_TRY(P->w_aux.alloc(c, 4 * sizeof(int)));
+  int* counter = P->w_aux.as<int>();
+  int* err = counter + 2;
+  XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
   // 1. rho, grad rho
-  XC_TRY(stage_density(P, nspin, Pd, rho, grad));
+  if (mixed) XC_TRY(mixed_density(c, P->basis->dev, P->dev, nspin, Pd, rho, grad, counter, err));
+  else XC_TRY(stage_density(P, nspin, Pd, rho, grad));
   // 2. functional + grid sums
   int nparts = 0;
   XC_TRY(launch_functional(c, func, nspin, n, kSkipBlock, rho, grad, P->w_epuv.as<double>(),
@@ -693,13 +720,24 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
   else XC_TRY(c->cuda(cudaMemsetAsync(P->w_sums.p, 0, 2 * sizeof(double), c->stream), "memset sums"));
   // 3. Vxc
   XC_TRY(c->cuda(cudaMemsetAsync(Vd, 0, (size_t)nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
-  XC_TRY(stage_adder(P, nspin, P->w_dfdrho.as<double>(), dfdgrad, thr, Vd));
+  if (mixed) {
+    XC_TRY(P->w_skip.alloc(c, (size_t)nspin * P->nblocks + 1));
+    XC_TRY(launch_block_skip_flags(c, P->dev, nspin, P->w_dfdrho.as<double>(), dfdgrad, thr,
+                                   P->w_skip.as<unsigned char>()));
+    XC_TRY(mixed_adder(c, P->basis->dev, P->dev, nspin, P->w_dfdrho.as<double>(), dfdgrad,
+                       P->w_skip.as<unsigned char>(), Vd, counter + 1, err));
+  } else {
+    XC_TRY(stage_adder(P, nspin, P->w_dfdrho.as<double>(), dfdgrad, thr, Vd));
+  }
+  int herr = 0;
+  XC_TRY(c->cuda(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
   double hs[2] = {0, 0};
   XC_TRY(c->cuda(cudaMemcpyAsync(hs, P->w_sums.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "sums"));
   if (mem == XCGPU_MEM_HOST)
     XC_TRY(c->cuda(cudaMemcpyAsync(V, Vd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
                    "V"));
   XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "vxc"));
+  if (herr) return c->fail(XCGPU_ERR_TIMEOUT, "vxc: a bounded device-side wait gave up (tensor-core pipeline)");
   if (Exc) *Exc = hs[0];
   if (Nel) *Nel = hs[1];
   return XCGPU_OK;

@@ -16,7 +16,13 @@ __host__ __device__ __forceinline__ int ncart_d(int l) { return (l + 1) * (l + 2
 
 template <class R> __device__ __forceinline__ R dexp(R x);
 template <> __device__ __forceinline__ double dexp<double>(double x) { return exp(x); }
+// FP32 exponential of the mixed-precision basis: the accurate expf by default;
+// XCGPU_FAST_EXP selects the approximate __expf.
+#ifdef XCGPU_FAST_EXP
 template <> __device__ __forceinline__ float dexp<float>(float x) { return __expf(x); }
+#else
+template <> __device__ __forceinline__ float dexp<float>(float x) { return expf(x); }
+#endif
 
 // radial part of shell s at squared distance r2; returns false if negligible
 template <class R, int DERIV>

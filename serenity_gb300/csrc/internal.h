@@ -189,6 +189,12 @@ xcgpu_status launch_block_skip_flags(Ctx* c, const DevPlan& P, int nspin, const 
 xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0, long w1, int chunk_b0,
                               const long* slab_off, const double* scratch, int nspin, const double* v,
                               const double* g, const unsigned char* skip, double* F);
+xcgpu_status launch_axpy(Ctx* c, long n, const double* x, double* y);  // y += x
 xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out /*device*/);
+// mixed precision (tcgen05, 3xTF32): density (rho, grad rho in FP64) and adder (V += D, then V + V^T)
+xcgpu_status mixed_density(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* Pm, double* rho,
+                           double* grad, int* counter, int* err);
+xcgpu_status mixed_adder(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* v, const double* g,
+                         const unsigned char* skip, double* V, int* counter, int* err);
 
 }  // namespace xcgpu

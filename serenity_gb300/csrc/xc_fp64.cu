@@ -540,6 +540,18 @@ __global__ void __launch_bounds__(256) sum_partials_kernel(const double* __restr
   }
 }
 
+__global__ void axpy_kernel(long n, const double* __restrict__ x, double* __restrict__ y) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += x[i];
+}
+
+xcgpu_status launch_axpy(Ctx* c, long n, const double* x, double* y) {
+  if (n == 0) return XCGPU_OK;
+  KernelTimer kt(c, kOther);
+  axpy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, x, y);
+  return c->check_launch("axpy_kernel");
+}
+
 xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out) {
   KernelTimer kt(c, kOther);
   sum_partials_kernel<<<1, 256, 0, c->stream>>>(partials, nparts, ncomp, out);

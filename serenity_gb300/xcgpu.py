@@ -87,10 +87,10 @@ def library(build_if_needed=True):
     L.xcgpu_block_active.argtypes = [vp, ctypes.c_uint32, vp]
     L.xcgpu_block_active.restype = ctypes.c_int32
     L.xcgpu_plan_destroy.argtypes = [vp]
-    L.xcgpu_density.argtypes = [vp, S, vp, vp, vp, S]
+    L.xcgpu_density.argtypes = [vp, S, vp, vp, vp, S, S]
     L.xcgpu_functional.argtypes = [vp, S, S, ctypes.c_uint64, ctypes.c_uint32, vp, vp, vp, vp, vp, S]
     L.xcgpu_functional_is_gga.argtypes = [S]
-    L.xcgpu_add_scalar.argtypes = [vp, ctypes.c_double, S, vp, vp, vp, S]
+    L.xcgpu_add_scalar.argtypes = [vp, ctypes.c_double, S, vp, vp, vp, S, S]
     L.xcgpu_vxc.argtypes = [vp, S, S, S, ctypes.c_double, vp, vp, dp, dp, S]
     for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
                  "xcgpu_grid_copy", "xcgpu_basis_create", "xcgpu_basis_coefs", "xcgpu_plan_create",
@@ -285,24 +285,24 @@ class Plan:
         self.ctx.L.xcgpu_block_active(self.h, block, _ptr(idx))
         return idx[:n]
 
-    def density(self, P, grad=True):
+    def density(self, P, grad=True, precision=PREC_FP64):
         """rho [nspin, n], grad [nspin, 3, n] for P [nbf, nbf] or [nspin, nbf, nbf] (symmetric)."""
         P = np.asarray(P, dtype=np.float64)
         nspin = 1 if P.ndim == 2 else P.shape[0]
         Pc = np.ascontiguousarray(np.stack([m.T for m in P.reshape(nspin, self.nbf, self.nbf)]))
         rho = np.zeros((nspin, self.grid.n))
         g = np.zeros((nspin, 3, self.grid.n)) if grad else None
-        self.ctx.check(self.ctx.L.xcgpu_density(self.h, nspin, _ptr(Pc), _ptr(rho), _ptr(g), MEM_HOST))
+        self.ctx.check(self.ctx.L.xcgpu_density(self.h, nspin, _ptr(Pc), _ptr(rho), _ptr(g), precision, MEM_HOST))
         return rho, g
 
-    def add_scalar(self, v, g=None, F=None, block_ave_threshold=1e-11):
+    def add_scalar(self, v, g=None, F=None, block_ave_threshold=1e-11, precision=PREC_FP64):
         v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
         nspin = v.size // self.grid.n
         gg = None if g is None else np.ascontiguousarray(g, dtype=np.float64).reshape(-1)
         Fc = np.zeros((nspin, self.nbf, self.nbf)) if F is None else np.ascontiguousarray(
             np.stack([m.T for m in np.asarray(F, dtype=np.float64).reshape(nspin, self.nbf, self.nbf)]))
         self.ctx.check(self.ctx.L.xcgpu_add_scalar(self.h, block_ave_threshold, nspin, _ptr(v), _ptr(gg), _ptr(Fc),
-                                                   MEM_HOST))
+                                                   precision, MEM_HOST))
         return Fc.transpose(0, 2, 1)
 
     def vxc(self, func, P, precision=PREC_FP64, block_ave_threshold=1e-11, out=None):
