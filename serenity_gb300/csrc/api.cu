@@ -251,7 +251,7 @@ xcgpu_status xcgpu_basis_create(xcgpu_ctx* c, const xcgpu_shell* shells, uint32_
       delete B;
       return c->fail(XCGPU_ERR_UNSUPPORTED, "Angular momentum too high for transformation spherical harmonics.");
     }
-    if (sh.nprim <= 0 || !sh.alpha || !sh.coef) {
+    if (sh.nprim <= 0 || sh.nprim > 31 || !sh.alpha || !sh.coef) {
       delete B;
       return c->fail(XCGPU_ERR_INVALID, "basis: shell without primitives");
     }
@@ -303,6 +303,12 @@ xcgpu_status xcgpu_basis_create(xcgpu_ctx* c, const xcgpu_shell* shells, uint32_
   if (!st) st = upload(c, B->d_cnorm, cnorm.data(), cnorm.size());
   if (!st) st = upload(c, B->d_toff, toff.data(), toff.size());
   if (!st) st = upload(c, B->d_coff, coff.data(), coff.size());
+  std::vector<float> prim2;
+  for (size_t i = 0; i < B->alpha.size(); ++i) {
+    prim2.push_back((float)B->alpha[i]);
+    prim2.push_back((float)B->coef[i]);
+  }
+  if (!st) st = upload(c, B->d_prim2, prim2.data(), prim2.size());
   if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "basis upload");
   if (st) {
     delete B;
@@ -324,6 +330,7 @@ xcgpu_status xcgpu_basis_create(xcgpu_ctx* c, const xcgpu_shell* shells, uint32_
   d.cnorm = B->d_cnorm.as<double>();
   d.trans_off = B->d_toff.as<int>();
   d.cnorm_off = B->d_coff.as<int>();
+  d.prim2 = B->d_prim2.as<float2>();
   *out = B;
   return XCGPU_OK;
 }
@@ -392,7 +399,25 @@ xcgpu_status xcgpu_plan_create(xcgpu_ctx* c, xcgpu_grid* g, xcgpu_basis* B, uint
       }
     P->work_off.push_back((long)P->work.size() / 3);
   }
-  st = upload(c, P->d_sh_off, P->sh_off.data(), P->sh_off.size());
+  std::vector<ShellRec> rec(P->sh_list.size());
+  for (int b = 0; b < nb; ++b) {
+    int f0 = 0;
+    for (int k = P->sh_off[b]; k < P->sh_off[b + 1]; ++k) {
+      const int s = P->sh_list[k];
+      ShellRec& r = rec[k];
+      for (int q = 0; q < 3; ++q) {
+        const double a = B->center[3 * s + q];
+        r.ah[q] = (float)a;
+        r.al[q] = (float)(a - (double)r.ah[q]);
+      }
+      const int nf = B->pure[s] ? 2 * B->l[s] + 1 : ncart(B->l[s]);
+      r.info = B->l[s] | (B->pure[s] << 3) | (B->nprim[s] << 4) | (nf << 9) | (f0 << 14);
+      r.prim0 = B->prim_off[s];
+      f0 += nf;
+    }
+  }
+  st = upload(c, P->d_rec, rec.data(), rec.size());
+  if (!st) st = upload(c, P->d_sh_off, P->sh_off.data(), P->sh_off.size());
   if (!st) st = upload(c, P->d_sh_list, P->sh_list.data(), P->sh_list.size());
   if (!st) st = upload(c, P->d_fn_off, P->fn_off.data(), P->fn_off.size());
   if (!st) st = upload(c, P->d_fn_list, P->fn_list.data(), P->fn_list.size());
@@ -413,6 +438,7 @@ xcgpu_status xcgpu_plan_create(xcgpu_ctx* c, xcgpu_grid* g, xcgpu_basis* B, uint
   d.sh_list = P->d_sh_list.as<int>();
   d.fn_off = P->d_fn_off.as<int>();
   d.fn_list = P->d_fn_list.as<int>();
+  d.rec = P->d_rec.as<ShellRec>();
   d.radial_threshold = thr;
   d.exponent_threshold = thr > 0 ? -std::log(thr) : HUGE_VAL;
   *out = P;
@@ -577,7 +603,9 @@ xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* r
   if (precision == XCGPU_PREC_MIXED) {
     XC_TRY(P->w_aux.alloc(c, 4 * sizeof(int)));
     XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
-    XC_TRY(mixed_density(c, P->basis->dev, P->dev, nspin, Pd, r, gr, P->w_aux.as<int>(), P->w_aux.as<int>() + 2));
+    XC_TRY(P->w_psplit.alloc(c, 2 * (size_t)nspin * nbf * nbf * sizeof(float)));
+    XC_TRY(mixed_density(c, P->basis->dev, P->dev, nspin, Pd, P->w_psplit.as<float>(), r, gr, P->w_aux.as<int>(),
+                         P->w_aux.as<int>() + 2));
   } else {
     XC_TRY(stage_density(P, nspin, Pd, r, gr));
   }
@@ -710,7 +738,10 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
   int* err = counter + 2;
   XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
   // 1. rho, grad rho
-  if (mixed) XC_TRY(mixed_density(c, P->basis->dev, P->dev, nspin, Pd, rho, grad, counter, err));
+  if (mixed) {
+    XC_TRY(P->w_psplit.alloc(c, 2 * (size_t)nspin * nbf * nbf * sizeof(float)));
+    XC_TRY(mixed_density(c, P->basis->dev, P->dev, nspin, Pd, P->w_psplit.as<float>(), rho, grad, counter, err));
+  }
   else XC_TRY(stage_density(P, nspin, Pd, rho, grad));
   // 2. functional + grid sums
   int nparts = 0;

@@ -14,6 +14,54 @@ namespace xcgpu {
 
 __host__ __device__ __forceinline__ int ncart_d(int l) { return (l + 1) * (l + 2) / 2; }
 
+// ---- compile-time real solid harmonic coefficients -----------------------------------
+// Same closed form as the host tables (Helgaker, Joergensen & Olsen, sec. 6.4):
+// S_lm = N_lm sum_{t,u,v} C_tuv x^(2t+|m|-2(u+v)) y^(2(u+v)) z^(l-2t-|m|), m = -l..l,
+// evaluated by constexpr code so the device kernels multiply by literal constants.
+namespace cx {
+constexpr double fact(int n) { return n <= 1 ? 1.0 : n * fact(n - 1); }
+constexpr double binom(int n, int k) { return (k < 0 || k > n) ? 0.0 : fact(n) / (fact(k) * fact(n - k)); }
+constexpr double sqrt_newton(double x, double g, int it) { return it == 0 ? g : sqrt_newton(x, 0.5 * (g + x / g), it - 1); }
+constexpr double sqrt(double x) { return x <= 0 ? 0.0 : sqrt_newton(x, x > 1 ? x : 1.0, 60); }
+constexpr double pow2(int n) { return n == 0 ? 1.0 : 2.0 * pow2(n - 1); }
+constexpr double pow025(int n) { return n == 0 ? 1.0 : 0.25 * pow025(n - 1); }
+struct Table {
+  double c[13][28];
+};
+constexpr int cart_index(int l, int a, int b) {
+  int k = 0;
+  for (int aa = l; aa > a; --aa) k += l - aa + 1;
+  return k + (l - a - b);
+}
+constexpr Table solid(int l) {
+  Table T{};
+  for (int m = -l; m <= l; ++m) {
+    const int am = m < 0 ? -m : m;
+    const int tv0 = m < 0 ? 1 : 0;
+    const double N = sqrt(2.0 * fact(l + am) * fact(l - am) / (m == 0 ? 2.0 : 1.0)) / (pow2(am) * fact(l));
+    for (int t = 0; t <= (l - am) / 2; ++t)
+      for (int u = 0; u <= t; ++u)
+        for (int tv = tv0; tv <= am; tv += 2) {
+          const int se = t + (tv - tv0) / 2;
+          const double C = (se % 2 ? -1.0 : 1.0) * pow025(t) * binom(l, t) * binom(l - t, am + t) * binom(t, u) *
+                           binom(am, tv);
+          const int py = 2 * u + tv, px = 2 * t + am - py;
+          T.c[m + l][cart_index(l, px, py)] += N * C;
+        }
+  }
+  return T;
+}
+constexpr double dfact(int n) { return n <= 1 ? 1.0 : n * dfact(n - 2); }
+constexpr Table cartesian(int l) {
+  Table T{};
+  int k = 0;
+  for (int a = l; a >= 0; --a)
+    for (int b = l - a; b >= 0; --b, ++k)
+      T.c[0][k] = sqrt(dfact(2 * l - 1) / (dfact(2 * a - 1) * dfact(2 * b - 1) * dfact(2 * (l - a - b) - 1)));
+  return T;
+}
+}  // namespace cx
+
 template <class R> __device__ __forceinline__ R dexp(R x);
 template <> __device__ __forceinline__ double dexp<double>(double x) { return exp(x); }
 // FP32 exponential of the mixed-precision basis: the accurate expf by default;
@@ -139,6 +187,84 @@ __device__ __forceinline__ void shell_functions(R x, R y, R z, R Rv, R dR, R ddR
       emit(m, sv[m], DERIV >= 1 ? sg[3 * m] : R(0), DERIV >= 1 ? sg[3 * m + 1] : R(0),
            DERIV >= 1 ? sg[3 * m + 2] : R(0), ht);
     }
+  }
+}
+
+// Same as shell_functions, with the transform coefficients as compile-time constants.
+template <class R, int L, int DERIV, class Emit>
+__device__ __forceinline__ void shell_functions_cx(R x, R y, R z, R Rv, R dR, bool pure, Emit&& emit) {
+  constexpr int NC = (L + 1) * (L + 2) / 2;
+  constexpr int NS = 2 * L + 1;
+  constexpr cx::Table TS = cx::solid(L);
+  constexpr cx::Table TC = cx::cartesian(L);
+  R px[L + 2], py[L + 2], pz[L + 2];
+  px[0] = py[0] = pz[0] = R(1);
+#pragma unroll
+  for (int k = 1; k < L + 2; ++k) {
+    px[k] = px[k - 1] * x;
+    py[k] = py[k - 1] * y;
+    pz[k] = pz[k - 1] * z;
+  }
+  R sv[NS], sg[3 * NS];
+#pragma unroll
+  for (int m = 0; m < NS; ++m) {
+    sv[m] = R(0);
+    sg[3 * m] = sg[3 * m + 1] = sg[3 * m + 2] = R(0);
+  }
+  int k = 0;
+#pragma unroll
+  for (int a = L; a >= 0; --a) {
+#pragma unroll
+    for (int b = L - a; b >= 0; --b, ++k) {
+      const int c = L - a - b;
+      const R mono = px[a] * py[b] * pz[c];
+      const R v = mono * Rv;
+      R g0 = R(0), g1 = R(0), g2 = R(0);
+      if (DERIV >= 1) {
+        const R dmx = a > 0 ? R(a) * px[a > 0 ? a - 1 : 0] * py[b] * pz[c] : R(0);
+        const R dmy = b > 0 ? R(b) * px[a] * py[b > 0 ? b - 1 : 0] * pz[c] : R(0);
+        const R dmz = c > 0 ? R(c) * px[a] * py[b] * pz[c > 0 ? c - 1 : 0] : R(0);
+        const R md = mono * dR;
+        g0 = dmx * Rv + md * x;
+        g1 = dmy * Rv + md * y;
+        g2 = dmz * Rv + md * z;
+      }
+      if (pure) {
+#pragma unroll
+        for (int m = 0; m < NS; ++m) {
+          const R t = R(TS.c[m][k]);
+          if (TS.c[m][k] != 0.0) {
+            sv[m] += t * v;
+            if (DERIV >= 1) {
+              sg[3 * m] += t * g0;
+              sg[3 * m + 1] += t * g1;
+              sg[3 * m + 2] += t * g2;
+            }
+          }
+        }
+      } else {
+        const R t = R(TC.c[0][k]);
+        emit(k, t * v, t * g0, t * g1, t * g2);
+      }
+    }
+  }
+  if (pure) {
+#pragma unroll
+    for (int m = 0; m < NS; ++m) emit(m, sv[m], sg[3 * m], sg[3 * m + 1], sg[3 * m + 2]);
+  }
+}
+
+template <class R, int DERIV, class Emit>
+__device__ __forceinline__ void shell_functions_cx_l(int l, R x, R y, R z, R Rv, R dR, bool pure, Emit&& emit) {
+  switch (l) {
+    case 0: shell_functions_cx<R, 0, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 1: shell_functions_cx<R, 1, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 2: shell_functions_cx<R, 2, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 3: shell_functions_cx<R, 3, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 4: shell_functions_cx<R, 4, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 5: shell_functions_cx<R, 5, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 6: shell_functions_cx<R, 6, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    default: break;
   }
 }
 

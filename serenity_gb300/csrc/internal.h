@@ -32,6 +32,18 @@ struct DevBasis {
   const double* cnorm = nullptr;   // per l, ncart(l) Cartesian factors
   const int* trans_off = nullptr;  // [kMaxL+1] offsets into trans
   const int* cnorm_off = nullptr;  // [kMaxL+1] offsets into cnorm
+  const float2* prim2 = nullptr;   // (alpha, normalised coef) in FP32 for the FP32 kernels
+};
+
+// Per (block, active shell) record used by the FP32 kernels (32 bytes).  The centre
+// is split into an FP32 high part and FP32 remainder so that p - A keeps FP32
+// relative accuracy; info packs l (bits 0-2), pure (3), nprim (4-8), nfunc (9-13)
+// and the shell's first function within the block's active list (14-31).
+struct __align__(16) ShellRec {
+  float ah[3];
+  float al[3];
+  int info;
+  int prim0;  // offset of the shell's (alpha, coef) pairs in DevBasis::prim2
 };
 
 // Device-side block table of a plan.
@@ -44,6 +56,7 @@ struct DevPlan {
   const int* sh_list = nullptr;
   const int* fn_off = nullptr;     // [nblocks+1] active functions of block b
   const int* fn_list = nullptr;
+  const ShellRec* rec = nullptr;   // parallel to sh_list
   double radial_threshold = 1e-9, exponent_threshold = 0.0;
 };
 
@@ -140,7 +153,8 @@ struct xcgpu_basis {
   int nshell = 0, nbf = 0, maxl = 0;
   std::vector<int> l, pure, nprim, prim_off, first;
   std::vector<double> center, alpha, coef;
-  xcgpu::DevBuf d_l, d_pure, d_nprim, d_prim_off, d_first, d_center, d_alpha, d_coef, d_trans, d_cnorm, d_toff, d_coff;
+  xcgpu::DevBuf d_l, d_pure, d_nprim, d_prim_off, d_first, d_center, d_alpha, d_coef, d_trans, d_cnorm, d_toff, d_coff,
+      d_prim2;
   xcgpu::DevBasis dev;
 };
 
@@ -153,7 +167,7 @@ struct xcgpu_plan {
   std::vector<int> sh_off, sh_list, fn_off, fn_list;  // host copies
   int max_active = 0;
   double flops = 0.0;
-  xcgpu::DevBuf d_sh_off, d_sh_list, d_fn_off, d_fn_list;
+  xcgpu::DevBuf d_sh_off, d_sh_list, d_fn_off, d_fn_list, d_rec;
   // adder tile work list (block, tile_i, tile_j) for 64-wide tiles, upper triangle
   std::vector<int> work;  // 3 ints per item, sorted by block
   std::vector<long> work_off;  // [nblocks+1]
@@ -163,7 +177,7 @@ struct xcgpu_plan {
   bool chunks_ready = false;
   std::vector<int> chunk_bounds;
   long chunk_max_doubles = 0;
-  xcgpu::DevBuf w_slab, w_P, w_V, w_rho, w_grad, w_epuv, w_dfdrho, w_dfdgrad, w_partials, w_sums, w_skip, w_aux;
+  xcgpu::DevBuf w_psplit, w_slab, w_P, w_V, w_rho, w_grad, w_epuv, w_dfdrho, w_dfdgrad, w_partials, w_sums, w_skip, w_aux;
 };
 
 namespace xcgpu {
@@ -192,8 +206,8 @@ xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0
 xcgpu_status launch_axpy(Ctx* c, long n, const double* x, double* y);  // y += x
 xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out /*device*/);
 // mixed precision (tcgen05, 3xTF32): density (rho, grad rho in FP64) and adder (V += D, then V + V^T)
-xcgpu_status mixed_density(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* Pm, double* rho,
-                           double* grad, int* counter, int* err);
+xcgpu_status mixed_density(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* Pm, float* Psplit,
+                           double* rho, double* grad, int* counter, int* err);
 xcgpu_status mixed_adder(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* v, const double* g,
                          const unsigned char* skip, double* V, int* counter, int* err);
 

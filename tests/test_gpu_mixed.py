@@ -2,8 +2,8 @@
 contractions with FP32 accumulation; FP64 functional, grid sums and cross-block
 Vxc) against the FP64 path and the oracle on the same inputs.
 
-Stated tolerances (water tetramer, def2-SVP, 30 x 110 grid): density relative to
-max rho 2e-6, adder 2e-6 absolute, E_xc 1e-6 Eh, max|dVxc| 2e-6."""
+Stated tolerances (water tetramer, def2-SVP / def2-TZVP, 30 x 110 grid): density
+relative to max rho 2e-6, adder 2e-6 absolute, E_xc 5e-6 Eh, max|dVxc| 1e-6."""
 import numpy as np
 import pytest
 
@@ -19,10 +19,9 @@ def ctx():
     return xcgpu.Context()
 
 
-def _case(func, unrestricted, max_block=128, seed=3):
-    from serenity_gb300 import xcgpu
+def _case(func, unrestricted, max_block=128, seed=3, basis="DEF2-SVP", spherical=True):
     sym, xyz = wl.water_cluster(4, seed, jitter=0.2, dims=(2, 2, 1))
-    w = wl.Workload(sym, xyz, "DEF2-SVP", func, (20, 19) if unrestricted else 20, 30, 110, seed)
+    w = wl.Workload(sym, xyz, basis, func, (20, 19) if unrestricted else 20, 30, 110, seed, spherical=spherical)
     pts, wts = po.becke_grid(w.Z, w.coords, n_rad=30, n_ang=110)
     return w, pts, wts
 
@@ -60,15 +59,17 @@ def test_mixed_adder_vs_fp64(ctx):
     assert np.abs(Fmx - F64).max() <= 2e-6 * max(1.0, np.abs(F64).max())
 
 
-@pytest.mark.parametrize("func,unrestricted", [("LDA", False), ("PBE", False), ("BLYP", False), ("PBE", True)])
-def test_mixed_vxc_vs_oracle(ctx, func, unrestricted):
+@pytest.mark.parametrize("func,unrestricted,basis,spherical", [
+    ("LDA", False, "DEF2-SVP", True), ("PBE", False, "DEF2-SVP", True), ("BLYP", False, "DEF2-SVP", True),
+    ("PBE", True, "DEF2-SVP", True), ("PBE", False, "DEF2-TZVP", True), ("PBE", False, "DEF2-TZVP", False)])
+def test_mixed_vxc_vs_oracle(ctx, func, unrestricted, basis, spherical):
     from serenity_gb300 import xcgpu
-    w, pts, wts = _case(func, unrestricted)
+    w, pts, wts = _case(func, unrestricted, basis=basis, spherical=spherical)
     plan = _plan(ctx, w, pts, wts)
     P = w.density()
     V, exc, nel = plan.vxc(func, P, precision=xcgpu.PREC_MIXED)
     rV, rexc, rnel = po.Basis(w.shells).vxc(pts, wts, func, P)
-    assert abs(exc - rexc) <= 1e-6, abs(exc - rexc)
+    assert abs(exc - rexc) <= 5e-6, abs(exc - rexc)
     assert abs(nel - rnel) <= 1e-6 * rnel
-    assert np.abs(V - rV).max() <= 2e-6, np.abs(V - rV).max()
+    assert np.abs(V - rV).max() <= 1e-6, np.abs(V - rV).max()
     np.testing.assert_allclose(V, np.swapaxes(V, 1, 2), rtol=0, atol=1e-14)

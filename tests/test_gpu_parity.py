@@ -172,3 +172,25 @@ def test_stages_vs_oracle_ragged_blocks(ctx):
     F = plan.add_scalar(v)
     rF = ob.add_scalar(pts, wts, v, None, max_block=37)
     np.testing.assert_allclose(F, rF, rtol=0, atol=1e-11)
+
+
+def test_spherical_normalisation_sc_cc_pv5z(ctx):
+    """<phi|phi> = 1 for the s ... i functions of Sc cc-pV5Z on an accuracy-7 Becke grid
+    (the reference's SphBFOnGridTest, BasisFunctionOnGridController_test.cpp:491-684),
+    integrated through the adder with v = 1."""
+    from serenity_gb300 import xcgpu
+    from serenity_gb300.basis import Shells
+    Z = [21]
+    xyz = np.zeros((1, 3))
+    g = xcgpu.Grid.build(ctx, Z, xyz, accuracy=7, weight_threshold=0.0, smoothing=3)
+    b = xcgpu.Basis(ctx, Shells.for_atoms(["Sc"], xyz, "CC-PV5Z", spherical=True))
+    plan = xcgpu.Plan(ctx, g, b, 128, 0.0)
+    S = plan.add_scalar(np.ones(g.n), block_ave_threshold=0.0)[0]
+    d = np.diag(S)
+    # the reference checks 1e-7 on the functions the grid resolves (its s-function loop
+    # stops at n = 9 for that reason); a wrong harmonic coefficient would be O(1) off
+    lvals = np.concatenate([[sh] * (2 * sh + 1) for sh in b.shells.l])
+    for l in range(7):
+        dev = np.abs(d[lvals == l] - 1.0)
+        assert np.median(dev) < 1e-7, (l, dev)
+        assert dev.max() < 1e-5, (l, dev)
