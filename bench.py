@@ -147,7 +147,37 @@ def build_workload(args):
     return w, P
 
 
+def time_builds(ctx, plan, w, P_dev, V_dev, prec, steps, warmup, flush, stream, clock_dev=None):
+    """Per-step CUDA events on the library's stream, L2 flushed between steps
+    (outside the events).  Returns (step_ms, kernel_ms[5], launches, results, clocks)."""
+    import ctypes
+    import torch
+    for _ in range(warmup):
+        flush.zero_()
+        plan.vxc(w.func, P_dev, precision=prec, out=V_dev)
+    torch.cuda.synchronize()
+    launches0 = ctx.kernel_launches
+    ctx.L.xcgpu_set_timing(ctx.h, 1)
+    ctx.L.xcgpu_get_timing(ctx.h, None, None)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    results = []
+    clk = ClockSampler(clock_dev if clock_dev is not None else 0)
+    with clk:
+        for i in range(steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            results.append(plan.vxc(w.func, P_dev, precision=prec, out=V_dev))
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    kms = (ctypes.c_double * 5)()
+    kcnt = (ctypes.c_uint64 * 5)()
+    ctx.L.xcgpu_get_timing(ctx.h, kms, kcnt)
+    ctx.L.xcgpu_set_timing(ctx.h, 0)
+    return [a.elapsed_time(b) for a, b in ev], list(kms), ctx.kernel_launches - launches0, results, clk.summary()
+
+
 def run_ours(args, dist):
+    import ctypes
     import torch
     from serenity_gb300 import xcgpu
 
@@ -161,47 +191,28 @@ def run_ours(args, dist):
     basis = xcgpu.Basis(ctx, w.shells)
     plan = xcgpu.Plan(ctx, grid, basis, 128, 1e-9)
     st = plan.stats()
-    nspin = w.nspin
-    nbf = w.nbf
+    nspin, nbf = w.nspin, w.nbf
     Pc = np.ascontiguousarray(np.stack([m.T for m in np.asarray(P).reshape(nspin, nbf, nbf)]))
     P_dev = torch.from_numpy(Pc).cuda()
     V_dev = torch.zeros_like(P_dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    prec = xcgpu.PREC_MIXED if args.precision == "mixed" else xcgpu.PREC_FP64
-
-    def step():
-        return plan.vxc(w.func, P_dev, precision=prec, out=V_dev)
-
-    for _ in range(args.warmup):
-        flush.zero_()
-        step()
-    torch.cuda.synchronize()
-    launches0 = ctx.kernel_launches
-    ctx.L.xcgpu_set_timing(ctx.h, 1)
-    ctx.L.xcgpu_get_timing(ctx.h, None, None)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    dist.barrier()
-    torch.cuda.synchronize()
-    results = []
-    with ClockSampler(dev) as clk:
-        for i in range(args.steps):
-            flush.zero_()
-            ev[i][0].record(stream)
-            results.append(step())
-            ev[i][1].record(stream)
-        torch.cuda.synchronize()
-    dist.barrier()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    import ctypes
-    kms = (ctypes.c_double * 5)()
-    kcnt = (ctypes.c_uint64 * 5)()
-    ctx.L.xcgpu_get_timing(ctx.h, kms, kcnt)
-    ctx.L.xcgpu_set_timing(ctx.h, 0)
-    launches = ctx.kernel_launches - launches0
-    total_ms = dist.max(sum(step_ms))
-    exc, nel = results[-1][1], results[-1][2]
-
-    # end to end through the public API with host buffers (pinned P, V out)
+    out = {"rank": dist.rank, "plan": st, "nspin": nspin, "nbf": nbf, "h2d": Pc.nbytes, "d2h": Pc.nbytes + 16}
+    precs = [("mixed", xcgpu.PREC_MIXED), ("fp64", xcgpu.PREC_FP64)]
+    if args.precision == "fp64":
+        precs = [("fp64", xcgpu.PREC_FP64)]
+    for name, prec in precs:
+        steps = args.steps if name == args.precision or args.precision == "both" else max(3, args.steps // 4)
+        if name == "fp64" and args.precision != "fp64":
+            steps = args.fp64_steps
+        dist.barrier()
+        step_ms, kms, launches, results, clocks = time_builds(ctx, plan, w, P_dev, V_dev, prec, steps, args.warmup,
+                                                              flush, stream, dev)
+        dist.barrier()
+        out[name] = {"step_ms": step_ms, "total_ms": dist.max(sum(step_ms)), "kernel_ms": kms, "launches": launches,
+                     "exc": results[-1][1], "nel": results[-1][2], "V": V_dev.cpu().numpy().copy(), "steps": steps,
+                     "clocks": clocks}
+    # end to end through the public API with host buffers (pinned P in, V, E_xc, N_el out)
+    head = precs[0]
     P_host = torch.from_numpy(Pc).pin_memory()
     V_host = torch.zeros_like(P_host).pin_memory()
     e2e_lat = []
@@ -210,20 +221,15 @@ def run_ours(args, dist):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         exc_h, nel_h = ctypes.c_double(), ctypes.c_double()
-        ctx.check(ctx.L.xcgpu_vxc(plan.h, xcgpu.FUNC[w.func], nspin, prec, 1e-11,
+        ctx.check(ctx.L.xcgpu_vxc(plan.h, xcgpu.FUNC[w.func], nspin, head[1], 1e-11,
                                   ctypes.c_void_p(P_host.data_ptr()), ctypes.c_void_p(V_host.data_ptr()),
                                   ctypes.byref(exc_h), ctypes.byref(nel_h), xcgpu.MEM_HOST))
         t1 = time.perf_counter()
         if i >= args.warmup:
             e2e_lat.append((t1 - t0) * 1e3)
-    e2e_total = dist.max(sum(e2e_lat))
-
-    out = {
-        "rank": dist.rank, "world": dist.world, "plan": st, "step_ms": step_ms, "total_ms": total_ms,
-        "kernel_ms": list(kms), "kernel_launches": list(kcnt), "launches": launches, "exc": exc, "nel": nel,
-        "e2e_ms": e2e_lat, "e2e_total_ms": e2e_total, "clocks": clk.summary(), "nspin": nspin, "nbf": nbf,
-        "V": V_dev.cpu().numpy(), "h2d": Pc.nbytes, "d2h": Pc.nbytes + 16, "exc_e2e": exc_h.value,
-    }
+    out["e2e_ms"] = e2e_lat
+    out["e2e_total_ms"] = dist.max(sum(e2e_lat))
+    out["head"] = head[0]
     return out, (w, P, grid)
 
 
@@ -243,7 +249,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="headline precision; with mixed the FP64 path is timed too for the comparison")
+    ap.add_argument("--fp64-steps", type=int, default=5, help="timed FP64 builds beside a mixed headline")
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -289,66 +297,83 @@ def main():
 
     res, (w, P, grid) = run_ours(args, dist)
     if dist.rank == 0:
+        import torch
         n = res["plan"]["npoints"]
-        steps = args.steps
-        value = dist.world * steps / (res["total_ms"] / 1e3)
-        lat = sorted(res["step_ms"])
-        p50 = float(np.percentile(lat, 50))
-        p99 = float(np.percentile(lat, 99))
         flops = res["plan"]["flops_per_spin"] * res["nspin"]
-        kms = res["kernel_ms"]
+        names = ["eval", "density", "functional", "adder", "other"]
         peaks = measured_peaks()
-        # roofline: dominant kernel class (density or adder); each does half the
-        # algorithmic contraction flops (2 * npts * n_b^2 per spin per block)
-        dom = 3 if kms[3] >= kms[1] else 1
-        dom_ms = kms[dom] / steps
-        achieved = (flops / 2) / (dom_ms / 1e3) / 1e12
-        if args.precision == "mixed":
-            peak = peaks.get("bf16_tflops_sustained")
-            roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": (achieved / peak) if peak else None, "traffic": None,
-                    "note": "algorithmic FP32-equivalent flops of the dominant kernel; peak = measured bf16 "
-                            "cuBLAS sustained (of measured)"}
-        else:
-            import torch
-            peak = fp64_peak_tflops(torch)
-            roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": None,
-                    "note": "FP64 pipe bound (no fast FP64 path on GB300); peak = cuBLAS DGEMM 4096^3 measured "
-                            "in this run (of measured)"}
-        roof["kernel"] = ["eval", "density", "functional", "adder", "other"][dom]
+
+        def summarize(name):
+            r = res[name]
+            steps = r["steps"]
+            value = dist.world * steps / (r["total_ms"] / 1e3)
+            kms = r["kernel_ms"]
+            dom = 3 if kms[3] >= kms[1] else 1
+            dom_ms = kms[dom] / steps
+            achieved = (flops / 2) / (dom_ms / 1e3) / 1e12
+            if name == "mixed":
+                peak = peaks.get("bf16_tflops_sustained")
+                roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": (achieved / peak) if peak else None, "traffic": None,
+                        "note": "useful FP32-equivalent flops (2 npts n_b^2 per block) of the dominant kernel "
+                                "over its CUDA-event time; peak = measured cuBLAS bf16 sustained (of measured). "
+                                "3xTF32 issues 3 TF32 MMAs per product at half the bf16 rate, so its useful "
+                                "ceiling is 1/6 of that peak"}
+            else:
+                peak = fp64_peak_tflops(torch)
+                roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "note": "FP64 pipe bound (GB300 has no fast FP64 path); peak = cuBLAS DGEMM 4096^3 "
+                                "measured in this run (of measured)"}
+            roof["kernel"] = names[dom]
+            lat = r["step_ms"]
+            return {"value": value, "ms_per_step": r["total_ms"] / steps, "mpts_per_s": n * value / 1e6,
+                    "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                    "roofline": roof, "kernel_ms_per_step": {k: v / steps for k, v in zip(names, kms)},
+                    "gpu_launches": r["launches"], "clocks": r["clocks"], "exc": r["exc"], "nel": r["nel"],
+                    "steps": steps}
+
+        head = res["head"]
+        H = summarize(head)
+        other = summarize("fp64") if head == "mixed" else None
         cpu = None
+        acc = {}
+        Vof = lambda r: r["V"].reshape(res["nspin"], w.nbf, w.nbf).transpose(0, 2, 1)
+        if head == "mixed":
+            acc["mixed_vs_fp64_gpu"] = {"dExc": res["mixed"]["exc"] - res["fp64"]["exc"],
+                                        "dNel": res["mixed"]["nel"] - res["fp64"]["nel"],
+                                        "max_dV": float(np.abs(Vof(res["mixed"]) - Vof(res["fp64"])).max())}
         if not args.no_cpu_baseline:
             pts = grid.points()
             dt, Vc, excc, nelc = cpu_baseline(w, P, pts, threads=0)
-            Vg = res["V"].reshape(res["nspin"], w.nbf, w.nbf).transpose(0, 2, 1)
             cpu = {"value": 1.0 / dt, "unit": "builds/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": "one full build of the same workload (grid, P) by the reference-algorithm "
-                             "restatement in oracle/ (FP64, OpenMP over 128-point blocks)",
-                   "dExc_vs_gpu": abs(excc - res["exc"]), "max_dV_vs_gpu": float(np.abs(Vc - Vg).max())}
+                             "restatement in oracle/ (FP64, OpenMP over 128-point blocks)"}
+            for name in ["fp64", "mixed"]:
+                if name in res:
+                    acc["%s_vs_oracle" % name] = {"dExc": res[name]["exc"] - excc, "dNel": res[name]["nel"] - nelc,
+                                                  "max_dV": float(np.abs(Vc - Vof(res[name])).max())}
         line = {
-            "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": args.gpus, "steps": steps,
-            "warmup": args.warmup, "ms_per_step": res["total_ms"] / steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "fp32+tf32x3/f64",
+            "metric": METRIC, "value": H["value"], "unit": "builds/s", "n_gpus": args.gpus, "steps": H["steps"],
+            "warmup": args.warmup, "ms_per_step": H["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if head == "fp64" else "fp32+tf32x3 (f64 functional, sums, Vxc)",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "npoints": n, "nbf": res["nbf"], "nblocks": res["plan"]["nblocks"],
-                       "mean_active": res["plan"]["sum_active"] / res["plan"]["nblocks"],
-                       "precision": args.precision, "parallelism": "replicas" if dist.world > 1 else "single",
+                       "mean_active": res["plan"]["sum_active"] / res["plan"]["nblocks"], "precision": head,
+                       "parallelism": "replicas" if dist.world > 1 else "single",
                        "l2": "flushed between steps (512 MB write, outside the timed events)"},
-            "mpts_per_s": n * value / 1e6,
-            "latency_ms": {"p50": p50, "p99": p99},
-            "roofline": roof,
-            "kernel_ms_per_step": {k: v / steps for k, v in zip(["eval", "density", "functional", "adder", "other"],
-                                                                  kms)},
-            "e2e": {"value": dist.world * steps / (res["e2e_total_ms"] / 1e3), "unit": "builds/s",
+            "mpts_per_s": H["mpts_per_s"], "latency_ms": H["latency_ms"], "roofline": H["roofline"],
+            "kernel_ms_per_step": H["kernel_ms_per_step"],
+            "e2e": {"value": dist.world * len(res["e2e_ms"]) / (res["e2e_total_ms"] / 1e3), "unit": "builds/s",
                     "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
                     "latency_ms": {"p50": float(np.percentile(res["e2e_ms"], 50)),
                                    "p99": float(np.percentile(res["e2e_ms"], 99))}},
-            "gpu_launches": res["launches"],
-            "clocks": res["clocks"],
-            "cpu_baseline": cpu,
-            "exc": res["exc"], "nel": res["nel"],
+            "gpu_launches": H["gpu_launches"], "clocks": H["clocks"], "cpu_baseline": cpu,
+            "fp64_gpu": other, "accuracy": acc, "exc": H["exc"], "nel": H["nel"],
         }
+        if other:
+            line["speedup_mixed_vs_fp64_gpu"] = H["value"] / other["value"]
         print(json.dumps(line))
     dist.close()
 

@@ -179,6 +179,32 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* plan, double block_ave_threshold, int 
 xcgpu_status xcgpu_vxc(xcgpu_plan* plan, int func, int nspin, int precision, double block_ave_threshold,
                        const double* P, double* V, double* Exc, double* Nel, int mem);
 
+/* ---- batched builds (many subsystems, e.g. a freeze-and-thaw step) -------------------
+ * All requests run as one persistent launch per heavy stage (mixed precision) on the
+ * context stream, without host synchronisation unless XCGPU_BATCH_SYNC is set; P, V and
+ * exc_nel are device pointers.  Results are valid once the stream has reached this
+ * point (xcgpu_check_async synchronises and reports a device-side timeout).  The call
+ * can be captured in a CUDA graph (xcgpu_graph_begin/end) once every request's plan has
+ * run one build of the same spin count and functional class (work buffers are allocated
+ * on first use). */
+typedef struct {
+  xcgpu_plan* plan;
+  int func;
+  int nspin;
+  double block_ave_threshold;
+  const double* P; /* device, nspin column-major n_bf x n_bf */
+  double* V;       /* device, overwritten */
+  double* exc_nel; /* device, 2 doubles: E_xc, N_el */
+} xcgpu_request;
+enum { XCGPU_BATCH_SYNC = 1 };
+xcgpu_status xcgpu_vxc_batch(xcgpu_ctx* ctx, const xcgpu_request* reqs, uint32_t n, int precision, int flags);
+xcgpu_status xcgpu_check_async(xcgpu_ctx* ctx);
+/* CUDA graph capture of the work issued on the context stream between begin and end */
+xcgpu_status xcgpu_graph_begin(xcgpu_ctx* ctx);
+xcgpu_status xcgpu_graph_end(xcgpu_ctx* ctx, void** graph_exec);
+xcgpu_status xcgpu_graph_launch(xcgpu_ctx* ctx, void* graph_exec);
+void xcgpu_graph_destroy(void* graph_exec);
+
 #ifdef __cplusplus
 }
 #endif

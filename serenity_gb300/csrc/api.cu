@@ -21,6 +21,28 @@ void DevBuf::release() {
   }
   p = nullptr;
   bytes = 0;
+  if (h) cudaFreeHost(h);
+  h = nullptr;
+  hbytes = 0;
+}
+
+xcgpu_status DevBuf::alloc_host(Ctx* c, size_t n) {
+  if (n <= hbytes && h) return XCGPU_OK;
+  if (h) {
+    // the previous contents may still be read by an in-flight copy
+    cudaStreamSynchronize(c->stream);
+    cudaFreeHost(h);
+  }
+  h = nullptr;
+  hbytes = 0;
+  cudaError_t e = cudaMallocHost(&h, n);
+  if (e != cudaSuccess) {
+    h = nullptr;
+    cudaGetLastError();
+    return c->fail(XCGPU_ERR_NO_MEMORY, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+  }
+  hbytes = n;
+  return XCGPU_OK;
 }
 
 xcgpu_status DevBuf::alloc(Ctx* c, size_t n) {
@@ -143,6 +165,11 @@ xcgpu_status xcgpu_ctx_create(const xcgpu_config* cfg, xcgpu_ctx** out) {
     return XCGPU_ERR_CUDA;
   }
   c->stream = c->own_stream;
+  if (mixed_init(c) != XCGPU_OK) {
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+    return XCGPU_ERR_CUDA;
+  }
   *out = c;
   return XCGPU_OK;
 }
@@ -155,6 +182,9 @@ void xcgpu_ctx_destroy(xcgpu_ctx* c) {
   c->scratch2.release();
   c->partials.release();
   c->skip.release();
+  c->batch_items.release();
+  c->host_items.release();
+  c->aux_by_stream.clear();
   for (auto& pe : c->ev_pending) {
     cudaEventDestroy(pe.second.first);
     cudaEventDestroy(pe.second.second);
@@ -574,6 +604,85 @@ static xcgpu_status to_device(Ctx* c, DevBuf& tmp, const T* src, size_t count, i
   return XCGPU_OK;
 }
 
+struct BuildReq {
+  xcgpu_plan* plan;
+  int func, nspin;
+  double thr;
+  const double* P;
+  double* V;
+  double* exc_nel;
+};
+
+// work buffers of one build, allocated on first use and kept in the plan
+static xcgpu_status ensure_work(xcgpu_plan* P, int nspin, bool gga, bool mixed) {
+  Ctx* c = P->ctx;
+  const long n = P->grid->n;
+  const int nbf = P->basis->nbf;
+  XC_TRY(P->w_rho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  XC_TRY(P->w_epuv.alloc(c, (size_t)n * sizeof(double)));
+  XC_TRY(P->w_dfdrho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  if (gga) {
+    XC_TRY(P->w_grad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+    XC_TRY(P->w_dfdgrad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+  }
+  XC_TRY(P->w_partials.alloc(c, 2 * ((n + 127) / 128) * sizeof(double) + 16));
+  XC_TRY(P->w_skip.alloc(c, (size_t)nspin * P->nblocks + 1));
+  XC_TRY(P->w_fskip.alloc(c, (size_t)(n + kSkipBlock - 1) / kSkipBlock + 1));
+  if (mixed) XC_TRY(P->w_psplit.alloc(c, 2 * (size_t)nspin * nbf * nbf * sizeof(float)));
+  return XCGPU_OK;
+}
+
+// Whole builds (FuncPotential::getMatrix) for a list of requests, all on the context
+// stream without host synchronisation: mixed precision runs one persistent launch per
+// heavy stage over the blocks of every request.
+static xcgpu_status run_builds(Ctx* c, std::vector<BuildReq>& reqs, int precision) {
+  const bool mixed = precision == XCGPU_PREC_MIXED;
+  for (auto& r : reqs) XC_TRY(ensure_work(r.plan, r.nspin, xc::is_gga(r.func), mixed));
+  int* counter = nullptr;
+  XC_TRY(c->aux(&counter));
+  int* err = counter + 2;
+  XC_TRY(c->cuda(cudaMemsetAsync(counter, 0, 4 * sizeof(int), c->stream), "memset aux"));
+  std::vector<MixedWork> work;
+  // 1. rho, grad rho
+  for (auto& r : reqs) {
+    xcgpu_plan* P = r.plan;
+    const bool gga = xc::is_gga(r.func);
+    double* grad = gga ? P->w_grad.as<double>() : nullptr;
+    if (mixed) {
+      XC_TRY(mixed_split(c, r.P, P->w_psplit.as<float>(), (long)r.nspin * P->basis->nbf * P->basis->nbf));
+      work.push_back(MixedWork{&P->basis->dev, &P->dev, r.nspin, P->w_psplit.as<float>(), P->w_rho.as<double>(),
+                               grad, P->w_dfdrho.as<double>(), gga ? P->w_dfdgrad.as<double>() : nullptr,
+                               P->w_skip.as<unsigned char>(), r.V});
+    } else {
+      XC_TRY(stage_density(P, r.nspin, r.P, P->w_rho.as<double>(), grad));
+    }
+  }
+  if (mixed) XC_TRY(mixed_density_batch(c, work, counter, err));
+  // 2. functional, E_xc and N_el, adder skip flags
+  for (auto& r : reqs) {
+    xcgpu_plan* P = r.plan;
+    const bool gga = xc::is_gga(r.func);
+    const long n = P->grid->n;
+    int nparts = 0;
+    XC_TRY(launch_functional(c, r.func, r.nspin, n, kSkipBlock, P->w_rho.as<double>(),
+                             gga ? P->w_grad.as<double>() : nullptr, P->w_epuv.as<double>(),
+                             P->w_dfdrho.as<double>(), gga ? P->w_dfdgrad.as<double>() : nullptr, P->dev.w,
+                             P->w_partials.as<double>(), &nparts, P->w_fskip.as<unsigned char>()));
+    if (nparts) XC_TRY(launch_sum_partials(c, P->w_partials.as<double>(), nparts, 2, r.exc_nel));
+    else XC_TRY(c->cuda(cudaMemsetAsync(r.exc_nel, 0, 2 * sizeof(double), c->stream), "memset sums"));
+    const int nbf = P->basis->nbf;
+    XC_TRY(c->cuda(cudaMemsetAsync(r.V, 0, (size_t)r.nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
+    if (mixed)
+      XC_TRY(launch_block_skip_flags(c, P->dev, r.nspin, P->w_dfdrho.as<double>(),
+                                     gga ? P->w_dfdgrad.as<double>() : nullptr, r.thr, P->w_skip.as<unsigned char>()));
+    else
+      XC_TRY(stage_adder(P, r.nspin, P->w_dfdrho.as<double>(), gga ? P->w_dfdgrad.as<double>() : nullptr, r.thr, r.V));
+  }
+  // 3. Vxc (mixed: one launch for all requests)
+  if (mixed) XC_TRY(mixed_adder_batch(c, work, counter + 1, err));
+  return XCGPU_OK;
+}
+
 }  // namespace xcgpu
 
 extern "C" {
@@ -604,8 +713,11 @@ xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* r
     XC_TRY(P->w_aux.alloc(c, 4 * sizeof(int)));
     XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
     XC_TRY(P->w_psplit.alloc(c, 2 * (size_t)nspin * nbf * nbf * sizeof(float)));
-    XC_TRY(mixed_density(c, P->basis->dev, P->dev, nspin, Pd, P->w_psplit.as<float>(), r, gr, P->w_aux.as<int>(),
-                         P->w_aux.as<int>() + 2));
+    XC_TRY(mixed_split(c, Pd, P->w_psplit.as<float>(), (long)nspin * nbf * nbf));
+    std::vector<MixedWork> work(1);
+    work[0] = MixedWork{&P->basis->dev, &P->dev, nspin, P->w_psplit.as<float>(), r, gr, nullptr, nullptr, nullptr,
+                        nullptr};
+    XC_TRY(mixed_density_batch(c, work, P->w_aux.as<int>(), P->w_aux.as<int>() + 2));
   } else {
     XC_TRY(stage_density(P, nspin, Pd, r, gr));
   }
@@ -646,7 +758,7 @@ xcgpu_status xcgpu_functional(xcgpu_ctx* c, int func, int nspin, uint64_t n, uin
     }
   }
   XC_TRY(launch_functional(c, func, nspin, (long)n, (int)skip_block, dr, gga ? dg : nullptr, e, v, gga ? vg : nullptr,
-                           nullptr, nullptr, nullptr));
+                           nullptr, nullptr, nullptr, nullptr));
   if (mem == XCGPU_MEM_HOST) {
     XC_TRY(c->cuda(cudaMemcpyAsync(epuv, e, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "epuv"));
     XC_TRY(c->cuda(cudaMemcpyAsync(dfdrho, v, (size_t)nspin * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
@@ -685,8 +797,10 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* P, double thr, int nspin, const double
     XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
     XC_TRY(P->w_skip.alloc(c, (size_t)nspin * P->nblocks + 1));
     XC_TRY(launch_block_skip_flags(c, P->dev, nspin, vd, gd, thr, P->w_skip.as<unsigned char>()));
-    XC_TRY(mixed_adder(c, P->basis->dev, P->dev, nspin, vd, gd, P->w_skip.as<unsigned char>(), tmpF.as<double>(),
-                       P->w_aux.as<int>() + 1, P->w_aux.as<int>() + 2));
+    std::vector<MixedWork> work(1);
+    work[0] = MixedWork{&P->basis->dev, &P->dev, nspin, nullptr, nullptr, nullptr, vd, gd,
+                        P->w_skip.as<unsigned char>(), tmpF.as<double>()};
+    XC_TRY(mixed_adder_batch(c, work, P->w_aux.as<int>() + 1, P->w_aux.as<int>() + 2));
     XC_TRY(launch_axpy(c, (long)nspin * nbf * nbf, tmpF.as<double>(), Fd));
   } else {
     XC_TRY(stage_adder(P, nspin, vd, gd, thr, Fd));
@@ -705,10 +819,7 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
   if ((nspin != 1 && nspin != 2) || !Pm || !V) return c->fail(XCGPU_ERR_INVALID, "vxc: bad arguments");
   if (precision != XCGPU_PREC_FP64 && precision != XCGPU_PREC_MIXED)
     return c->fail(XCGPU_ERR_INVALID, "vxc: unknown precision");
-  const bool mixed = precision == XCGPU_PREC_MIXED;
   cudaSetDevice(c->device);
-  const bool gga = xc::is_gga(func);
-  const long n = P->grid->n;
   const int nbf = P->basis->nbf;
   const double* Pd = Pm;
   if (mem == XCGPU_MEM_HOST) {
@@ -720,50 +831,16 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
     XC_TRY(P->w_V.alloc(c, (size_t)nspin * nbf * nbf * sizeof(double)));
     Vd = P->w_V.as<double>();
   }
-  XC_TRY(P->w_rho.alloc(c, (size_t)nspin * n * sizeof(double)));
-  XC_TRY(P->w_epuv.alloc(c, (size_t)n * sizeof(double)));
-  XC_TRY(P->w_dfdrho.alloc(c, (size_t)nspin * n * sizeof(double)));
-  if (gga) {
-    XC_TRY(P->w_grad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
-    XC_TRY(P->w_dfdgrad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
-  }
-  const long nparts_max = (n + 127) / 128;
-  XC_TRY(P->w_partials.alloc(c, 2 * nparts_max * sizeof(double) + 16));
   XC_TRY(P->w_sums.alloc(c, 2 * sizeof(double)));
-  double* rho = P->w_rho.as<double>();
-  double* grad = gga ? P->w_grad.as<double>() : nullptr;
-  double* dfdgrad = gga ? P->w_dfdgrad.as<double>() : nullptr;
-  XC_TRY(P->w_aux.alloc(c, 4 * sizeof(int)));
-  int* counter = P->w_aux.as<int>();
-  int* err = counter + 2;
-  XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
-  // 1. rho, grad rho
-  if (mixed) {
-    XC_TRY(P->w_psplit.alloc(c, 2 * (size_t)nspin * nbf * nbf * sizeof(float)));
-    XC_TRY(mixed_density(c, P->basis->dev, P->dev, nspin, Pd, P->w_psplit.as<float>(), rho, grad, counter, err));
-  }
-  else XC_TRY(stage_density(P, nspin, Pd, rho, grad));
-  // 2. functional + grid sums
-  int nparts = 0;
-  XC_TRY(launch_functional(c, func, nspin, n, kSkipBlock, rho, grad, P->w_epuv.as<double>(),
-                           P->w_dfdrho.as<double>(), dfdgrad, P->dev.w, P->w_partials.as<double>(), &nparts));
-  if (nparts) XC_TRY(launch_sum_partials(c, P->w_partials.as<double>(), nparts, 2, P->w_sums.as<double>()));
-  else XC_TRY(c->cuda(cudaMemsetAsync(P->w_sums.p, 0, 2 * sizeof(double), c->stream), "memset sums"));
-  // 3. Vxc
-  XC_TRY(c->cuda(cudaMemsetAsync(Vd, 0, (size_t)nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
-  if (mixed) {
-    XC_TRY(P->w_skip.alloc(c, (size_t)nspin * P->nblocks + 1));
-    XC_TRY(launch_block_skip_flags(c, P->dev, nspin, P->w_dfdrho.as<double>(), dfdgrad, thr,
-                                   P->w_skip.as<unsigned char>()));
-    XC_TRY(mixed_adder(c, P->basis->dev, P->dev, nspin, P->w_dfdrho.as<double>(), dfdgrad,
-                       P->w_skip.as<unsigned char>(), Vd, counter + 1, err));
-  } else {
-    XC_TRY(stage_adder(P, nspin, P->w_dfdrho.as<double>(), dfdgrad, thr, Vd));
-  }
-  int herr = 0;
-  XC_TRY(c->cuda(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
+  std::vector<BuildReq> reqs(1);
+  reqs[0] = BuildReq{P, func, nspin, thr, Pd, Vd, P->w_sums.as<double>()};
+  XC_TRY(run_builds(c, reqs, precision));
   double hs[2] = {0, 0};
+  int herr = 0;
   XC_TRY(c->cuda(cudaMemcpyAsync(hs, P->w_sums.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "sums"));
+  int* aux = nullptr;
+  XC_TRY(c->aux(&aux));
+  XC_TRY(c->cuda(cudaMemcpyAsync(&herr, aux + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
   if (mem == XCGPU_MEM_HOST)
     XC_TRY(c->cuda(cudaMemcpyAsync(V, Vd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
                    "V"));
@@ -772,6 +849,62 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
   if (Exc) *Exc = hs[0];
   if (Nel) *Nel = hs[1];
   return XCGPU_OK;
+}
+
+xcgpu_status xcgpu_vxc_batch(xcgpu_ctx* c, const xcgpu_request* reqs, uint32_t n, int precision, int flags) {
+  if (!c || (n && !reqs)) return c ? c->fail(XCGPU_ERR_INVALID, "vxc_batch: null argument") : XCGPU_ERR_INVALID;
+  if (precision != XCGPU_PREC_FP64 && precision != XCGPU_PREC_MIXED)
+    return c->fail(XCGPU_ERR_INVALID, "vxc_batch: unknown precision");
+  cudaSetDevice(c->device);
+  std::vector<BuildReq> rq;
+  for (uint32_t i = 0; i < n; ++i) {
+    const xcgpu_request& r = reqs[i];
+    if (!r.plan || r.plan->ctx != c || !xc::is_known(r.func) || (r.nspin != 1 && r.nspin != 2) || !r.P || !r.V ||
+        !r.exc_nel)
+      return c->fail(XCGPU_ERR_INVALID, "vxc_batch: bad request " + std::to_string(i));
+    rq.push_back(BuildReq{r.plan, r.func, r.nspin, r.block_ave_threshold, r.P, r.V, r.exc_nel});
+  }
+  XC_TRY(run_builds(c, rq, precision));
+  if (flags & XCGPU_BATCH_SYNC) return xcgpu_check_async(c);
+  return XCGPU_OK;
+}
+
+xcgpu_status xcgpu_check_async(xcgpu_ctx* c) {
+  if (!c) return XCGPU_ERR_INVALID;
+  int herr = 0;
+  int* aux = nullptr;
+  XC_TRY(c->aux(&aux));
+  XC_TRY(c->cuda(cudaMemcpyAsync(&herr, aux + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "check_async"));
+  if (herr) return c->fail(XCGPU_ERR_TIMEOUT, "a bounded device-side wait gave up (tensor-core pipeline)");
+  return XCGPU_OK;
+}
+
+xcgpu_status xcgpu_graph_begin(xcgpu_ctx* c) {
+  if (!c) return XCGPU_ERR_INVALID;
+  if (c->stream == nullptr) return c->fail(XCGPU_ERR_INVALID, "graph capture needs a non-default stream");
+  return c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+}
+
+xcgpu_status xcgpu_graph_end(xcgpu_ctx* c, void** graph_exec) {
+  if (!c || !graph_exec) return XCGPU_ERR_INVALID;
+  cudaGraph_t g = nullptr;
+  XC_TRY(c->cuda(cudaStreamEndCapture(c->stream, &g), "end capture"));
+  cudaGraphExec_t ge = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  XC_TRY(c->cuda(e, "graph instantiate"));
+  *graph_exec = ge;
+  return XCGPU_OK;
+}
+
+xcgpu_status xcgpu_graph_launch(xcgpu_ctx* c, void* graph_exec) {
+  if (!c || !graph_exec) return XCGPU_ERR_INVALID;
+  return c->cuda(cudaGraphLaunch(static_cast<cudaGraphExec_t>(graph_exec), c->stream), "graph launch");
+}
+
+void xcgpu_graph_destroy(void* graph_exec) {
+  if (graph_exec) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(graph_exec));
 }
 
 }  // extern "C"

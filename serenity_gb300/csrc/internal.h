@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -71,7 +73,10 @@ struct DevBuf {
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf();
-  xcgpu_status alloc(Ctx* c, size_t n);  // no-op if already >= n
+  void* h = nullptr;  // pinned host buffer (alloc_host)
+  size_t hbytes = 0;
+  xcgpu_status alloc(Ctx* c, size_t n);       // device; no-op if already >= n
+  xcgpu_status alloc_host(Ctx* c, size_t n);  // pinned host; no-op if already >= n
   void release();
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
@@ -102,7 +107,18 @@ struct Ctx {
   std::string err;
   int sm_count = 0;
   // reusable scratch
-  DevBuf scratch, scratch2, partials, skip;
+  DevBuf scratch, scratch2, partials, skip, batch_items, host_items;
+  // block counters and the error word of the builds issued on each stream (builds on
+  // different streams may be in flight together)
+  std::map<cudaStream_t, std::unique_ptr<DevBuf>> aux_by_stream;
+  xcgpu_status aux(int** out) {
+    auto& b = aux_by_stream[stream];
+    if (!b) b.reset(new DevBuf());
+    xcgpu_status st = b->alloc(this, 4 * sizeof(int));
+    if (st) return st;
+    *out = b->as<int>();
+    return XCGPU_OK;
+  }
   xcgpu_status fail(xcgpu_status s, const std::string& msg) {
     err = msg;
     return s;
@@ -177,7 +193,7 @@ struct xcgpu_plan {
   bool chunks_ready = false;
   std::vector<int> chunk_bounds;
   long chunk_max_doubles = 0;
-  xcgpu::DevBuf w_psplit, w_slab, w_P, w_V, w_rho, w_grad, w_epuv, w_dfdrho, w_dfdgrad, w_partials, w_sums, w_skip, w_aux;
+  xcgpu::DevBuf w_fskip, w_psplit, w_slab, w_P, w_V, w_rho, w_grad, w_epuv, w_dfdrho, w_dfdgrad, w_partials, w_sums, w_skip, w_aux;
 };
 
 namespace xcgpu {
@@ -197,7 +213,8 @@ xcgpu_status fp64_density_chunk(Ctx* c, const DevPlan& P, int b0, int b1, const 
                                 int nspin, const double* Pm, double* rho, double* grad);
 xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_block, const double* rho,
                                const double* grad, double* epuv, double* dfdrho, double* dfdgrad, const double* w,
-                               double* partials /*2*nparts or null*/, int* nparts);
+                               double* partials /*2*nparts or null*/, int* nparts,
+                               unsigned char* skipbuf /*(n+skip_block-1)/skip_block, or null: context buffer*/);
 xcgpu_status launch_block_skip_flags(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
                                      double thr, unsigned char* skip /*nspin*nblocks*/);
 xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0, long w1, int chunk_b0,
@@ -205,10 +222,24 @@ xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0
                               const double* g, const unsigned char* skip, double* F);
 xcgpu_status launch_axpy(Ctx* c, long n, const double* x, double* y);  // y += x
 xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out /*device*/);
-// mixed precision (tcgen05, 3xTF32): density (rho, grad rho in FP64) and adder (V += D, then V + V^T)
-xcgpu_status mixed_density(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* Pm, float* Psplit,
-                           double* rho, double* grad, int* counter, int* err);
-xcgpu_status mixed_adder(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* v, const double* g,
-                         const unsigned char* skip, double* V, int* counter, int* err);
+// mixed precision (tcgen05, 3xTF32): one persistent launch per stage over the blocks of
+// every build in `work`; density writes rho / grad rho (FP64), the adder accumulates
+// V += D and then symmetrises V <- V + V^T.
+struct MixedWork {
+  const DevBasis* B;
+  const DevPlan* P;
+  int nspin;
+  float* Psplit;  // 2 * nspin * nbf^2 floats
+  double* rho;
+  double* grad;
+  const double* v;
+  const double* g;
+  const unsigned char* skip;
+  double* V;
+};
+xcgpu_status mixed_init(Ctx* c);
+xcgpu_status mixed_split(Ctx* c, const double* Pm, float* Psplit, long n);
+xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
+xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
 
 }  // namespace xcgpu

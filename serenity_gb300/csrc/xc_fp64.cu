@@ -352,24 +352,28 @@ __global__ void __launch_bounds__(128) functional_kernel(int func, int nspin, lo
 
 xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_block, const double* rho,
                                const double* grad, double* epuv, double* dfdrho, double* dfdgrad, const double* w,
-                               double* partials, int* nparts) {
+                               double* partials, int* nparts, unsigned char* skipbuf) {
   if (n == 0) {
     if (nparts) *nparts = 0;
     return XCGPU_OK;
   }
   const int sb = skip_block > 0 ? skip_block : 1 << 30;
   const long nsk = (n + sb - 1) / sb;
-  xcgpu_status st = c->skip.alloc(c, nsk);
-  if (st) return st;
+  xcgpu_status st = XCGPU_OK;
+  unsigned char* skip = skipbuf;
+  if (!skip) {
+    if ((st = c->skip.alloc(c, nsk))) return st;
+    skip = c->skip.as<unsigned char>();
+  }
   KernelTimer kt(c, kFunctional);
   if (skip_block > 0) {
-    skip_flags_kernel<<<(unsigned)nsk, 128, 0, c->stream>>>(n, sb, nspin, rho, c->skip.as<unsigned char>());
+    skip_flags_kernel<<<(unsigned)nsk, 128, 0, c->stream>>>(n, sb, nspin, rho, skip);
     if ((st = c->check_launch("skip_flags_kernel"))) return st;
   } else {
-    if ((st = c->cuda(cudaMemsetAsync(c->skip.p, 0, nsk, c->stream), "memset skip"))) return st;
+    if ((st = c->cuda(cudaMemsetAsync(skip, 0, nsk, c->stream), "memset skip"))) return st;
   }
   const unsigned grid = (unsigned)((n + 127) / 128);
-  functional_kernel<<<grid, 128, 0, c->stream>>>(func, nspin, n, sb, c->skip.as<unsigned char>(), rho, grad, epuv,
+  functional_kernel<<<grid, 128, 0, c->stream>>>(func, nspin, n, sb, skip, rho, grad, epuv,
                                                  dfdrho, dfdgrad, w, partials);
   if (nparts) *nparts = (int)grid;
   return c->check_launch("functional_kernel");

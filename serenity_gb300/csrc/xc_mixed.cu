@@ -17,6 +17,10 @@
 // timeout through the error word instead of hanging.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "basis_eval.cuh"
 #include "internal.h"
 #include "tcgen05.cuh"
@@ -148,13 +152,48 @@ __device__ __forceinline__ void drain64(uint32_t tmem_cols, int warp, int lane, 
   }
 }
 
+// One XC build inside a batched launch: its basis, plan, spin count and buffers.
+struct MxItem {
+  DevBasis B;
+  DevPlan P;
+  int nspin;
+  const float* Phi;  // TF32 split of the density matrices (density kernel)
+  const float* Plo;
+  double* rho;  // outputs of the density kernel
+  double* grad;
+  const double* v;  // inputs of the adder kernel
+  const double* g;
+  const unsigned char* skip;
+  double* V;
+};
+// Up to kMaxItems builds per launch, passed by value as the kernel parameter (no
+// host staging buffer, so launches can be issued back to back and captured in a
+// graph); the blocks of all items form one index space, item i owning
+// [bstart[i], bstart[i+1]).
+constexpr int kMaxItems = 64;
+struct MxBatch {
+  MxItem items[kMaxItems];
+  int bstart[kMaxItems + 1];
+  int nitems;
+  int nblocks;
+};
+
+__device__ __forceinline__ const MxItem& locate(const MxBatch& bt, int gb, int& b) {
+  int lo = 0, hi = bt.nitems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (bt.bstart[mid] <= gb) lo = mid;
+    else hi = mid - 1;
+  }
+  b = gb - bt.bstart[lo];
+  return bt.items[lo];
+}
+
 // =====================================================================================
 // density
 // =====================================================================================
 __global__ void __launch_bounds__(kT, 1)
-    mx_density_kernel(DevBasis B, DevPlan P, int nspin, const float* __restrict__ Phi, const float* __restrict__ Plo,
-                      double* __restrict__ rho, double* __restrict__ grad, int* __restrict__ counter,
-                      int* __restrict__ err) {
+    mx_density_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t mbar[2];
   __shared__ uint32_t tmem_slot;
@@ -179,14 +218,22 @@ __global__ void __launch_bounds__(kT, 1)
   const uint32_t tmem = tmem_slot;
   uint32_t phase[2] = {0, 0};
   int outstanding = -1;  // stage whose commit has not been waited for (-1: none)
-  const int nbf = P.nbf;
 
   for (;;) {
     __syncthreads();
     if (tid == 0) s_block = atomicAdd(counter, 1);
     __syncthreads();
-    const int b = s_block;
-    if (b >= P.nblocks || s_abort) break;
+    const int gb = s_block;
+    if (gb >= bt.nblocks || s_abort) break;
+    int b;
+    const MxItem& I = locate(bt, gb, b);
+    const DevBasis& B = I.B;
+    const DevPlan& P = I.P;
+    const int nspin = I.nspin, nbf = P.nbf;
+    const float* __restrict__ Phi = I.Phi;
+    const float* __restrict__ Plo = I.Plo;
+    double* __restrict__ rho = I.rho;
+    double* __restrict__ grad = I.grad;
     const long first = (long)b * P.max_block;
     const int npts = (int)min((long)P.max_block, P.npoints - first);
     const int nact = P.fn_off[b + 1] - P.fn_off[b];
@@ -357,9 +404,7 @@ done:
 // adder
 // =====================================================================================
 __global__ void __launch_bounds__(kT, 1)
-    mx_adder_kernel(DevBasis B, DevPlan P, int nspin, const double* __restrict__ v, const double* __restrict__ g,
-                    const unsigned char* __restrict__ skip, double* __restrict__ V, int* __restrict__ counter,
-                    int* __restrict__ err) {
+    mx_adder_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t mbar[2];
   __shared__ uint32_t tmem_slot;
@@ -383,14 +428,22 @@ __global__ void __launch_bounds__(kT, 1)
   const uint32_t tmem = tmem_slot;
   uint32_t phase[2] = {0, 0};
   int outstanding = -1;
-  const int nbf = P.nbf;
 
   for (;;) {
     __syncthreads();
     if (tid == 0) s_block = atomicAdd(counter, 1);
     __syncthreads();
-    const int b = s_block;
-    if (b >= P.nblocks || s_abort) break;
+    const int gb = s_block;
+    if (gb >= bt.nblocks || s_abort) break;
+    int b;
+    const MxItem& I = locate(bt, gb, b);
+    const DevBasis& B = I.B;
+    const DevPlan& P = I.P;
+    const int nspin = I.nspin, nbf = P.nbf;
+    const double* __restrict__ v = I.v;
+    const double* __restrict__ g = I.g;
+    const unsigned char* __restrict__ skip = I.skip;
+    double* __restrict__ V = I.V;
     const long first = (long)b * P.max_block;
     const int npts = (int)min((long)P.max_block, P.npoints - first);
     const int nact = P.fn_off[b + 1] - P.fn_off[b];
@@ -438,7 +491,8 @@ __global__ void __launch_bounds__(kT, 1)
             }
           }
           __syncthreads();
-          for (int kc = 0; kc < 4; ++kc) {
+          const int nkp = (npts + 31) / 32;  // 32-point chunks holding live points
+          for (int kc = 0; kc < nkp; ++kc) {
             const int st = kc & 1;
             uint8_t* Ahi = sm + st * kStageBytes;
             uint8_t* Alo = Ahi + kTileA;
@@ -501,17 +555,18 @@ __global__ void __launch_bounds__(kT, 1)
             }
             outstanding = st;
           }
-          // last chunk (kc = 3, stage 1): drain, add the cross terms, scatter into V
+          // last chunk: drain, add the cross terms, scatter into V
           {
-            const bool ok = wait_or_abort(&mbar[1], phase[1], err);
-            phase[1] ^= 1;
+            const int pst = (nkp - 1) & 1;
+            const bool ok = wait_or_abort(&mbar[pst], phase[pst], err);
+            phase[pst] ^= 1;
             outstanding = -1;
             if (__syncthreads_or(!ok)) {
               if (tid == 0) s_abort = 1;
               goto done;
             }
             tc::fence_after_sync();
-            drain64(tmem + kColsHH1, warp, lane, Ds, ld, 64 * (warp >> 2), N, false);
+            drain64(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Ds, ld, 64 * (warp >> 2), N, nkp == 1);
             drain64(tmem + kColsX, warp, lane, Ds, ld, 64 * (warp >> 2), N, false);
             tc::fence_before_sync();
             const int row = 32 * (warp & 3) + lane;
@@ -565,42 +620,78 @@ __global__ void symmetrize_kernel(double* V, int nbf, int nspin) {
 
 static size_t mixed_smem() { return 2 * kStageBytes + 128 * (kNT + 1) * sizeof(float) + 1024; }
 
-xcgpu_status mixed_density(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* Pm, float* Psplit,
-                           double* rho, double* grad, int* counter, int* err) {
-  if (P.nblocks == 0) return XCGPU_OK;
-  const long n = (long)P.nbf * P.nbf * nspin;
-  xcgpu_status st;
-  {
-    KernelTimer kt(c, kOther);
-    split_p_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(Pm, Psplit, Psplit + n, n);
-    if ((st = c->check_launch("split_p_kernel"))) return st;
-  }
-  if ((st = c->cuda(cudaFuncSetAttribute(mx_density_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)mixed_smem()), "density smem attribute")))
-    return st;
-  if ((st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter"))) return st;
-  KernelTimer kt(c, kDensity);
-  mx_density_kernel<<<c->sm_count, kT, mixed_smem(), c->stream>>>(B, P, nspin, Psplit, Psplit + n, rho, grad, counter,
-                                                                  err);
-  return c->check_launch("mx_density_kernel");
+xcgpu_status mixed_init(Ctx* c) {
+  xcgpu_status st = c->cuda(cudaFuncSetAttribute(mx_density_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)mixed_smem()), "density smem attribute");
+  if (st) return st;
+  return c->cuda(cudaFuncSetAttribute(mx_adder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mixed_smem()),
+                 "adder smem attribute");
 }
 
-xcgpu_status mixed_adder(Ctx* c, const DevBasis& B, const DevPlan& P, int nspin, const double* v, const double* g,
-                         const unsigned char* skip, double* V, int* counter, int* err) {
-  if (P.nblocks == 0) return XCGPU_OK;
-  xcgpu_status st = c->cuda(cudaFuncSetAttribute(mx_adder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)mixed_smem()), "adder smem attribute");
-  if (st) return st;
-  if ((st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter"))) return st;
-  {
+static void fill_item(MxItem& it, const MixedWork& w) {
+  it.B = *w.B;
+  it.P = *w.P;
+  it.nspin = w.nspin;
+  const long n = (long)w.P->nbf * w.P->nbf * w.nspin;
+  it.Phi = w.Psplit;
+  it.Plo = w.Psplit ? w.Psplit + n : nullptr;
+  it.rho = w.rho;
+  it.grad = w.grad;
+  it.v = w.v;
+  it.g = w.g;
+  it.skip = w.skip;
+  it.V = w.V;
+}
+
+// parameter blocks for the items [i0, i1) of a batch
+static void make_batch(const std::vector<MixedWork>& work, size_t i0, size_t i1, MxBatch& bt) {
+  bt.nitems = (int)(i1 - i0);
+  bt.bstart[0] = 0;
+  for (size_t i = i0; i < i1; ++i) {
+    fill_item(bt.items[i - i0], work[i]);
+    bt.bstart[i - i0 + 1] = bt.bstart[i - i0] + work[i].P->nblocks;
+  }
+  bt.nblocks = bt.bstart[bt.nitems];
+}
+
+xcgpu_status mixed_split(Ctx* c, const double* Pm, float* Psplit, long n) {
+  KernelTimer kt(c, kOther);
+  split_p_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(Pm, Psplit, Psplit + n, n);
+  return c->check_launch("split_p_kernel");
+}
+
+xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
+  static thread_local MxBatch bt;  // host-side parameter block (the launch copies it)
+  for (size_t i0 = 0; i0 < work.size(); i0 += kMaxItems) {
+    make_batch(work, i0, std::min(work.size(), i0 + kMaxItems), bt);
+    if (bt.nblocks == 0) continue;
+    xcgpu_status st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter");
+    if (st) return st;
+    KernelTimer kt(c, kDensity);
+    mx_density_kernel<<<c->sm_count, kT, mixed_smem(), c->stream>>>(bt, counter, err);
+    if ((st = c->check_launch("mx_density_kernel"))) return st;
+  }
+  return XCGPU_OK;
+}
+
+xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
+  static thread_local MxBatch bt;
+  xcgpu_status st = XCGPU_OK;
+  for (size_t i0 = 0; i0 < work.size(); i0 += kMaxItems) {
+    make_batch(work, i0, std::min(work.size(), i0 + kMaxItems), bt);
+    if (bt.nblocks == 0) continue;
+    if ((st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter"))) return st;
     KernelTimer kt(c, kAdder);
-    mx_adder_kernel<<<c->sm_count, kT, mixed_smem(), c->stream>>>(B, P, nspin, v, g, skip, V, counter, err);
+    mx_adder_kernel<<<c->sm_count, kT, mixed_smem(), c->stream>>>(bt, counter, err);
     if ((st = c->check_launch("mx_adder_kernel"))) return st;
   }
   KernelTimer kt2(c, kOther);
-  const long n = (long)P.nbf * P.nbf * nspin;
-  symmetrize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(V, P.nbf, nspin);
-  return c->check_launch("symmetrize_kernel");
+  for (const auto& w : work) {
+    const long n = (long)w.P->nbf * w.P->nbf * w.nspin;
+    symmetrize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(w.V, w.P->nbf, w.nspin);
+    if ((st = c->check_launch("symmetrize_kernel"))) return st;
+  }
+  return XCGPU_OK;
 }
 
 }  // namespace xcgpu

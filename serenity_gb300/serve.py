@@ -1,0 +1,226 @@
+"""Request loop for Vxc builds with continuous batching under an HBM budget.
+
+Requests (geometry, basis, functional, density matrix) arrive over time.  The loop
+keeps grids, bases and plans resident across repeat geometries (an LRU cache counted
+against the budget), admits waiting requests into the next batch as in-flight
+batches retire and memory frees up, and runs each batch as one persistent launch per
+heavy stage (``xcgpu_vxc_batch``).  Batches alternate between compute streams so the
+next batch's kernels start on SMs the previous batch's tail leaves idle, and the
+setup of new geometries (grid, screening) runs on its own stream while batches
+compute.  Latency is measured from a request's arrival to the completion of its batch.
+"""
+import collections
+import math
+import time
+
+import numpy as np
+
+from . import workload as wl
+from . import xcgpu
+
+
+class Request:
+    __slots__ = ("rid", "arrival", "key", "workload", "P_dev", "V_dev", "en_dev", "func", "done", "latency",
+                 "nbytes", "plan_slot", "exc", "nel")
+
+    def __init__(self, rid, arrival, key, workload, P_dev, func):
+        self.rid, self.arrival, self.key, self.workload = rid, arrival, key, workload
+        self.P_dev, self.func = P_dev, func
+        self.V_dev = self.en_dev = None
+        self.done = None
+        self.latency = None
+        self.exc = self.nel = None
+
+
+def _work_bytes(npts, nbf, nspin, gga, nblocks):
+    per_point = 8 * (nspin * (1 + (3 if gga else 0)) * 2 + 1) + 32
+    return npts * per_point + nspin * nbf * nbf * (8 + 8) + nblocks * 64
+
+
+class Resident:
+    """Grid + basis of one geometry and its plan instances (one per concurrent use)."""
+
+    def __init__(self, ctx, w):
+        self.grid = xcgpu.Grid.build(ctx, w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
+        self.basis = xcgpu.Basis(ctx, w.shells)
+        self.plans = []
+        self.busy = set()
+        self.ctx = ctx
+        self.S = None
+
+    def plan(self):
+        for i, p in enumerate(self.plans):
+            if i not in self.busy:
+                self.busy.add(i)
+                return i, p
+        p = xcgpu.Plan(self.ctx, self.grid, self.basis, 128, 1e-9)
+        self.plans.append(p)
+        self.busy.add(len(self.plans) - 1)
+        return len(self.plans) - 1, p
+
+    def release(self, i):
+        self.busy.discard(i)
+
+
+class Server:
+    def __init__(self, ctx, hbm_budget, precision=xcgpu.PREC_MIXED, max_batch=64, nstreams=2):
+        import torch
+        self.torch = torch
+        self.ctx = ctx
+        self.budget = hbm_budget
+        self.precision = precision
+        self.max_batch = max_batch
+        self.streams = [torch.cuda.Stream() for _ in range(nstreams)]
+        self.setup_stream = torch.cuda.Stream()
+        self.cache = collections.OrderedDict()
+        self.inflight = []
+        self.reserved = 0
+
+    # -- resident data --------------------------------------------------------------------
+    def resident(self, key, w):
+        r = self.cache.get(key)
+        if r is None:
+            self.ctx.set_stream(self.setup_stream.cuda_stream)
+            r = Resident(self.ctx, w)
+            self.cache[key] = r
+        self.cache.move_to_end(key)
+        return r
+
+    def _evict(self):
+        while self.ctx.bytes_in_use + self.reserved > self.budget and self.cache:
+            key, r = next(iter(self.cache.items()))
+            if r.busy:
+                self.cache.move_to_end(key)
+                if all(x.busy for x in self.cache.values()):
+                    return
+                continue
+            self.cache.pop(key)
+
+    # -- batches --------------------------------------------------------------------------
+    def _launch(self, batch, stream):
+        torch = self.torch
+        items = []
+        with torch.cuda.stream(stream):
+            for rq in batch:
+                w = rq.workload
+                rq.V_dev = torch.empty_like(rq.P_dev)
+                rq.en_dev = torch.empty(2, dtype=torch.float64, device="cuda")
+                items.append((rq.plan_slot[1], rq.func, rq.P_dev, rq.V_dev, rq.en_dev))
+        self.ctx.set_stream(stream.cuda_stream)
+        self.ctx.vxc_batch(items, self.precision)
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        self.inflight.append((batch, ev, stream))
+
+    def _retire(self, now_fn):
+        keep = []
+        for batch, ev, stream in self.inflight:
+            if ev.query():
+                self.ctx.set_stream(stream.cuda_stream)
+                self.ctx.check_async()
+                t = now_fn()
+                for rq in batch:
+                    rq.done = t
+                    rq.latency = t - rq.arrival
+                    r, (i, _) = self.cache.get(rq.key), rq.plan_slot
+                    if r is not None:
+                        r.release(i)
+                    self.reserved -= rq.nbytes
+                yield batch
+            else:
+                keep.append((batch, ev, stream))
+        self.inflight = keep
+
+    def run(self, requests, on_complete=None):
+        """Serve requests (sorted by arrival, seconds from start).  Returns stats."""
+        pending = collections.deque()
+        todo = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0  # noqa: E731
+        sidx = 0
+        completed = 0
+        while todo or pending or self.inflight:
+            t = now()
+            while todo and todo[0].arrival <= t:
+                pending.append(todo.popleft())
+            for batch in self._retire(now):
+                completed += len(batch)
+                if on_complete:
+                    on_complete(batch)
+            if pending and len(self.inflight) < len(self.streams):
+                batch = []
+                while pending and len(batch) < self.max_batch:
+                    rq = pending[0]
+                    w = rq.workload
+                    r = self.resident(rq.key, w)
+                    slot = r.plan()
+                    st = slot[1].stats()
+                    rq.nbytes = _work_bytes(st["npoints"], w.nbf, w.nspin, True, st["nblocks"])
+                    self._evict()
+                    if batch and self.ctx.bytes_in_use + self.reserved + rq.nbytes > self.budget:
+                        r.release(slot[0])
+                        break
+                    rq.plan_slot = slot
+                    self.reserved += rq.nbytes
+                    batch.append(pending.popleft())
+                if batch:
+                    self._launch(batch, self.streams[sidx % len(self.streams)])
+                    sidx += 1
+                    continue
+            if not self.inflight and todo and not pending:
+                time.sleep(max(0.0, min(0.001, todo[0].arrival - now())))
+            else:
+                time.sleep(0.0002)
+        total = now()
+        lat = np.array([r.latency for r in requests])
+        return {"requests": len(requests), "wall_s": total, "throughput_req_s": len(requests) / total,
+                "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "mean_ms": float(lat.mean() * 1e3), "batches": sidx, "resident_geometries": len(self.cache)}
+
+
+def density_on_gpu(S_dev, nocc, seed):
+    """Random orthonormalised density P = 2 C C^T (restricted) on the GPU, column-major."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    n = S_dev.shape[0]
+    C = torch.randn(n, nocc, generator=g, device="cuda", dtype=torch.float64)
+    M = C.T @ S_dev @ C
+    e, U = torch.linalg.eigh(M)
+    C = C @ (U * e.rsqrt()) @ U.T
+    P = 2.0 * C @ C.T
+    return P.T.contiguous().reshape(1, n, n)
+
+
+def overlap_on_gpu(ctx, resident, n):
+    """Overlap matrix of a resident geometry by grid integration (adder with v = 1)."""
+    import torch
+    if resident.S is None:
+        plan = resident.plans[0] if resident.plans else xcgpu.Plan(ctx, resident.grid, resident.basis, 128, 1e-9)
+        if not resident.plans:
+            resident.plans.append(plan)
+        S = plan.add_scalar(np.ones(resident.grid.n), block_ave_threshold=0.0, precision=xcgpu.PREC_MIXED)[0]
+        resident.S = torch.from_numpy(np.ascontiguousarray(S)).cuda()
+    return resident.S
+
+
+def make_requests(server, n=2000, rate=200.0, seed=0, max_waters=128, n_rad=50, n_ang=194):
+    """Poisson stream: sizes 1..max_waters log-uniform, def2-SVP / def2-TZVP 70/30, LDA / PBE
+    50/50, each with its own random orthonormalised P (generated on the GPU up front)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    reqs = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        m = int(round(math.exp(rng.uniform(0.0, math.log(max_waters)))))
+        basis = "DEF2-SVP" if rng.uniform() < 0.7 else "DEF2-TZVP"
+        func = "LDA" if rng.uniform() < 0.5 else "PBE"
+        key = (m, basis)
+        sym, xyz = wl.water_cluster(m, seed=1000 + m, jitter=0.2)
+        w = wl.Workload(sym, xyz, basis, func, 5 * m, n_rad, n_ang, seed)
+        r = server.resident(key, w)
+        S = overlap_on_gpu(server.ctx, r, w.nbf)
+        P = density_on_gpu(S, 5 * m, seed * 100000 + i)
+        reqs.append(Request(i, t, key, w, P, func))
+    server.ctx.set_stream(server.streams[0].cuda_stream)
+    return reqs

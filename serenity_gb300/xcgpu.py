@@ -38,6 +38,12 @@ class Shell(ctypes.Structure):
                 ("coef", ctypes.POINTER(ctypes.c_double))]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("plan", ctypes.c_void_p), ("func", ctypes.c_int), ("nspin", ctypes.c_int),
+                ("block_ave_threshold", ctypes.c_double), ("P", ctypes.c_void_p), ("V", ctypes.c_void_p),
+                ("exc_nel", ctypes.c_void_p)]
+
+
 class PlanStats(ctypes.Structure):
     _fields_ = [("nblocks", ctypes.c_uint32), ("max_block", ctypes.c_uint32), ("nbf", ctypes.c_uint32),
                 ("max_active", ctypes.c_uint32), ("npoints", ctypes.c_uint64), ("sum_active", ctypes.c_uint64),
@@ -92,6 +98,17 @@ def library(build_if_needed=True):
     L.xcgpu_functional_is_gga.argtypes = [S]
     L.xcgpu_add_scalar.argtypes = [vp, ctypes.c_double, S, vp, vp, vp, S, S]
     L.xcgpu_vxc.argtypes = [vp, S, S, S, ctypes.c_double, vp, vp, dp, dp, S]
+    L.xcgpu_vxc_batch.argtypes = [vp, ctypes.POINTER(Request), ctypes.c_uint32, S, S]
+    L.xcgpu_check_async.argtypes = [vp]
+    L.xcgpu_graph_begin.argtypes = [vp]
+    L.xcgpu_graph_end.argtypes = [vp, ctypes.POINTER(vp)]
+    L.xcgpu_graph_launch.argtypes = [vp, vp]
+    L.xcgpu_graph_destroy.argtypes = [vp]
+    L.xcgpu_set_timing.argtypes = [vp, S]
+    L.xcgpu_get_timing.argtypes = [vp, vp, vp]
+    for name in ["xcgpu_vxc_batch", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
+                 "xcgpu_graph_launch", "xcgpu_set_timing", "xcgpu_get_timing"]:
+        getattr(L, name).restype = S
     for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
                  "xcgpu_grid_copy", "xcgpu_basis_create", "xcgpu_basis_coefs", "xcgpu_plan_create",
                  "xcgpu_plan_get_stats", "xcgpu_block_on_grid", "xcgpu_density", "xcgpu_functional",
@@ -160,6 +177,34 @@ class Context:
     @property
     def kernel_launches(self):
         return int(self.L.xcgpu_kernel_launches(self.h))
+
+    def vxc_batch(self, items, precision=PREC_MIXED, sync=False):
+        """items: list of (plan, func, P_dev, V_dev, exc_nel_dev) with device tensors
+        (P, V column-major per spin); all builds run in one persistent launch per stage."""
+        arr = (Request * len(items))()
+        for i, (plan, func, P, V, en) in enumerate(items):
+            nspin = P.numel() // (plan.nbf * plan.nbf)
+            arr[i] = Request(plan.h.value if isinstance(plan.h, ctypes.c_void_p) else plan.h,
+                             FUNC[func] if isinstance(func, str) else int(func), nspin, 1e-11,
+                             P.data_ptr(), V.data_ptr(), en.data_ptr())
+        self.check(self.L.xcgpu_vxc_batch(self.h, arr, len(items), precision, 1 if sync else 0))
+
+    def check_async(self):
+        self.check(self.L.xcgpu_check_async(self.h))
+
+    def graph_begin(self):
+        self.check(self.L.xcgpu_graph_begin(self.h))
+
+    def graph_end(self):
+        g = vp()
+        self.check(self.L.xcgpu_graph_end(self.h, ctypes.byref(g)))
+        return g
+
+    def graph_launch(self, g):
+        self.check(self.L.xcgpu_graph_launch(self.h, g))
+
+    def graph_destroy(self, g):
+        self.L.xcgpu_graph_destroy(g)
 
     def functional(self, func, rho, grad=None, skip_block=128):
         """FunctionalLibrary::calcData(GRADIENTS, ., order 1) on host arrays
