@@ -159,6 +159,17 @@ void xcgpu_plan_destroy(xcgpu_plan* plan);
  * precision: XCGPU_PREC_FP64 (the drop-in) or XCGPU_PREC_MIXED (3xTF32 tensor cores). */
 xcgpu_status xcgpu_density(xcgpu_plan* plan, int nspin, const double* P, double* rho, double* grad, int precision,
                            int mem);
+/* FP64 rho and grad rho without any device allocation.  No counterpart in the reference:
+ * it serves hosts that cannot call cudaMalloc when they need the density (a program that
+ * owns all device memory through its own fixed pool, or a loop whose memory was reserved
+ * up front).  Same kernels and results as xcgpu_density at XCGPU_PREC_FP64; the per-block
+ * scratch lives in a fixed 64 MiB static device array that every GPU loading the library
+ * holds until exit, so a block needing more (more than ~16 000 active functions) is
+ * rejected with XCGPU_ERR_BUDGET.  P, rho, grad (may be NULL) are device pointers; the call
+ * synchronises the context stream.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
+ * share the array, so calls that overlap on the GPU race. */
+xcgpu_status xcgpu_density_fp64_noalloc(xcgpu_plan* plan, int nspin, const double* P, double* rho, double* grad);
 /* FunctionalLibrary::calcData(GRADIENTS, f, ., order 1) (FunctionalLibrary.cpp:40-71,
  * XCFun.cpp:39-158): epuv (energy per volume), dF/drho and, for GGAs, dF/d(grad rho).
  * skip_block > 0 applies the reference's block skip (sum |rho| < n * 1e-12 on blocks of
