@@ -460,6 +460,7 @@ xcgpu_status xcgpu_plan_create(xcgpu_ctx* c, xcgpu_grid* g, xcgpu_basis* B, uint
   DevPlan& d = P->dev;
   d.nblocks = nb;
   d.max_block = P->max_block;
+  d.max_active = P->max_active;
   d.nbf = B->nbf;
   d.npoints = g->n;
   d.xyz = g->xyz.as<double>();
@@ -604,6 +605,14 @@ static xcgpu_status to_device(Ctx* c, DevBuf& tmp, const T* src, size_t count, i
   return XCGPU_OK;
 }
 
+// status for the error word of the mixed-precision kernels (0: none)
+static xcgpu_status device_error(Ctx* c, int herr, const char* where) {
+  if (herr == 0) return XCGPU_OK;
+  if (herr == 2)
+    return c->fail(XCGPU_ERR_INVALID, std::string(where) + ": a block needs more basis scratch than was sized for it");
+  return c->fail(XCGPU_ERR_TIMEOUT, std::string(where) + ": a bounded device-side wait gave up (tensor-core pipeline)");
+}
+
 struct BuildReq {
   xcgpu_plan* plan;
   int func, nspin;
@@ -727,7 +736,12 @@ xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* r
       XC_TRY(c->cuda(cudaMemcpyAsync(grad, gr, (size_t)nspin * 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
                      "grad"));
   }
-  return c->cuda(cudaStreamSynchronize(c->stream), "density");
+  int herr = 0;
+  if (precision == XCGPU_PREC_MIXED)
+    XC_TRY(c->cuda(cudaMemcpyAsync(&herr, P->w_aux.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
+                   "error word"));
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "density"));
+  return device_error(c, herr, "density");
 }
 
 xcgpu_status xcgpu_functional(xcgpu_ctx* c, int func, int nspin, uint64_t n, uint32_t skip_block, const double* rho,
@@ -808,7 +822,12 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* P, double thr, int nspin, const double
   if (mem == XCGPU_MEM_HOST)
     XC_TRY(c->cuda(cudaMemcpyAsync(F, Fd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
                    "F"));
-  return c->cuda(cudaStreamSynchronize(c->stream), "add_scalar");
+  int herr = 0;
+  if (precision == XCGPU_PREC_MIXED)
+    XC_TRY(c->cuda(cudaMemcpyAsync(&herr, P->w_aux.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
+                   "error word"));
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "add_scalar"));
+  return device_error(c, herr, "add_scalar");
 }
 
 xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double thr, const double* Pm, double* V,
@@ -845,7 +864,7 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* P, int func, int nspin, int precision, double
     XC_TRY(c->cuda(cudaMemcpyAsync(V, Vd, (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
                    "V"));
   XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "vxc"));
-  if (herr) return c->fail(XCGPU_ERR_TIMEOUT, "vxc: a bounded device-side wait gave up (tensor-core pipeline)");
+  if (herr) return device_error(c, herr, "vxc");
   if (Exc) *Exc = hs[0];
   if (Nel) *Nel = hs[1];
   return XCGPU_OK;
@@ -876,7 +895,7 @@ xcgpu_status xcgpu_check_async(xcgpu_ctx* c) {
   XC_TRY(c->aux(&aux));
   XC_TRY(c->cuda(cudaMemcpyAsync(&herr, aux + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
   XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "check_async"));
-  if (herr) return c->fail(XCGPU_ERR_TIMEOUT, "a bounded device-side wait gave up (tensor-core pipeline)");
+  if (herr) return device_error(c, herr, "check_async");
   return XCGPU_OK;
 }
 

@@ -51,6 +51,7 @@ struct __align__(16) ShellRec {
 // Device-side block table of a plan.
 struct DevPlan {
   int nblocks = 0, max_block = 0, nbf = 0;
+  int max_active = 0;              // largest active-function count of the blocks
   long npoints = 0;
   const double* xyz = nullptr;     // [3*npoints]
   const double* w = nullptr;       // [npoints]
@@ -111,6 +112,8 @@ struct Ctx {
   // block counters and the error word of the builds issued on each stream (builds on
   // different streams may be in flight together)
   std::map<cudaStream_t, std::unique_ptr<DevBuf>> aux_by_stream;
+  // per-CTA basis scratch of the mixed-precision kernels, per stream
+  std::map<cudaStream_t, std::unique_ptr<DevBuf>> mixed_by_stream;
   xcgpu_status aux(int** out) {
     auto& b = aux_by_stream[stream];
     if (!b) b.reset(new DevBuf());

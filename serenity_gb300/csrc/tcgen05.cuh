@@ -105,6 +105,22 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parit
   }
 }
 
+// mbarrier arrival that also announces `bytes` of bulk-copy transactions
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+// bulk copy (TMA, non-tensor) global -> shared, completing on an mbarrier; both
+// addresses 16-byte aligned, size a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(gmem_src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+// order this thread's generic-proxy global writes before later async-proxy (TMA) reads
+__device__ __forceinline__ void fence_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
 // 32 lanes x 32 columns of FP32 from TMEM: thread i of the warp gets row
 // (lane base + i), columns [col, col + 32).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {

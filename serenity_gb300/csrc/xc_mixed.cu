@@ -29,7 +29,8 @@ namespace xcgpu {
 
 constexpr uint32_t kTileA = 128 * 128;  // bytes of a 128-row x 32-element operand tile
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
-constexpr int kErrTimeout = 1;
+constexpr int kErrTimeout = 1;  // error word values (read by the host after a build)
+constexpr int kErrScratch = 2;
 
 // Point coordinates as FP32 high part + remainder; with the shell records' split
 // centres, x = (p_hi - A_hi) + (p_lo - A_lo) carries FP32 relative accuracy of p - A.
@@ -66,9 +67,10 @@ __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float2* __
     const float2 ac = __ldg(prim2 + r.prim0 + i);
     const float t = ac.x * r2;
     if (t < expthr) {
-      const float e = ac.y * expf(-t);
-      Rv += e;
-      if (DERIV >= 1) dR -= 2.f * ac.x * e;
+      // explicit roundings: R comes out bit-identical whether or not dR is formed
+      const float e = __fmul_rn(ac.y, expf(-t));
+      Rv = __fadd_rn(Rv, e);
+      if (DERIV >= 1) dR = fmaf(-2.f * ac.x, e, dR);
     }
   }
   const int l = rec_l(r.info);
@@ -108,31 +110,32 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* mbar, uint32_t parity, i
   return ok;
 }
 
-// Pipeline shared by both kernels (256 threads, 8 warps, one CTA per SM):
-//   per K-chunk of 32: fill operand stage (kc & 1) -> wait for the MMAs of chunk kc-1
-//   -> drain its hi*hi accumulator into an FP32 (round-to-nearest) sum in shared
-//   memory -> issue chunk kc: hi*hi into a fresh TMEM accumulator (kc & 1), the two
-//   cross products into one accumulator for the whole pass.
-// Keeping every hi*hi accumulation chain to 4 MMAs (and the small cross terms in
-// their own accumulator) bounds the bias of the tensor core's truncating FP32
-// accumulation; long chains over all K gave a relative density bias of -6e-7.
-// TMEM columns: hh0 [0,128), hh1 [128,256), cross [256,384).
+// Tensor-memory layout (512 columns per CTA): two hi*hi accumulators used in turn by
+// consecutive 32-wide K chunks, and two cross-term accumulators used in turn by
+// consecutive output tiles.  A fresh hi*hi accumulator per chunk keeps every chain of
+// the tensor core's truncating FP32 accumulation at 4 MMAs; the chunk results are then
+// summed in round-to-nearest FP32 on the CUDA cores (one long chain over all K gave a
+// relative density bias of -6e-7).  The cross terms (~2^-11 smaller) stay in one
+// accumulator per tile.
 constexpr int kT = 256;
-constexpr int kNT = 128;  // functions per pass / tile (N), and rows of an M tile
-constexpr uint32_t kStageBytes = 4 * kTileA;  // A_hi, A_lo, B_hi, B_lo (128 rows each)
-constexpr uint32_t kColsHH0 = 0, kColsHH1 = 128, kColsX = 256;
+constexpr int kNT = 128;                      // rows of an operand tile (M, and N at most)
+constexpr uint32_t kStageBytes = 4 * kTileA;  // A_hi, A_lo, B_hi, B_lo
+constexpr uint32_t kColsHH0 = 0, kColsHH1 = 128, kColsX0 = 256, kColsX1 = 384;
+constexpr int kTileFloats = 128 * 32;         // one operand tile (hi or lo) in floats
+constexpr int kAdderStages = 3;
 
-// hi*hi (fresh per chunk) + cross terms for one 32-wide K chunk
+// hi*hi of one 32-wide K chunk into a fresh accumulator, the two cross products into
+// the tile's cross accumulator
 __device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl, int N,
-                                            int hh_cols, bool first_chunk) {
+                                            uint32_t hh_cols, uint32_t x_cols, bool first_chunk) {
   const uint32_t idesc = tc::idesc_tf32(128, N);
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks) {
     const uint32_t o = ks * 32;
     tc::mma_tf32(tmem + hh_cols, tc::smem_desc_sw128(ah + o), tc::smem_desc_sw128(bh + o), idesc, ks > 0 ? 1u : 0u);
-    tc::mma_tf32(tmem + kColsX, tc::smem_desc_sw128(ah + o), tc::smem_desc_sw128(bl + o), idesc,
+    tc::mma_tf32(tmem + x_cols, tc::smem_desc_sw128(ah + o), tc::smem_desc_sw128(bl + o), idesc,
                  (!first_chunk || ks > 0) ? 1u : 0u);
-    tc::mma_tf32(tmem + kColsX, tc::smem_desc_sw128(al + o), tc::smem_desc_sw128(bh + o), idesc, 1u);
+    tc::mma_tf32(tmem + x_cols, tc::smem_desc_sw128(al + o), tc::smem_desc_sw128(bh + o), idesc, 1u);
   }
 }
 
@@ -152,6 +155,30 @@ __device__ __forceinline__ void drain64(uint32_t tmem_cols, int warp, int lane, 
   }
 }
 
+// add (or store) this warp's 32 lanes x 64 columns [64 (warp >> 2), +64) of a TMEM
+// accumulator into registers
+__device__ __forceinline__ void drain_regs(uint32_t tmem_cols, int warp, float* acc, bool store, int N) {
+  const int c0 = 64 * (warp >> 2);
+  const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    if (c0 + 32 * h < N) {  // warp-uniform
+      float v[32];
+      tc::tmem_ld32(tmem_cols + lanes + (uint32_t)(c0 + 32 * h), v);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) acc[32 * h + i] = store ? v[i] : acc[32 * h + i] + v[i];
+    }
+  }
+}
+
+// split v into TF32 hi (at t[0]) and lo (at t[kTileFloats])
+__device__ __forceinline__ void st_split(float* t, float v) {
+  uint32_t h, l;
+  tc::split_tf32(v, h, l);
+  t[0] = __uint_as_float(h);
+  t[kTileFloats] = __uint_as_float(l);
+}
+
 // One XC build inside a batched launch: its basis, plan, spin count and buffers.
 struct MxItem {
   DevBasis B;
@@ -169,14 +196,19 @@ struct MxItem {
 // Up to kMaxItems builds per launch, passed by value as the kernel parameter (no
 // host staging buffer, so launches can be issued back to back and captured in a
 // graph); the blocks of all items form one index space, item i owning
-// [bstart[i], bstart[i+1]).
+// [bstart[i], bstart[i+1]).  Each CTA owns `cta_floats` floats of `scratch` for the
+// basis values of the block it works on.
 constexpr int kMaxItems = 64;
 struct MxBatch {
   MxItem items[kMaxItems];
   int bstart[kMaxItems + 1];
   int nitems;
   int nblocks;
+  float* scratch;
+  long cta_floats;
+  int ft_max;  // 128-function tiles of the largest block (adder scratch layout)
 };
+static_assert(sizeof(MxBatch) <= 32764, "kernel parameter block too large");
 
 __device__ __forceinline__ const MxItem& locate(const MxBatch& bt, int gb, int& b) {
   int lo = 0, hi = bt.nitems - 1;
@@ -191,7 +223,15 @@ __device__ __forceinline__ const MxItem& locate(const MxBatch& bt, int gb, int& 
 
 // =====================================================================================
 // density
+//   1. every active shell of the block is evaluated once (value and, for GGA, gradient)
+//      into the CTA's scratch, FP32, [component][function][128 points];
+//   2. per pass of <= 128 functions nu: X = Phi P_b over K chunks of 32 functions mu,
+//      A = Phi (points x mu) split from the scratch, B = P_b (nu x mu) gathered from the
+//      pre-split density matrix (rows of P_b by symmetry, one warp per row);
+//   3. rho_p += sum_nu X_p,nu phi_nu(p), grad rho_p += 2 sum_nu X_p,nu grad phi_nu(p),
+//      reading phi and grad phi back from the scratch.
 // =====================================================================================
+template <int DERIV>
 __global__ void __launch_bounds__(kT, 1)
     mx_density_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
@@ -218,6 +258,7 @@ __global__ void __launch_bounds__(kT, 1)
   const uint32_t tmem = tmem_slot;
   uint32_t phase[2] = {0, 0};
   int outstanding = -1;  // stage whose commit has not been waited for (-1: none)
+  float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
 
   for (;;) {
     __syncthreads();
@@ -230,28 +271,53 @@ __global__ void __launch_bounds__(kT, 1)
     const DevBasis& B = I.B;
     const DevPlan& P = I.P;
     const int nspin = I.nspin, nbf = P.nbf;
-    const float* __restrict__ Phi = I.Phi;
-    const float* __restrict__ Plo = I.Plo;
     double* __restrict__ rho = I.rho;
     double* __restrict__ grad = I.grad;
     const long first = (long)b * P.max_block;
     const int npts = (int)min((long)P.max_block, P.npoints - first);
     const int nact = P.fn_off[b + 1] - P.fn_off[b];
-    const int* fn = P.fn_list + P.fn_off[b];
+    const int* __restrict__ fn = P.fn_list + P.fn_off[b];
     const int s0 = P.sh_off[b], s1 = P.sh_off[b + 1];
+    if (4L * nact * 128 > bt.cta_floats) {  // scratch sized for a smaller block: report, skip
+      if (tid == 0) atomicExch(err, kErrScratch);
+      continue;
+    }
     const bool live = p < npts;
-    const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
-    const ShellRec* recs = P.rec;
-    const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
+    const long cs = (long)nact * 128;  // component stride of the scratch
+    // ---- 1. basis values (and gradients) of the block ----
+    {
+      const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
+      const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
+      float* const col = my + p;
+      for (int si = s0 + half; si < s1; si += 2) {
+        const ShellRec r = load_rec(P.rec + si);
+        float* const t0 = col + (long)rec_f0(r.info) * 128;
+        auto put = [&](int f, float v, float dx, float dy, float dz) {
+          float* t = t0 + f * 128;
+          t[0] = v;
+          if (DERIV) {
+            t[cs] = dx;
+            t[2 * cs] = dy;
+            t[3 * cs] = dz;
+          }
+        };
+        if (live) {
+          shell_rec_at<DERIV>(r, B.prim2, pt, expthr, thr, put);
+        } else {
+          const int nf = rec_nf(r.info);
+          for (int f = 0; f < nf; ++f) put(f, 0.f, 0.f, 0.f, 0.f);
+        }
+      }
+    }
+    __syncthreads();
     for (int s = 0; s < nspin; ++s) {
-      const float* Ph = Phi + (long)s * nbf * nbf;
-      const float* Pl = Plo + (long)s * nbf * nbf;
+      const float* __restrict__ Ph = I.Phi + (long)s * nbf * nbf;
+      const float* __restrict__ Pl = I.Plo + (long)s * nbf * nbf;
       double r_acc = 0.0, g_acc[3] = {0.0, 0.0, 0.0};
       for (int nu0 = 0; nu0 < nact; nu0 += kNT) {
         const int nnu = min(kNT, nact - nu0);
         const int N = (nnu + 15) & ~15;
         const int nkc = (nact + 31) / 32;
-        int sh_cursor = s0;
         for (int kc = 0; kc < nkc; ++kc) {
           const int st = kc & 1;
           uint8_t* Ahi = sm + st * kStageBytes;
@@ -259,51 +325,35 @@ __global__ void __launch_bounds__(kT, 1)
           uint8_t* Bhi = Alo + kTileA;
           uint8_t* Blo = Bhi + kTileA;
           const int mu0 = kc * 32;
-          // ---- A: Phi[p][mu0 + 16 half .. + 16) ----
-          {
-            const int k0 = 16 * half;
+          // ---- A: Phi[p][mu0 + 4q .. + 4) for the 4 quads q of this half, 16-byte stores ----
 #pragma unroll
-            for (int k = k0; k < k0 + 16; ++k) {
-              *reinterpret_cast<uint32_t*>(Ahi + tc::swz_offset(p, k)) = 0u;
-              *reinterpret_cast<uint32_t*>(Alo + tc::swz_offset(p, k)) = 0u;
+          for (int qq = 0; qq < 4; ++qq) {
+            const int q = 4 * half + qq;
+            uint32_t h[4], l[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int mu = mu0 + 4 * q + e;
+              tc::split_tf32(mu < nact ? my[(long)mu * 128 + p] : 0.f, h[e], l[e]);
             }
-            const int lo = mu0 + k0;
-            while (sh_cursor < s1) {
-              const int info = __ldg(&recs[sh_cursor].info);
-              if (rec_f0(info) + rec_nf(info) > lo) break;
-              ++sh_cursor;
-            }
-            if (live) {
-              for (int si = sh_cursor; si < s1; ++si) {
-                const ShellRec r = load_rec(recs + si);
-                const int f0 = rec_f0(r.info);
-                if (f0 >= lo + 16) break;
-                shell_rec_at<0>(r, B.prim2, pt, expthr, thr, [&](int f, float v, float, float, float) {
-                  const int k = f0 + f - mu0;
-                  if (k >= k0 && k < k0 + 16) st_tf32_pair(Ahi, Alo, tc::swz_offset(p, k), v);
-                });
-              }
-            }
+            const uint32_t off = (uint32_t)(p * 128 + ((q ^ (p & 7)) << 4));
+            *reinterpret_cast<uint4*>(Ahi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+            *reinterpret_cast<uint4*>(Alo + off) = make_uint4(l[0], l[1], l[2], l[3]);
           }
-          // ---- B: P_b[nu][mu0 .. mu0 + 32), pre-split TF32 parts ----
+          // ---- B: P_b[nu][mu0 + lane] = P[fn[mu]][fn[nu]] (symmetric P), one warp per row ----
           {
-            const int nu = tid & 127;
-            if (nu < N) {
-              const bool nuok = nu < nnu;
-              const long colnu = nuok ? fn[nu0 + nu] : 0;
-#pragma unroll 4
-              for (int k = half; k < 32; k += 2) {
-                const int mu = mu0 + k;
-                float h = 0.f, l = 0.f;
-                if (nuok && mu < nact) {
-                  const long o = (long)fn[mu] * nbf + colnu;
-                  h = __ldg(Ph + o);
-                  l = __ldg(Pl + o);
-                }
-                const uint32_t off = tc::swz_offset(nu, k);
-                *reinterpret_cast<float*>(Bhi + off) = h;
-                *reinterpret_cast<float*>(Blo + off) = l;
+            const int mu = mu0 + lane;
+            const bool muok = mu < nact;
+            const long cmu = muok ? (long)__ldg(fn + mu) : 0;
+            for (int row = warp; row < N; row += kT / 32) {
+              float h = 0.f, l = 0.f;
+              if (muok && row < nnu) {
+                const long o = (long)__ldg(fn + nu0 + row) * nbf + cmu;
+                h = __ldg(Ph + o);
+                l = __ldg(Pl + o);
               }
+              const uint32_t off = tc::swz_offset(row, lane);
+              *reinterpret_cast<float*>(Bhi + off) = h;
+              *reinterpret_cast<float*>(Blo + off) = l;
             }
           }
           tc::fence_async_smem();
@@ -325,7 +375,7 @@ __global__ void __launch_bounds__(kT, 1)
           if (tid == 0) {
             tc::fence_after_sync();
             issue_chunk(tmem, tc::smem_u32(Ahi), tc::smem_u32(Alo), tc::smem_u32(Bhi), tc::smem_u32(Blo), N,
-                        st ? kColsHH1 : kColsHH0, kc == 0);
+                        st ? kColsHH1 : kColsHH0, kColsX0, kc == 0);
             tc::mma_commit(&mbar[st]);
           }
           outstanding = st;
@@ -342,30 +392,30 @@ __global__ void __launch_bounds__(kT, 1)
           }
           tc::fence_after_sync();
           drain64(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Xs, ld, 64 * (warp >> 2), N, nkc == 1);
-          drain64(tmem + kColsX, warp, lane, Xs, ld, 64 * (warp >> 2), N, false);
+          drain64(tmem + kColsX0, warp, lane, Xs, ld, 64 * (warp >> 2), N, false);
           tc::fence_before_sync();
           __syncthreads();
         }
-        // ---- row dots: rho_p += sum_nu X_p,nu phi_p,nu (shells split between the two halves) ----
+        // ---- rho_p += sum_nu X_p,nu phi_nu(p) over this half's 64 columns, FP32 runs of 8 ----
         if (live) {
-          int j = 0;
-          for (int si = s0; si < s1; ++si) {
-            const int info = __ldg(&recs[si].info);
-            const int f0 = rec_f0(info), nf = rec_nf(info);
-            if (f0 + nf > nu0 && f0 < nu0 + nnu && ((j++ & 1) == half)) {
-              const ShellRec r = load_rec(recs + si);
-              float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-              shell_rec_at<1>(r, B.prim2, pt, expthr, thr, [&](int f, float v, float dx, float dy, float dz) {
-                const int c = f0 + f - nu0;
-                if (c >= 0 && c < nnu) {
-                  const float xv = Xs[p * ld + c];
-                  rr = fmaf(xv, v, rr);
-                  gx = fmaf(xv, dx, gx);
-                  gy = fmaf(xv, dy, gy);
-                  gz = fmaf(xv, dz, gz);
-                }
-              });
-              r_acc += (double)rr;
+          const float* xs = Xs + p * ld;
+          const float* t = my + (long)nu0 * 128 + p;
+          const int c1 = min(nnu, 64 * half + 64);
+          for (int c8 = 64 * half; c8 < c1; c8 += 8) {
+            float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+            const int ce = min(c1, c8 + 8);
+            for (int c = c8; c < ce; ++c) {
+              const float xv = xs[c];
+              const float* tc_ = t + (long)c * 128;
+              rr = fmaf(xv, tc_[0], rr);
+              if (DERIV) {
+                gx = fmaf(xv, tc_[cs], gx);
+                gy = fmaf(xv, tc_[2 * cs], gy);
+                gz = fmaf(xv, tc_[3 * cs], gz);
+              }
+            }
+            r_acc += (double)rr;
+            if (DERIV) {
               g_acc[0] += (double)gx;
               g_acc[1] += (double)gy;
               g_acc[2] += (double)gz;
@@ -384,7 +434,7 @@ __global__ void __launch_bounds__(kT, 1)
       __syncthreads();
       if (half == 0 && live) {
         rho[(long)s * P.npoints + first + p] = r_acc + s_part[0][p];
-        if (grad) {
+        if (DERIV && grad) {
           grad[((long)s * 3 + 0) * P.npoints + first + p] = 2.0 * (g_acc[0] + s_part[1][p]);
           grad[((long)s * 3 + 1) * P.npoints + first + p] = 2.0 * (g_acc[1] + s_part[2][p]);
           grad[((long)s * 3 + 2) * P.npoints + first + p] = 2.0 * (g_acc[2] + s_part[3][p]);
@@ -401,24 +451,34 @@ done:
 }
 
 // =====================================================================================
-// adder
+// adder: D = Phi^T G per block, G = w (v/2 Phi + g . grad Phi), V += D (FP64 red.add)
+//   1. every active shell of the block is evaluated once; its functions go to the CTA's
+//      scratch as ready-made operand tiles (TF32 hi and lo, 128 functions x 32 points,
+//      128-byte swizzled K-major, the shared-memory image of the tile): Phi, and G for
+//      each spin.  A warp writes whole 128-byte rows (32 points of one function).
+//   2. the tile products (spin, function tile m, function tile n, 32-point chunk) run as
+//      one pipeline: thread 0 streams the four operand tiles of each step into one of
+//      three shared-memory stages with bulk copies (TMA) two steps ahead and issues the
+//      MMAs; all threads drain the finished step's accumulator into registers; at the
+//      end of a tile pair the sums go to V with FP64 atomics.
 // =====================================================================================
+template <int DERIV>
 __global__ void __launch_bounds__(kT, 1)
     mx_adder_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t mbar[2];
+  __shared__ uint64_t full[kAdderStages], mdone[kAdderStages];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort;
-  __shared__ float s_wv[128], s_wg[3][128];
+  __shared__ float s_w[2][4][128];  // per spin and point: w v / 2, w g_x, w g_y, w g_z
   const uint32_t base_s = tc::smem_u32(smem_raw);
   uint8_t* sm = smem_raw + ((1024 - (base_s & 1023)) & 1023);
-  float* Ds = reinterpret_cast<float*>(sm + 2 * kStageBytes);  // [128][kNT + 1]
-  const int ld = kNT + 1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
   if (tid == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
+    for (int i = 0; i < kAdderStages; ++i) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&mdone[i], 1);
+    }
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -426,8 +486,10 @@ __global__ void __launch_bounds__(kT, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  uint32_t phase[2] = {0, 0};
-  int outstanding = -1;
+  uint32_t fph = 0, mph = 0;  // phase bit per stage of full (thread 0) and mdone
+  int issued = 0, consumed = 0, committed = 0, drained = 0;  // pipeline steps of the current block
+  float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
+  const long opstride = (long)bt.ft_max * 4 * 2 * kTileFloats;  // floats per operand (Phi, G_0, G_1)
 
   for (;;) {
     __syncthreads();
@@ -440,150 +502,190 @@ __global__ void __launch_bounds__(kT, 1)
     const DevBasis& B = I.B;
     const DevPlan& P = I.P;
     const int nspin = I.nspin, nbf = P.nbf;
-    const double* __restrict__ v = I.v;
-    const double* __restrict__ g = I.g;
-    const unsigned char* __restrict__ skip = I.skip;
-    double* __restrict__ V = I.V;
     const long first = (long)b * P.max_block;
     const int npts = (int)min((long)P.max_block, P.npoints - first);
     const int nact = P.fn_off[b + 1] - P.fn_off[b];
-    const int* fn = P.fn_list + P.fn_off[b];
+    const int* __restrict__ fn = P.fn_list + P.fn_off[b];
     const int s0 = P.sh_off[b], s1 = P.sh_off[b + 1];
-    for (int s = 0; s < nspin; ++s) {
-      if (skip[(long)s * P.nblocks + b]) continue;
-      if (tid < 128) {
-        const int q = tid;
-        float wv = 0.f, wg0 = 0.f, wg1 = 0.f, wg2 = 0.f;
-        if (q < npts) {
-          const double w = P.w[first + q];
-          wv = (float)(0.5 * w * v[(long)s * P.npoints + first + q]);
-          if (g) {
-            wg0 = (float)(w * g[((long)s * 3 + 0) * P.npoints + first + q]);
-            wg1 = (float)(w * g[((long)s * 3 + 1) * P.npoints + first + q]);
-            wg2 = (float)(w * g[((long)s * 3 + 2) * P.npoints + first + q]);
+    int smask = 0;
+    for (int s = 0; s < nspin; ++s)
+      if (!I.skip[(long)s * P.nblocks + b]) smask |= 1 << s;
+    if (smask == 0 || nact == 0) continue;
+    const int nft = (nact + 127) >> 7, nkc = (npts + 31) >> 5;
+    if (nft > bt.ft_max || (long)(1 + nspin) * opstride > bt.cta_floats) {  // scratch too small: report, skip
+      if (tid == 0) atomicExch(err, kErrScratch);
+      continue;
+    }
+    // ---- weights ----
+    {
+      const int s = tid >> 7, q = tid & 127;
+      float w4[4] = {0.f, 0.f, 0.f, 0.f};
+      if (((smask >> s) & 1) && q < npts) {
+        const double w = P.w[first + q];
+        w4[0] = (float)(0.5 * w * I.v[(long)s * P.npoints + first + q]);
+        if (DERIV && I.g) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) w4[1 + c] = (float)(w * I.g[((long)s * 3 + c) * P.npoints + first + q]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) s_w[s][c][q] = w4[c];
+    }
+    __syncthreads();
+    // ---- 1. operand tiles of the block ----
+    {
+      const int p = tid & 127, par = tid >> 7;
+      const int kc = p >> 5, k = p & 31;
+      if (kc < nkc) {  // warp-uniform
+        const bool live = p < npts;
+        const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
+        const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
+        float wsp[2][4];
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) wsp[s][c] = s_w[s][c][p];
+        const bool sp0 = smask & 1, sp1 = (smask >> 1) & 1;
+        const int kq = k >> 2, kr = k & 3;
+        float* const base = my + kc * 2 * kTileFloats + kr;
+        for (int si = s0 + par; si < s1; si += 2) {
+          const ShellRec r = load_rec(P.rec + si);
+          const int f0 = rec_f0(r.info);
+          auto put = [&](int f, float val, float dx, float dy, float dz) {
+            const int mu = f0 + f, row = mu & 127;
+            float* t = base + (long)(mu >> 7) * 4 * 2 * kTileFloats + row * 32 + (((kq ^ (row & 7)) & 7) << 2);
+            st_split(t, val);
+            if (sp0) {
+              float gv = wsp[0][0] * val;
+              if (DERIV) gv += wsp[0][1] * dx + wsp[0][2] * dy + wsp[0][3] * dz;
+              st_split(t + opstride, gv);
+            }
+            if (sp1) {
+              float gv = wsp[1][0] * val;
+              if (DERIV) gv += wsp[1][1] * dx + wsp[1][2] * dy + wsp[1][3] * dz;
+              st_split(t + 2 * opstride, gv);
+            }
+          };
+          if (live) {
+            shell_rec_at<DERIV>(r, B.prim2, pt, expthr, thr, put);
+          } else {
+            const int nf = rec_nf(r.info);
+            for (int f = 0; f < nf; ++f) put(f, 0.f, 0.f, 0.f, 0.f);
           }
         }
-        s_wv[q] = wv;
-        s_wg[0][q] = wg0;
-        s_wg[1][q] = wg1;
-        s_wg[2][q] = wg2;
+      }
+      tc::fence_async_global();  // these generic writes are read by the bulk copies below
+    }
+    __syncthreads();
+    // ---- 2. tile products ----
+    const int nsteps = __popc(smask) * nft * nft * nkc;
+    // step i -> (spin, m tile, n tile, chunk), chunk fastest
+    auto decode = [&](int i, int& s, int& mt, int& nt, int& kc) {
+      kc = i % nkc;
+      int r = i / nkc;
+      nt = r % nft;
+      r /= nft;
+      mt = r % nft;
+      const int si = r / nft;
+      s = (smask == 2) ? 1 : si;
+    };
+    auto issue_copy = [&](int i) {
+      int s, mt, nt, kc;
+      decode(i, s, mt, nt, kc);
+      const int st = i % kAdderStages;
+      uint8_t* dst = sm + st * kStageBytes;
+      const int nM = min(128, nact - 128 * mt), nN = min(128, nact - 128 * nt);
+      const uint32_t ab = (uint32_t)((nM + 7) & ~7) * 128u, bb = (uint32_t)((nN + 15) & ~15) * 128u;
+      const float* a = my + (long)(mt * 4 + kc) * 2 * kTileFloats;
+      const float* g = my + (long)(1 + s) * opstride + (long)(nt * 4 + kc) * 2 * kTileFloats;
+      tc::mbar_arrive_expect_tx(&full[st], 2 * ab + 2 * bb);
+      tc::bulk_g2s(dst, a, ab, &full[st]);
+      tc::bulk_g2s(dst + kTileA, a + kTileFloats, ab, &full[st]);
+      tc::bulk_g2s(dst + 2 * kTileA, g, bb, &full[st]);
+      tc::bulk_g2s(dst + 3 * kTileA, g + kTileFloats, bb, &full[st]);
+    };
+    issued = consumed = committed = drained = 0;
+    float acc[64];  // this thread's 64 columns of one row of the current tile pair
+    if (tid == 0)
+      for (; issued < min(kAdderStages, nsteps); ++issued) issue_copy(issued);
+    for (int i = 0; i <= nsteps; ++i) {
+      bool bad = false;
+      if (tid == 0 && i < nsteps) {
+        const int st = i % kAdderStages;
+        if (tc::mbar_wait_bounded(&full[st], (fph >> st) & 1u, kWaitLimitNs)) {
+          fph ^= 1u << st;
+          ++consumed;
+          tc::fence_after_sync();
+          int s, mt, nt, kc;
+          decode(i, s, mt, nt, kc);
+          const int N = (min(128, nact - 128 * nt) + 15) & ~15;
+          const uint32_t sa = tc::smem_u32(sm + st * kStageBytes);
+          issue_chunk(tmem, sa, sa + kTileA, sa + 2 * kTileA, sa + 3 * kTileA, N, (i & 1) ? kColsHH1 : kColsHH0,
+                      ((i / nkc) & 1) ? kColsX1 : kColsX0, kc == 0);
+          tc::mma_commit(&mdone[st]);
+          ++committed;
+        } else {
+          bad = true;
+        }
+      }
+      if (i >= 1) {
+        const int j = i - 1, st = j % kAdderStages;
+        if (tc::mbar_wait_bounded(&mdone[st], (mph >> st) & 1u, kWaitLimitNs)) {
+          mph ^= 1u << st;
+          ++drained;
+          // the MMAs of step j are done with stage st: refill it for step j + 3
+          if (tid == 0 && j + kAdderStages < nsteps) {
+            issue_copy(j + kAdderStages);
+            ++issued;
+          }
+        } else {
+          bad = true;
+        }
+      }
+      if (__syncthreads_or(bad)) {
+        if (bad) atomicExch(err, kErrTimeout);
+        goto abort;
+      }
+      if (i >= 1) {
+        tc::fence_after_sync();
+        const int j = i - 1;
+        int s, mt, nt, kc;
+        decode(j, s, mt, nt, kc);
+        const int nN = min(128, nact - 128 * nt);
+        const int N = (nN + 15) & ~15;
+        drain_regs(tmem + ((j & 1) ? kColsHH1 : kColsHH0), warp, acc, kc == 0, N);
+        if (kc == nkc - 1) {
+          drain_regs(tmem + (((j / nkc) & 1) ? kColsX1 : kColsX0), warp, acc, false, N);
+          const int nM = min(128, nact - 128 * mt);
+          const int row = 32 * (warp & 3) + lane, c0 = 64 * (warp >> 2);
+          if (row < nM) {
+            double* Vs = I.V + (long)s * nbf * nbf + __ldg(fn + 128 * mt + row);
+            const int* fnn = fn + 128 * nt + c0;
+#pragma unroll
+            for (int c = 0; c < 64; ++c)
+              if (c0 + c < nN) atomicAdd(Vs + (long)__ldg(fnn + c) * nbf, (double)acc[c]);
+          }
+        }
+        tc::fence_before_sync();
       }
       __syncthreads();
-      double* Vs = V + (long)s * nbf * nbf;
-      for (int nt0 = 0; nt0 < nact; nt0 += kNT) {
-        const int nN = min(kNT, nact - nt0);
-        const int N = (nN + 15) & ~15;
-        for (int mt0 = 0; mt0 < nact; mt0 += kNT) {
-          const int nM = min(kNT, nact - mt0);
-          // zero the padding rows of both stages (A rows >= nM, B rows in [nN, N))
-          for (int e = tid; e < 2 * ((128 - nM) + (N - nN)) * 32; e += kT) {
-            const int stg = e / (((128 - nM) + (N - nN)) * 32);
-            const int r0 = (e / 32) % ((128 - nM) + (N - nN)), k = e % 32;
-            uint8_t* base = sm + stg * kStageBytes;
-            if (r0 < 128 - nM) {
-              const uint32_t off = tc::swz_offset(nM + r0, k);
-              *reinterpret_cast<uint32_t*>(base + off) = 0u;
-              *reinterpret_cast<uint32_t*>(base + kTileA + off) = 0u;
-            } else {
-              const uint32_t off = tc::swz_offset(nN + r0 - (128 - nM), k);
-              *reinterpret_cast<uint32_t*>(base + 2 * kTileA + off) = 0u;
-              *reinterpret_cast<uint32_t*>(base + 3 * kTileA + off) = 0u;
-            }
-          }
-          __syncthreads();
-          const int nkp = (npts + 31) / 32;  // 32-point chunks holding live points
-          for (int kc = 0; kc < nkp; ++kc) {
-            const int st = kc & 1;
-            uint8_t* Ahi = sm + st * kStageBytes;
-            uint8_t* Alo = Ahi + kTileA;
-            uint8_t* Bhi = Alo + kTileA;
-            uint8_t* Blo = Bhi + kTileA;
-            // fill: lane <-> point of the chunk, warps split the shells
-            {
-              const int q = kc * 32 + lane;
-              const bool qlive = q < npts;
-              const Pt pt = make_pt(P.xyz + 3 * (first + (qlive ? q : 0)));
-              float wv = 0.f, wx = 0.f, wy = 0.f, wz = 0.f;
-              if (qlive) {
-                wv = s_wv[q];
-                wx = s_wg[0][q];
-                wy = s_wg[1][q];
-                wz = s_wg[2][q];
-              }
-              int j = 0;
-              for (int si = s0; si < s1; ++si) {
-                const int info = __ldg(&P.rec[si].info);
-                const int f0 = rec_f0(info), nf = rec_nf(info);
-                const bool inM = (f0 + nf > mt0) && (f0 < mt0 + nM);
-                const bool inN = (f0 + nf > nt0) && (f0 < nt0 + nN);
-                if ((inM || inN) && ((j++ & 7) == warp)) {
-                  auto put = [&](int f, float val, float dx, float dy, float dz) {
-                    const int mu = f0 + f;
-                    if (mu >= mt0 && mu < mt0 + nM) st_tf32_pair(Ahi, Alo, tc::swz_offset(mu - mt0, lane), val);
-                    if (mu >= nt0 && mu < nt0 + nN)
-                      st_tf32_pair(Bhi, Blo, tc::swz_offset(mu - nt0, lane), wv * val + wx * dx + wy * dy + wz * dz);
-                  };
-                  if (qlive) {
-                    shell_rec_at<1>(load_rec(P.rec + si), B.prim2, pt, (float)P.exponent_threshold,
-                                    (float)P.radial_threshold, put);
-                  } else {
-                    for (int f = 0; f < nf; ++f) put(f, 0.f, 0.f, 0.f, 0.f);
-                  }
-                }
-              }
-            }
-            tc::fence_async_smem();
-            if (kc > 0) {
-              const int pst = (kc - 1) & 1;
-              const bool ok = wait_or_abort(&mbar[pst], phase[pst], err);
-              phase[pst] ^= 1;
-              outstanding = -1;
-              if (__syncthreads_or(!ok)) {
-                if (tid == 0) s_abort = 1;
-                goto done;
-              }
-              tc::fence_after_sync();
-              drain64(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Ds, ld, 64 * (warp >> 2), N, kc == 1);
-              tc::fence_before_sync();
-            }
-            __syncthreads();
-            if (tid == 0) {
-              tc::fence_after_sync();
-              issue_chunk(tmem, tc::smem_u32(Ahi), tc::smem_u32(Alo), tc::smem_u32(Bhi), tc::smem_u32(Blo), N,
-                          st ? kColsHH1 : kColsHH0, kc == 0);
-              tc::mma_commit(&mbar[st]);
-            }
-            outstanding = st;
-          }
-          // last chunk: drain, add the cross terms, scatter into V
-          {
-            const int pst = (nkp - 1) & 1;
-            const bool ok = wait_or_abort(&mbar[pst], phase[pst], err);
-            phase[pst] ^= 1;
-            outstanding = -1;
-            if (__syncthreads_or(!ok)) {
-              if (tid == 0) s_abort = 1;
-              goto done;
-            }
-            tc::fence_after_sync();
-            drain64(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Ds, ld, 64 * (warp >> 2), N, nkp == 1);
-            drain64(tmem + kColsX, warp, lane, Ds, ld, 64 * (warp >> 2), N, false);
-            tc::fence_before_sync();
-            const int row = 32 * (warp & 3) + lane;
-            if (row < nM) {
-              const long colmu = fn[mt0 + row];
-              const int c0 = 64 * (warp >> 2);
-              for (int c = c0; c < c0 + 64 && c < nN; ++c)
-                atomicAdd(&Vs[(long)fn[nt0 + c] * nbf + colmu], (double)Ds[row * ld + c]);
-            }
-            __syncthreads();
-          }
-        }
-      }
+    }
+  }
+  goto done;
+abort:
+  if (tid == 0) {
+    s_abort = 1;
+    // let every copy and MMA still in flight land before the CTA gives up its memory
+    for (int i = consumed; i < issued; ++i) {
+      const int st = i % kAdderStages;
+      if (tc::mbar_wait_bounded(&full[st], (fph >> st) & 1u, kWaitLimitNs)) fph ^= 1u << st;
+    }
+    for (int i = drained; i < committed; ++i) {
+      const int st = i % kAdderStages;
+      if (tc::mbar_wait_bounded(&mdone[st], (mph >> st) & 1u, kWaitLimitNs)) mph ^= 1u << st;
     }
   }
 done:
-  if (outstanding >= 0) wait_or_abort(&mbar[outstanding], phase[outstanding], err);
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
@@ -618,14 +720,24 @@ __global__ void symmetrize_kernel(double* V, int nbf, int nspin) {
   }
 }
 
-static size_t mixed_smem() { return 2 * kStageBytes + 128 * (kNT + 1) * sizeof(float) + 1024; }
+static size_t density_smem() { return 2 * kStageBytes + 128 * (kNT + 1) * sizeof(float) + 1024; }
+static size_t adder_smem() { return kAdderStages * kStageBytes + 1024; }
 
 xcgpu_status mixed_init(Ctx* c) {
-  xcgpu_status st = c->cuda(cudaFuncSetAttribute(mx_density_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)mixed_smem()), "density smem attribute");
-  if (st) return st;
-  return c->cuda(cudaFuncSetAttribute(mx_adder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mixed_smem()),
-                 "adder smem attribute");
+  const struct {
+    const void* fn;
+    size_t bytes;
+    const char* what;
+  } k[] = {{(const void*)mx_density_kernel<0>, density_smem(), "density smem attribute"},
+           {(const void*)mx_density_kernel<1>, density_smem(), "density smem attribute"},
+           {(const void*)mx_adder_kernel<0>, adder_smem(), "adder smem attribute"},
+           {(const void*)mx_adder_kernel<1>, adder_smem(), "adder smem attribute"}};
+  for (const auto& e : k) {
+    xcgpu_status st =
+        c->cuda(cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.bytes), e.what);
+    if (st) return st;
+  }
+  return XCGPU_OK;
 }
 
 static void fill_item(MxItem& it, const MixedWork& w) {
@@ -643,6 +755,21 @@ static void fill_item(MxItem& it, const MixedWork& w) {
   it.V = w.V;
 }
 
+// Scratch floats per CTA for the items [i0, i1): the density's [4][n_b][128] values
+// and the adder's (1 + nspin) operands of ft_max x 4 tiles (hi + lo).
+static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t i1, int* ft_max) {
+  int amax = 0, smax = 1;
+  for (size_t i = i0; i < i1; ++i) {
+    amax = std::max(amax, work[i].P->max_active);
+    smax = std::max(smax, work[i].nspin);
+  }
+  const int ft = std::max(1, (amax + 127) / 128);
+  *ft_max = ft;
+  const long dens = 4L * amax * 128;
+  const long add = (long)(1 + smax) * ft * 4 * 2 * kTileFloats;
+  return (std::max(dens, add) + 63) & ~63L;
+}
+
 // parameter blocks for the items [i0, i1) of a batch
 static void make_batch(const std::vector<MixedWork>& work, size_t i0, size_t i1, MxBatch& bt) {
   bt.nitems = (int)(i1 - i0);
@@ -654,6 +781,28 @@ static void make_batch(const std::vector<MixedWork>& work, size_t i0, size_t i1,
   bt.nblocks = bt.bstart[bt.nitems];
 }
 
+// the calling stream's scratch, grown to the batch's need (allocation happens only on
+// growth, so graph capture works after one uncaptured run of the same batch)
+static xcgpu_status batch_scratch(Ctx* c, const std::vector<MixedWork>& work, size_t i0, size_t i1, MxBatch& bt) {
+  bt.cta_floats = cta_floats_for(work, i0, i1, &bt.ft_max);
+  const size_t bytes = (size_t)bt.cta_floats * c->sm_count * sizeof(float);
+  auto& buf = c->mixed_by_stream[c->stream];
+  if (!buf) buf.reset(new DevBuf());
+  if (buf->bytes < bytes || !buf->p) {
+    xcgpu_status st = buf->alloc(c, bytes);
+    if (st) return st;
+    if ((st = c->cuda(cudaMemsetAsync(buf->p, 0, bytes, c->stream), "memset mixed scratch"))) return st;
+  }
+  bt.scratch = buf->as<float>();
+  return XCGPU_OK;
+}
+
+static bool any_gga(const std::vector<MixedWork>& work, size_t i0, size_t i1, bool density) {
+  for (size_t i = i0; i < i1; ++i)
+    if (density ? work[i].grad != nullptr : work[i].g != nullptr) return true;
+  return false;
+}
+
 xcgpu_status mixed_split(Ctx* c, const double* Pm, float* Psplit, long n) {
   KernelTimer kt(c, kOther);
   split_p_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(Pm, Psplit, Psplit + n, n);
@@ -663,12 +812,17 @@ xcgpu_status mixed_split(Ctx* c, const double* Pm, float* Psplit, long n) {
 xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
   static thread_local MxBatch bt;  // host-side parameter block (the launch copies it)
   for (size_t i0 = 0; i0 < work.size(); i0 += kMaxItems) {
-    make_batch(work, i0, std::min(work.size(), i0 + kMaxItems), bt);
+    const size_t i1 = std::min(work.size(), i0 + kMaxItems);
+    make_batch(work, i0, i1, bt);
     if (bt.nblocks == 0) continue;
-    xcgpu_status st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter");
+    xcgpu_status st = batch_scratch(c, work, i0, i1, bt);
     if (st) return st;
+    if ((st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter"))) return st;
     KernelTimer kt(c, kDensity);
-    mx_density_kernel<<<c->sm_count, kT, mixed_smem(), c->stream>>>(bt, counter, err);
+    if (any_gga(work, i0, i1, true))
+      mx_density_kernel<1><<<c->sm_count, kT, density_smem(), c->stream>>>(bt, counter, err);
+    else
+      mx_density_kernel<0><<<c->sm_count, kT, density_smem(), c->stream>>>(bt, counter, err);
     if ((st = c->check_launch("mx_density_kernel"))) return st;
   }
   return XCGPU_OK;
@@ -678,11 +832,16 @@ xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* 
   static thread_local MxBatch bt;
   xcgpu_status st = XCGPU_OK;
   for (size_t i0 = 0; i0 < work.size(); i0 += kMaxItems) {
-    make_batch(work, i0, std::min(work.size(), i0 + kMaxItems), bt);
+    const size_t i1 = std::min(work.size(), i0 + kMaxItems);
+    make_batch(work, i0, i1, bt);
     if (bt.nblocks == 0) continue;
+    if ((st = batch_scratch(c, work, i0, i1, bt))) return st;
     if ((st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter"))) return st;
     KernelTimer kt(c, kAdder);
-    mx_adder_kernel<<<c->sm_count, kT, mixed_smem(), c->stream>>>(bt, counter, err);
+    if (any_gga(work, i0, i1, false))
+      mx_adder_kernel<1><<<c->sm_count, kT, adder_smem(), c->stream>>>(bt, counter, err);
+    else
+      mx_adder_kernel<0><<<c->sm_count, kT, adder_smem(), c->stream>>>(bt, counter, err);
     if ((st = c->check_launch("mx_adder_kernel"))) return st;
   }
   KernelTimer kt2(c, kOther);
