@@ -117,7 +117,9 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* mbar, uint32_t parity, i
 // summed in round-to-nearest FP32 on the CUDA cores (one long chain over all K gave a
 // relative density bias of -6e-7).  The cross terms (~2^-11 smaller) stay in one
 // accumulator per tile.
-constexpr int kT = 256;
+constexpr int kT = 512;                       // threads per CTA (one CTA per SM)
+constexpr int kWarps = kT / 32;
+constexpr int kQ = kT / 128;                  // threads per point of a 128-point block
 constexpr int kNT = 128;                      // rows of an operand tile (M, and N at most)
 constexpr uint32_t kStageBytes = 4 * kTileA;  // A_hi, A_lo, B_hi, B_lo
 constexpr uint32_t kColsHH0 = 0, kColsHH1 = 128, kColsX0 = 256, kColsX1 = 384;
@@ -139,36 +141,29 @@ __device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t ah, uint32_t
   }
 }
 
-// add (or store) TMEM columns [col, col + 64) of this warp's 32 lanes into S rows
-__device__ __forceinline__ void drain64(uint32_t tmem_cols, int warp, int lane, float* S, int ld, int c0, int N,
-                                        bool store) {
-  const int row = 32 * (warp & 3) + lane;
-  for (int c = c0; c < c0 + 64 && c < N; c += 32) {
-    float v[32];
-    tc::tmem_ld32(tmem_cols + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c, v);
+// add (or store) TMEM columns [32 (warp >> 2), +32) of this warp's 32 lanes into S rows
+__device__ __forceinline__ void drain32(uint32_t tmem_cols, int warp, int lane, float* S, int ld, int N, bool store) {
+  const int row = 32 * (warp & 3) + lane, c = 32 * (warp >> 2);
+  if (c >= N) return;  // warp-uniform
+  float v[32];
+  tc::tmem_ld32(tmem_cols + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c, v);
 #pragma unroll
-    for (int i = 0; i < 32; ++i)
-      if (c + i < N) {
-        float* d = S + row * ld + c + i;
-        *d = store ? v[i] : *d + v[i];
-      }
-  }
+  for (int i = 0; i < 32; ++i)
+    if (c + i < N) {
+      float* d = S + row * ld + c + i;
+      *d = store ? v[i] : *d + v[i];
+    }
 }
 
-// add (or store) this warp's 32 lanes x 64 columns [64 (warp >> 2), +64) of a TMEM
+// add (or store) this warp's 32 lanes x 32 columns [32 (warp >> 2), +32) of a TMEM
 // accumulator into registers
 __device__ __forceinline__ void drain_regs(uint32_t tmem_cols, int warp, float* acc, bool store, int N) {
-  const int c0 = 64 * (warp >> 2);
-  const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;
+  const int c0 = 32 * (warp >> 2);
+  if (c0 >= N) return;  // warp-uniform
+  float v[32];
+  tc::tmem_ld32(tmem_cols + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c0, v);
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    if (c0 + 32 * h < N) {  // warp-uniform
-      float v[32];
-      tc::tmem_ld32(tmem_cols + lanes + (uint32_t)(c0 + 32 * h), v);
-#pragma unroll
-      for (int i = 0; i < 32; ++i) acc[32 * h + i] = store ? v[i] : acc[32 * h + i] + v[i];
-    }
-  }
+  for (int i = 0; i < 32; ++i) acc[i] = store ? v[i] : acc[i] + v[i];
 }
 
 // split v into TF32 hi (at t[0]) and lo (at t[kTileFloats])
@@ -238,13 +233,13 @@ __global__ void __launch_bounds__(kT, 1)
   __shared__ uint64_t mbar[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort;
-  __shared__ double s_part[4][128];
+  __shared__ double s_part[4][kQ - 1][128];
   const uint32_t base_s = tc::smem_u32(smem_raw);
   uint8_t* sm = smem_raw + ((1024 - (base_s & 1023)) & 1023);
   float* Xs = reinterpret_cast<float*>(sm + 2 * kStageBytes);  // [128][kNT + 1]
   const int ld = kNT + 1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int p = tid & 127, half = tid >> 7;
+  const int p = tid & 127, quarter = tid >> 7;  // point, and which of its kQ threads
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
   if (tid == 0) {
     tc::mbar_init(&mbar[0], 1);
@@ -289,8 +284,11 @@ __global__ void __launch_bounds__(kT, 1)
       const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
       const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
       float* const col = my + p;
-      for (int si = s0 + half; si < s1; si += 2) {
-        const ShellRec r = load_rec(P.rec + si);
+      ShellRec next;
+      if (s0 + quarter < s1) next = load_rec(P.rec + s0 + quarter);
+      for (int si = s0 + quarter; si < s1; si += kQ) {
+        const ShellRec r = next;
+        if (si + kQ < s1) next = load_rec(P.rec + si + kQ);  // in flight while r is evaluated
         float* const t0 = col + (long)rec_f0(r.info) * 128;
         auto put = [&](int f, float v, float dx, float dy, float dz) {
           float* t = t0 + f * 128;
@@ -325,10 +323,10 @@ __global__ void __launch_bounds__(kT, 1)
           uint8_t* Bhi = Alo + kTileA;
           uint8_t* Blo = Bhi + kTileA;
           const int mu0 = kc * 32;
-          // ---- A: Phi[p][mu0 + 4q .. + 4) for the 4 quads q of this half, 16-byte stores ----
+          // ---- A: Phi[p][mu0 + 4q .. + 4) for this thread's 2 quads q, 16-byte stores ----
 #pragma unroll
-          for (int qq = 0; qq < 4; ++qq) {
-            const int q = 4 * half + qq;
+          for (int qq = 0; qq < 2; ++qq) {
+            const int q = 2 * quarter + qq;
             uint32_t h[4], l[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -344,7 +342,8 @@ __global__ void __launch_bounds__(kT, 1)
             const int mu = mu0 + lane;
             const bool muok = mu < nact;
             const long cmu = muok ? (long)__ldg(fn + mu) : 0;
-            for (int row = warp; row < N; row += kT / 32) {
+#pragma unroll 4
+            for (int row = warp; row < N; row += kWarps) {
               float h = 0.f, l = 0.f;
               if (muok && row < nnu) {
                 const long o = (long)__ldg(fn + nu0 + row) * nbf + cmu;
@@ -368,7 +367,7 @@ __global__ void __launch_bounds__(kT, 1)
               goto done;
             }
             tc::fence_after_sync();
-            drain64(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Xs, ld, 64 * (warp >> 2), N, kc == 1);
+            drain32(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Xs, ld, N, kc == 1);
             tc::fence_before_sync();
           }
           __syncthreads();
@@ -391,17 +390,17 @@ __global__ void __launch_bounds__(kT, 1)
             goto done;
           }
           tc::fence_after_sync();
-          drain64(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Xs, ld, 64 * (warp >> 2), N, nkc == 1);
-          drain64(tmem + kColsX0, warp, lane, Xs, ld, 64 * (warp >> 2), N, false);
+          drain32(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Xs, ld, N, nkc == 1);
+          drain32(tmem + kColsX0, warp, lane, Xs, ld, N, false);
           tc::fence_before_sync();
           __syncthreads();
         }
-        // ---- rho_p += sum_nu X_p,nu phi_nu(p) over this half's 64 columns, FP32 runs of 8 ----
+        // ---- rho_p += sum_nu X_p,nu phi_nu(p) over this thread's 32 columns, FP32 runs of 8 ----
         if (live) {
           const float* xs = Xs + p * ld;
           const float* t = my + (long)nu0 * 128 + p;
-          const int c1 = min(nnu, 64 * half + 64);
-          for (int c8 = 64 * half; c8 < c1; c8 += 8) {
+          const int c1 = min(nnu, 32 * quarter + 32);
+          for (int c8 = 32 * quarter; c8 < c1; c8 += 8) {
             float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
             const int ce = min(c1, c8 + 8);
             for (int c = c8; c < ce; ++c) {
@@ -424,20 +423,27 @@ __global__ void __launch_bounds__(kT, 1)
         }
         __syncthreads();  // Xs and the stages are reused by the next pass
       }
-      // combine the two halves of each point
-      if (half == 1) {
-        s_part[0][p] = r_acc;
-        s_part[1][p] = g_acc[0];
-        s_part[2][p] = g_acc[1];
-        s_part[3][p] = g_acc[2];
+      // combine the kQ partial sums of each point
+      if (quarter > 0) {
+        s_part[0][quarter - 1][p] = r_acc;
+        s_part[1][quarter - 1][p] = g_acc[0];
+        s_part[2][quarter - 1][p] = g_acc[1];
+        s_part[3][quarter - 1][p] = g_acc[2];
       }
       __syncthreads();
-      if (half == 0 && live) {
-        rho[(long)s * P.npoints + first + p] = r_acc + s_part[0][p];
+      if (quarter == 0 && live) {
+#pragma unroll
+        for (int k = 0; k < kQ - 1; ++k) {
+          r_acc += s_part[0][k][p];
+          g_acc[0] += s_part[1][k][p];
+          g_acc[1] += s_part[2][k][p];
+          g_acc[2] += s_part[3][k][p];
+        }
+        rho[(long)s * P.npoints + first + p] = r_acc;
         if (DERIV && grad) {
-          grad[((long)s * 3 + 0) * P.npoints + first + p] = 2.0 * (g_acc[0] + s_part[1][p]);
-          grad[((long)s * 3 + 1) * P.npoints + first + p] = 2.0 * (g_acc[1] + s_part[2][p]);
-          grad[((long)s * 3 + 2) * P.npoints + first + p] = 2.0 * (g_acc[2] + s_part[3][p]);
+          grad[((long)s * 3 + 0) * P.npoints + first + p] = 2.0 * g_acc[0];
+          grad[((long)s * 3 + 1) * P.npoints + first + p] = 2.0 * g_acc[1];
+          grad[((long)s * 3 + 2) * P.npoints + first + p] = 2.0 * g_acc[2];
         }
       }
       __syncthreads();
@@ -517,7 +523,7 @@ __global__ void __launch_bounds__(kT, 1)
       continue;
     }
     // ---- weights ----
-    {
+    if (tid < 256) {
       const int s = tid >> 7, q = tid & 127;
       float w4[4] = {0.f, 0.f, 0.f, 0.f};
       if (((smask >> s) & 1) && q < npts) {
@@ -534,7 +540,7 @@ __global__ void __launch_bounds__(kT, 1)
     __syncthreads();
     // ---- 1. operand tiles of the block ----
     {
-      const int p = tid & 127, par = tid >> 7;
+      const int p = tid & 127, quarter = tid >> 7;
       const int kc = p >> 5, k = p & 31;
       if (kc < nkc) {  // warp-uniform
         const bool live = p < npts;
@@ -548,8 +554,11 @@ __global__ void __launch_bounds__(kT, 1)
         const bool sp0 = smask & 1, sp1 = (smask >> 1) & 1;
         const int kq = k >> 2, kr = k & 3;
         float* const base = my + kc * 2 * kTileFloats + kr;
-        for (int si = s0 + par; si < s1; si += 2) {
-          const ShellRec r = load_rec(P.rec + si);
+        ShellRec next;
+        if (s0 + quarter < s1) next = load_rec(P.rec + s0 + quarter);
+        for (int si = s0 + quarter; si < s1; si += kQ) {
+          const ShellRec r = next;
+          if (si + kQ < s1) next = load_rec(P.rec + si + kQ);  // in flight while r is evaluated
           const int f0 = rec_f0(r.info);
           auto put = [&](int f, float val, float dx, float dy, float dz) {
             const int mu = f0 + f, row = mu & 127;
@@ -605,7 +614,7 @@ __global__ void __launch_bounds__(kT, 1)
       tc::bulk_g2s(dst + 3 * kTileA, g + kTileFloats, bb, &full[st]);
     };
     issued = consumed = committed = drained = 0;
-    float acc[64];  // this thread's 64 columns of one row of the current tile pair
+    float acc[32];  // this thread's 32 columns of one row of the current tile pair
     if (tid == 0)
       for (; issued < min(kAdderStages, nsteps); ++issued) issue_copy(issued);
     for (int i = 0; i <= nsteps; ++i) {
@@ -657,12 +666,12 @@ __global__ void __launch_bounds__(kT, 1)
         if (kc == nkc - 1) {
           drain_regs(tmem + (((j / nkc) & 1) ? kColsX1 : kColsX0), warp, acc, false, N);
           const int nM = min(128, nact - 128 * mt);
-          const int row = 32 * (warp & 3) + lane, c0 = 64 * (warp >> 2);
+          const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
           if (row < nM) {
             double* Vs = I.V + (long)s * nbf * nbf + __ldg(fn + 128 * mt + row);
             const int* fnn = fn + 128 * nt + c0;
 #pragma unroll
-            for (int c = 0; c < 64; ++c)
+            for (int c = 0; c < 32; ++c)
               if (c0 + c < nN) atomicAdd(Vs + (long)__ldg(fnn + c) * nbf, (double)acc[c]);
           }
         }
