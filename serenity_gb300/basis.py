@@ -8,6 +8,7 @@ exponent markers are read as ``E+``/``E-``, and each contraction is
 ``<nprim> <l-letter>`` followed by ``nprim`` pairs ``exponent coefficient``.
 Coefficients are passed on raw; normalisation happens in the library.
 """
+import functools
 import os
 import re
 
@@ -32,7 +33,17 @@ class BasisError(ValueError):
 
 
 def read_element(name, element, library=BASIS_DIR):
-    """Contractions ``[(l, exponents, coefficients), ...]`` of ``element`` in basis ``name``."""
+    """Contractions ``[(l, exponents, coefficients), ...]`` of ``element`` in basis ``name``
+    (parsed once per (file, element) and cached)."""
+    return [(l, list(e), list(c)) for l, e, c in _read_element_cached(name, element.lower(), library)]
+
+
+@functools.lru_cache(maxsize=None)
+def _read_element_cached(name, element, library):
+    return tuple((l, tuple(e), tuple(c)) for l, e, c in _parse_element(name, element, library))
+
+
+def _parse_element(name, element, library):
     path = os.path.join(library, name)
     if not os.path.exists(path):
         raise BasisError("Error while parsing basis file %s: file not found" % path)

@@ -63,7 +63,7 @@ static void radial(double alpha, int n, std::vector<double>& r, std::vector<doub
 }
 
 // Becke cell weight of candidate point i (one thread per point).
-__global__ void becke_kernel(int natoms, const double* __restrict__ A, const double* __restrict__ dist,
+__global__ void becke_kernel(int natoms, const double* __restrict__ A, const double* __restrict__ rdist,
                              const double* __restrict__ adj, const int* __restrict__ sig_off,
                              const int* __restrict__ sig_list, long npts, const double* __restrict__ pts,
                              const int* __restrict__ owner, const double* __restrict__ wref, int smoothing,
@@ -74,17 +74,27 @@ __global__ void becke_kernel(int natoms, const double* __restrict__ A, const dou
   const int k = owner[i];
   const int s0 = sig_off[k], s1 = sig_off[k + 1];
   double weight = wref[i], sum = 0.0;
+  const double dxk = A[3 * k] - gx, dyk = A[3 * k + 1] - gy, dzk = A[3 * k + 2] - gz;
+  const double rk = sqrt(dxk * dxk + dyk * dyk + dzk * dzk);
   for (int li = s0; li < s1; ++li) {
     const int l = sig_list[li];
     const double dxl = A[3 * l] - gx, dyl = A[3 * l + 1] - gy, dzl = A[3 * l + 2] - gz;
     const double rl = sqrt(dxl * dxl + dyl * dyl + dzl * dzl);
+    if (l != k) {
+      // the owner atom's factor first: for atoms far from the point it is exactly zero,
+      // and a zero factor makes the cell zero in any order of the product
+      const double mu = (rl - rk) * rdist[l + (long)natoms * k];
+      double nu = mu + adj[k + (long)natoms * l] * (1.0 - mu * mu);
+      for (int s = 0; s < smoothing; ++s) nu = (3.0 - nu * nu) * nu / 2.0;
+      if (0.5 * (1.0 - nu) == 0.0) continue;
+    }
     double cell = 1.0;
     for (int ji = s0; ji < s1 && cell != 0.0; ++ji) {
       const int j = sig_list[ji];
       if (j == l) continue;
       const double dxj = A[3 * j] - gx, dyj = A[3 * j + 1] - gy, dzj = A[3 * j + 2] - gz;
       const double rj = sqrt(dxj * dxj + dyj * dyj + dzj * dzj);
-      const double mu = (rl - rj) / dist[l + (long)natoms * j];
+      const double mu = (rl - rj) * rdist[l + (long)natoms * j];
       double nu = mu + adj[j + (long)natoms * l] * (1.0 - mu * mu);
       for (int s = 0; s < smoothing; ++s) nu = (3.0 - nu * nu) * nu / 2.0;
       cell *= 0.5 * (1.0 - nu);
@@ -196,12 +206,13 @@ extern "C" xcgpu_status xcgpu_grid_build(xcgpu_ctx* c, int natoms, const int* Z,
     }
   }
   // pair data
-  std::vector<double> dist((size_t)natoms * natoms), adj((size_t)natoms * natoms);
+  std::vector<double> dist((size_t)natoms * natoms), rdist((size_t)natoms * natoms), adj((size_t)natoms * natoms);
   for (int i = 0; i < natoms; ++i)
     for (int j = 0; j < natoms; ++j) {
       double s = 0;
       for (int q = 0; q < 3; ++q) s += (xyz[3 * i + q] - xyz[3 * j + q]) * (xyz[3 * i + q] - xyz[3 * j + q]);
       dist[i + (size_t)natoms * j] = std::sqrt(s);
+      rdist[i + (size_t)natoms * j] = i == j ? 0.0 : 1.0 / std::sqrt(s);
       const double chi = std::sqrt(kBraggSlaterR[Z[j]] / kBraggSlaterR[Z[i]]);
       const double u = (chi - 1) / (chi + 1);
       adj[j + (size_t)natoms * i] = std::min(0.5, std::max(-0.5, u / (u * u - 1)));
@@ -221,7 +232,7 @@ extern "C" xcgpu_status xcgpu_grid_build(xcgpu_ctx* c, int natoms, const int* Z,
     return c->cuda(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, c->stream), "grid upload");
   };
   xcgpu_status st = up(dA, A.data(), A.size() * 8);
-  if (!st) st = up(dD, dist.data(), dist.size() * 8);
+  if (!st) st = up(dD, rdist.data(), rdist.size() * 8);
   if (!st) st = up(dAdj, adj.data(), adj.size() * 8);
   if (!st) st = up(dSo, sig_off.data(), sig_off.size() * 4);
   if (!st) st = up(dSl, sig_list.data(), sig_list.size() * 4);

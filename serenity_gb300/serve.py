@@ -20,16 +20,22 @@ from . import xcgpu
 
 
 class Request:
+    """One Vxc request.  Its density matrix is the request payload: it is formed on the
+    GPU when the request arrives (seeded), so that only requests in the system hold one."""
     __slots__ = ("rid", "arrival", "key", "workload", "P_dev", "V_dev", "en_dev", "func", "done", "latency",
-                 "nbytes", "plan_slot", "exc", "nel")
+                 "nbytes", "plan_slot", "exc", "nel", "seed", "ready")
 
-    def __init__(self, rid, arrival, key, workload, P_dev, func):
+    def __init__(self, rid, arrival, key, workload, func, seed):
         self.rid, self.arrival, self.key, self.workload = rid, arrival, key, workload
-        self.P_dev, self.func = P_dev, func
-        self.V_dev = self.en_dev = None
+        self.func, self.seed = func, seed
+        self.P_dev = self.V_dev = self.en_dev = self.ready = None
         self.done = None
         self.latency = None
         self.exc = self.nel = None
+
+    def fresh(self):
+        """The same request, not yet served."""
+        return Request(self.rid, self.arrival, self.key, self.workload, self.func, self.seed)
 
 
 def _work_bytes(npts, nbf, nspin, gga, nblocks):
@@ -40,8 +46,8 @@ def _work_bytes(npts, nbf, nspin, gga, nblocks):
 class Resident:
     """Grid + basis of one geometry and its plan instances (one per concurrent use)."""
 
-    def __init__(self, ctx, w):
-        self.grid = xcgpu.Grid.build(ctx, w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
+    def __init__(self, ctx, w, grid=None):
+        self.grid = grid if grid is not None else xcgpu.Grid.build(ctx, w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
         self.basis = xcgpu.Basis(ctx, w.shells)
         self.plans = []
         self.busy = set()
@@ -73,6 +79,7 @@ class Server:
         self.streams = [torch.cuda.Stream() for _ in range(nstreams)]
         self.setup_stream = torch.cuda.Stream()
         self.cache = collections.OrderedDict()
+        self.grids = {}  # geometry -> grid, shared by the bases of that geometry
         self.inflight = []
         self.reserved = 0
 
@@ -81,7 +88,10 @@ class Server:
         r = self.cache.get(key)
         if r is None:
             self.ctx.set_stream(self.setup_stream.cuda_stream)
-            r = Resident(self.ctx, w)
+            gkey = key[0]
+            if gkey not in self.grids:
+                self.grids[gkey] = xcgpu.Grid.build(self.ctx, w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
+            r = Resident(self.ctx, w, self.grids[gkey])
             self.cache[key] = r
         self.cache.move_to_end(key)
         return r
@@ -97,11 +107,21 @@ class Server:
             self.cache.pop(key)
 
     # -- batches --------------------------------------------------------------------------
+    def _arrive(self, rq):
+        """Form the request's density matrix on the setup stream (no host synchronisation)."""
+        torch = self.torch
+        r = self.resident(rq.key, rq.workload)
+        with torch.cuda.stream(self.setup_stream):
+            rq.P_dev = density_on_gpu(r.S, rq.workload.nocc, rq.seed)
+            rq.ready = torch.cuda.Event()
+            rq.ready.record(self.setup_stream)
+
     def _launch(self, batch, stream):
         torch = self.torch
         items = []
         with torch.cuda.stream(stream):
             for rq in batch:
+                stream.wait_event(rq.ready)
                 w = rq.workload
                 rq.V_dev = torch.empty_like(rq.P_dev)
                 rq.en_dev = torch.empty(2, dtype=torch.float64, device="cuda")
@@ -112,7 +132,7 @@ class Server:
         ev.record(stream)
         self.inflight.append((batch, ev, stream))
 
-    def _retire(self, now_fn):
+    def _retire(self, now_fn, keep_results):
         keep = []
         for batch, ev, stream in self.inflight:
             if ev.query():
@@ -126,13 +146,17 @@ class Server:
                     if r is not None:
                         r.release(i)
                     self.reserved -= rq.nbytes
+                    if not keep_results:
+                        rq.P_dev = rq.V_dev = None
                 yield batch
             else:
                 keep.append((batch, ev, stream))
         self.inflight = keep
 
-    def run(self, requests, on_complete=None):
-        """Serve requests (sorted by arrival, seconds from start).  Returns stats."""
+    def run(self, requests, on_complete=None, keep_results=True):
+        """Serve requests (sorted by arrival, seconds from start).  Returns stats.  With
+        keep_results False a request's P and V are dropped when it completes (E_xc and
+        N_el stay in en_dev)."""
         pending = collections.deque()
         todo = collections.deque(sorted(requests, key=lambda r: r.arrival))
         t0 = time.perf_counter()
@@ -142,8 +166,10 @@ class Server:
         while todo or pending or self.inflight:
             t = now()
             while todo and todo[0].arrival <= t:
-                pending.append(todo.popleft())
-            for batch in self._retire(now):
+                rq = todo.popleft()
+                self._arrive(rq)
+                pending.append(rq)
+            for batch in self._retire(now, keep_results):
                 completed += len(batch)
                 if on_complete:
                     on_complete(batch)
@@ -179,17 +205,21 @@ class Server:
 
 
 def density_on_gpu(S_dev, nocc, seed):
-    """Random orthonormalised density P = 2 C C^T (restricted) on the GPU, column-major."""
+    """Random orthonormalised density on the GPU: P = 2 C (C^T S C)^-1 C^T for a seeded
+    Gaussian C (the projector onto span C, the same P as Loewdin-orthonormalising C),
+    symmetrised, returned in FP64 as [1, n, n].  This is synthetic request input, formed
+    with FP32 GEMMs (the FP64 form cost a third of the serving run's GPU time); Cholesky
+    without an info check keeps the host unsynchronised."""
     import torch
     g = torch.Generator(device="cuda")
     g.manual_seed(seed)
     n = S_dev.shape[0]
-    C = torch.randn(n, nocc, generator=g, device="cuda", dtype=torch.float64)
-    M = C.T @ S_dev @ C
-    e, U = torch.linalg.eigh(M)
-    C = C @ (U * e.rsqrt()) @ U.T
-    P = 2.0 * C @ C.T
-    return P.T.contiguous().reshape(1, n, n)
+    S = S_dev.to(torch.float32)
+    C = torch.randn(n, nocc, generator=g, device="cuda", dtype=torch.float32)
+    L, _ = torch.linalg.cholesky_ex(C.T @ (S @ C))
+    P = 2.0 * C @ torch.cholesky_solve(C.T.contiguous(), L)
+    P = (0.5 * (P + P.T)).to(torch.float64)
+    return P.contiguous().reshape(1, n, n)
 
 
 def overlap_on_gpu(ctx, resident, n):
@@ -204,23 +234,28 @@ def overlap_on_gpu(ctx, resident, n):
     return resident.S
 
 
-def make_requests(server, n=2000, rate=200.0, seed=0, max_waters=128, n_rad=50, n_ang=194):
-    """Poisson stream: sizes 1..max_waters log-uniform, def2-SVP / def2-TZVP 70/30, LDA / PBE
-    50/50, each with its own random orthonormalised P (generated on the GPU up front)."""
+def make_requests(server, n=2000, rate=200.0, seed=0, max_waters=128, n_rad=50, n_ang=110, geometries=32):
+    """Poisson stream: cluster sizes 1..max_waters log-uniform, def2-SVP / def2-TZVP 70/30,
+    LDA / PBE 50/50, each request with its own random orthonormalised P (seeded; formed on
+    arrival).  Requests draw their cluster from a pool of `geometries` clusters whose sizes
+    are themselves drawn log-uniform, so geometries repeat and stay resident.  The pool is
+    made resident here (grid, basis, plan, overlap for the P generator); returns
+    (requests, setup seconds)."""
     rng = np.random.default_rng(seed)
+    pool = [int(round(math.exp(rng.uniform(0.0, math.log(max_waters))))) for _ in range(geometries)]
     t = 0.0
     reqs = []
+    t0 = time.perf_counter()
     for i in range(n):
         t += rng.exponential(1.0 / rate)
-        m = int(round(math.exp(rng.uniform(0.0, math.log(max_waters)))))
+        m = pool[int(rng.integers(len(pool)))]
         basis = "DEF2-SVP" if rng.uniform() < 0.7 else "DEF2-TZVP"
         func = "LDA" if rng.uniform() < 0.5 else "PBE"
         key = (m, basis)
         sym, xyz = wl.water_cluster(m, seed=1000 + m, jitter=0.2)
         w = wl.Workload(sym, xyz, basis, func, 5 * m, n_rad, n_ang, seed)
         r = server.resident(key, w)
-        S = overlap_on_gpu(server.ctx, r, w.nbf)
-        P = density_on_gpu(S, 5 * m, seed * 100000 + i)
-        reqs.append(Request(i, t, key, w, P, func))
+        overlap_on_gpu(server.ctx, r, w.nbf)
+        reqs.append(Request(i, t, key, w, func, seed * 100000 + i))
     server.ctx.set_stream(server.streams[0].cuda_stream)
-    return reqs
+    return reqs, time.perf_counter() - t0

@@ -56,7 +56,7 @@ def test_graph_replay_and_loop(ctx):
 def test_serving_results_same_alone_and_in_the_mix(ctx):
     from serenity_gb300 import serve, xcgpu
     server = serve.Server(ctx, hbm_budget=8 << 30, max_batch=4, nstreams=2)
-    reqs = serve.make_requests(server, n=14, rate=2000.0, seed=3, max_waters=6, n_rad=30, n_ang=110)
+    reqs, _ = serve.make_requests(server, n=14, rate=2000.0, seed=3, max_waters=6, n_rad=30, n_ang=110)
     stats = server.run(reqs)
     assert stats["requests"] == 14 and stats["batches"] >= 2
     for rq in reqs:
