@@ -138,14 +138,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// TF32 split of an FP32 value: hi = round-to-nearest TF32(x), lo = TF32(x - hi).
+// Round an FP32 bit pattern to TF32 (10 stored mantissa bits), to nearest with ties
+// away from zero: adding half a TF32 unit (bit 12) to the sign-magnitude pattern carries
+// into bit 13 exactly when the dropped magnitude is at least half a unit (a carry out of
+// the mantissa steps the exponent, which is the correctly rounded result); then clear the
+// 13 dropped bits.  Two integer operations instead of a conversion instruction.
+__device__ __forceinline__ uint32_t round_tf32(float x) { return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u; }
+
+// TF32 split of an FP32 value: hi = round-to-nearest TF32(x), lo = TF32(x - hi) (x - hi
+// is exact in FP32).
 __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
-  uint32_t h, l;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
-  const float r = x - __uint_as_float(h);
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+  const uint32_t h = round_tf32(x);
   hi = h;
-  lo = l;
+  lo = round_tf32(x - __uint_as_float(h));
 }
 // same for an FP64 value (the remainder is taken in FP64 before rounding)
 __device__ __forceinline__ void split_tf32(double x, uint32_t& hi, uint32_t& lo) {

@@ -468,7 +468,7 @@ done:
 //      MMAs; all threads drain the finished step's accumulator into registers; at the
 //      end of a tile pair the sums go to V with FP64 atomics.
 // =====================================================================================
-template <int DERIV>
+template <int DERIV, bool TWO_SPINS>
 __global__ void __launch_bounds__(kT, 1)
     mx_adder_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
@@ -540,20 +540,22 @@ __global__ void __launch_bounds__(kT, 1)
     __syncthreads();
     // ---- 1. operand tiles of the block ----
     {
-      const int p = tid & 127, quarter = tid >> 7;
+      const int p = tid & 127;
       const int kc = p >> 5, k = p & 31;
       if (kc < nkc) {  // warp-uniform
         const bool live = p < npts;
         const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
         const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
-        float wsp[2][4];
+        constexpr int NS = TWO_SPINS ? 2 : 1;
+        float wsp[NS][4];
 #pragma unroll
-        for (int s = 0; s < 2; ++s)
+        for (int s = 0; s < NS; ++s)
 #pragma unroll
           for (int c = 0; c < 4; ++c) wsp[s][c] = s_w[s][c][p];
-        const bool sp0 = smask & 1, sp1 = (smask >> 1) & 1;
+        const bool sp0 = smask & 1, sp1 = TWO_SPINS && ((smask >> 1) & 1);
         const int kq = k >> 2, kr = k & 3;
         float* const base = my + kc * 2 * kTileFloats + kr;
+        const int quarter = tid >> 7;
         ShellRec next;
         if (s0 + quarter < s1) next = load_rec(P.rec + s0 + quarter);
         for (int si = s0 + quarter; si < s1; si += kQ) {
@@ -569,9 +571,9 @@ __global__ void __launch_bounds__(kT, 1)
               if (DERIV) gv += wsp[0][1] * dx + wsp[0][2] * dy + wsp[0][3] * dz;
               st_split(t + opstride, gv);
             }
-            if (sp1) {
-              float gv = wsp[1][0] * val;
-              if (DERIV) gv += wsp[1][1] * dx + wsp[1][2] * dy + wsp[1][3] * dz;
+            if (TWO_SPINS && sp1) {
+              float gv = wsp[NS - 1][0] * val;
+              if (DERIV) gv += wsp[NS - 1][1] * dx + wsp[NS - 1][2] * dy + wsp[NS - 1][3] * dz;
               st_split(t + 2 * opstride, gv);
             }
           };
@@ -739,8 +741,10 @@ xcgpu_status mixed_init(Ctx* c) {
     const char* what;
   } k[] = {{(const void*)mx_density_kernel<0>, density_smem(), "density smem attribute"},
            {(const void*)mx_density_kernel<1>, density_smem(), "density smem attribute"},
-           {(const void*)mx_adder_kernel<0>, adder_smem(), "adder smem attribute"},
-           {(const void*)mx_adder_kernel<1>, adder_smem(), "adder smem attribute"}};
+           {(const void*)mx_adder_kernel<0, false>, adder_smem(), "adder smem attribute"},
+           {(const void*)mx_adder_kernel<1, false>, adder_smem(), "adder smem attribute"},
+           {(const void*)mx_adder_kernel<0, true>, adder_smem(), "adder smem attribute"},
+           {(const void*)mx_adder_kernel<1, true>, adder_smem(), "adder smem attribute"}};
   for (const auto& e : k) {
     xcgpu_status st =
         c->cuda(cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.bytes), e.what);
@@ -847,10 +851,12 @@ xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* 
     if ((st = batch_scratch(c, work, i0, i1, bt))) return st;
     if ((st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter"))) return st;
     KernelTimer kt(c, kAdder);
-    if (any_gga(work, i0, i1, false))
-      mx_adder_kernel<1><<<c->sm_count, kT, adder_smem(), c->stream>>>(bt, counter, err);
-    else
-      mx_adder_kernel<0><<<c->sm_count, kT, adder_smem(), c->stream>>>(bt, counter, err);
+    bool two = false;
+    for (size_t i = i0; i < i1; ++i) two = two || work[i].nspin == 2;
+    const bool gga = any_gga(work, i0, i1, false);
+    auto* kern = gga ? (two ? mx_adder_kernel<1, true> : mx_adder_kernel<1, false>)
+                     : (two ? mx_adder_kernel<0, true> : mx_adder_kernel<0, false>);
+    kern<<<c->sm_count, kT, adder_smem(), c->stream>>>(bt, counter, err);
     if ((st = c->check_launch("mx_adder_kernel"))) return st;
   }
   KernelTimer kt2(c, kOther);
