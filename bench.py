@@ -31,6 +31,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "XC builds/s & Mpts/s, (H2O)32 PBE, mixed vs FP64 GPU at 1e-7 Eh; p50/p99 latency"
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the mixed kernels on the
+# (H2O)32 workload, from one ncu --set full capture (profiles/mx_kernels_h2o32_pbe.md)
+MIXED_DRAM_BYTES = {"density": 120.1e6 + 546.5e6, "adder": 209.1e6 + 756.1e6}
 WORKLOAD = "(H2O)32 def2-SVP PBE restricted, 75x302 Becke grid, 128-point blocks"
 
 
@@ -373,7 +376,10 @@ def main():
             if name == "mixed":
                 peak = peaks.get("bf16_tflops_sustained")
                 roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                        "frac": (achieved / peak) if peak else None, "traffic": None,
+                        "frac": (achieved / peak) if peak else None,
+                        "traffic": MIXED_DRAM_BYTES[names[dom]] if args.config == 1 else None,
+                        "traffic_note": "DRAM read + write bytes per launch of this kernel on this workload, "
+                                        "one ncu capture (profiles/mx_kernels_h2o32_pbe.md)",
                         "note": "useful FP32-equivalent flops (2 npts n_b^2 per block) of the dominant kernel "
                                 "over its CUDA-event time; peak = measured cuBLAS bf16 sustained (of measured). "
                                 "3xTF32 issues 3 TF32 MMAs per product at half the bf16 rate, so its useful "
