@@ -7,6 +7,7 @@
  *   FunctionalLibrary<M>              src/dft/functionals/FunctionalLibrary.h:51-64
  *   ScalarOperatorToMatrixAdder<M>    src/data/grid/ScalarOperatorToMatrixAdder.h:56-93
  *   FuncPotential<M> (getMatrix, getEnergy)  src/potentials/FuncPotential.h
+ *   NAddFuncPotential<M> (getMatrix, getEnergy)  src/potentials/NAddFuncPotential.h
  *
  * Errors are thrown as SerenityError, as in the reference.  Matrices and grid data are
  * plain column-major containers with the memory layout of Eigen's defaults
@@ -444,6 +445,51 @@ class FuncPotential {
   double thr_;
   int precision_;
   double energy_ = 0.0, nel_ = 0.0;
+};
+
+// NAddFuncPotential<M> (src/potentials/NAddFuncPotential.h:93-200): the non-additive XC
+// potential of an active subsystem in the field of environment subsystems, all densities
+// on the active system's grid.  getMatrix(P_active, P_env) returns the potential in the
+// active basis (NAddFuncPotential.cpp:189-243); getEnergy() the non-additive energy
+// E_xc[sum] - E_xc[active] - sum E_xc[env] of that call.  Environment controllers must be
+// built on the same grid controller as the active one.
+template <Options::SCF_MODES M>
+class NAddFuncPotential {
+ public:
+  NAddFuncPotential(std::shared_ptr<BasisFunctionOnGridController> active,
+                    std::vector<std::shared_ptr<BasisFunctionOnGridController>> env, Functional f,
+                    double blockAveThreshold = 1e-11, int precision = XCGPU_PREC_FP64)
+      : active_(active), env_(std::move(env)), f_(f), thr_(blockAveThreshold), precision_(precision) {}
+  FockMatrix<M> getMatrix(const DensityMatrix<M>& P, const std::vector<DensityMatrix<M>>& Penv) {
+    if (Penv.size() != env_.size()) throw SerenityError("NAddFuncPotential: one density matrix per environment system");
+    const int ns = detail::nspin<M>();
+    const long nbf = active_->getNBasisFunctions();
+    std::vector<double> Pv, Vv((size_t)ns * nbf * nbf);
+    detail::pack(P, Pv);
+    std::vector<std::vector<double>> Pe(env_.size());
+    std::vector<xcgpu_plan*> plans;
+    std::vector<const double*> ptrs;
+    for (size_t i = 0; i < env_.size(); ++i) {
+      detail::pack(Penv[i], Pe[i]);
+      plans.push_back(env_[i]->handle());
+      ptrs.push_back(Pe[i].data());
+    }
+    detail::check(active_->ctx(), xcgpu_nadd_vxc(active_->handle(), plans.data(), (uint32_t)plans.size(), (int)f_, ns,
+                                                 precision_, thr_, Pv.data(), ptrs.data(), Vv.data(), &energy_,
+                                                 XCGPU_MEM_HOST));
+    FockMatrix<M> F = P;
+    detail::unpack(Vv.data(), F);
+    return F;
+  }
+  double getEnergy() const { return energy_; }
+
+ private:
+  std::shared_ptr<BasisFunctionOnGridController> active_;
+  std::vector<std::shared_ptr<BasisFunctionOnGridController>> env_;
+  Functional f_;
+  double thr_;
+  int precision_;
+  double energy_ = 0.0;
 };
 
 }  // namespace Serenity

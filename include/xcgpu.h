@@ -111,6 +111,15 @@ xcgpu_status xcgpu_grid_create(xcgpu_ctx* ctx, const double* xyz, const double* 
 xcgpu_status xcgpu_grid_build(xcgpu_ctx* ctx, int natoms, const int* Z, const double* xyz_bohr, int n_rad, int n_ang,
                               int accuracy, double weight_threshold, int smoothing, int sort,
                               const char* lebedev_table, xcgpu_grid** out);
+/* Atom partition of the grid weights (Options::GRID_TYPES, GridFactory.cpp:176-268). */
+enum {
+  XCGPU_PARTITION_BECKE = 0, /* Becke cells with size adjustment and `smoothing` iterations */
+  XCGPU_PARTITION_SSF = 1    /* Stratmann-Scuseria-Frisch (a = 0.64, no size adjustment, smoothing unused) */
+};
+/* xcgpu_grid_build with the partition chosen (the reference's GRIDTYPE setting). */
+xcgpu_status xcgpu_grid_build_partition(xcgpu_ctx* ctx, int natoms, const int* Z, const double* xyz_bohr, int n_rad,
+                                        int n_ang, int accuracy, double weight_threshold, int partition, int smoothing,
+                                        int sort, const char* lebedev_table, xcgpu_grid** out);
 uint64_t xcgpu_grid_npoints(const xcgpu_grid* grid);
 xcgpu_status xcgpu_grid_copy(const xcgpu_grid* grid, double* xyz, double* w); /* to host */
 void xcgpu_grid_destroy(xcgpu_grid* grid);
@@ -189,6 +198,21 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* plan, double block_ave_threshold, int 
  * Nel = sum_p w_p rho_p (total density).  P, V in `mem` space; Exc, Nel host scalars. */
 xcgpu_status xcgpu_vxc(xcgpu_plan* plan, int func, int nspin, int precision, double block_ave_threshold,
                        const double* P, double* V, double* Exc, double* Nel, int mem);
+
+/* ---- non-additive XC potential of subsystem DFT (frozen-density embedding) -----------
+ * NAddFuncPotential<M>::getMatrix / getEnergy (NAddFuncPotential.cpp:189-243, 297-318) with
+ * the supersystem density of SupersystemDensityOnGridController.cpp:101-187: every
+ * subsystem's density is formed from its own basis and density matrix on the active
+ * system's grid (all plans share one grid; one batched launch in mixed precision), then
+ *   rho_tot = rho_active + sum_i rho_env_i,
+ *   V       = adder_active(dF/drho[rho_tot] - dF/drho[rho_active], same for dF/d grad rho),
+ *   E_nadd  = E_xc[rho_tot] - E_xc[rho_active] - sum_i E_xc[rho_env_i].
+ * P_active: nspin column-major matrices of the active basis; P_env[i] those of env[i]'s
+ * basis; V (nspin, active basis) is overwritten; all in `mem` space; E_nadd a host scalar.
+ * The exact-exchange part of hybrid functionals (integrals) is not part of this path. */
+xcgpu_status xcgpu_nadd_vxc(xcgpu_plan* active, xcgpu_plan* const* env, uint32_t n_env, int func, int nspin,
+                            int precision, double block_ave_threshold, const double* P_active,
+                            const double* const* P_env, double* V, double* E_nadd, int mem);
 
 /* ---- batched builds (many subsystems, e.g. a freeze-and-thaw step) -------------------
  * All requests run as one persistent launch per heavy stage (mixed precision) on the

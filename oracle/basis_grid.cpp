@@ -378,8 +378,43 @@ void hilbert_sort(std::vector<double>& pts, std::vector<double>& w) {
   w.swap(w2);
 }
 
+// Stratmann-Scuseria-Frisch weight of a point of atom k (GridFactory.cpp:209-268): untouched
+// inside 0.5 (1 - a) of the nearest-neighbour distance, zero once some nu_kj >= a, otherwise
+// the cell products with the piecewise polynomial of SSF Eq. (14), a = 0.64, no size
+// adjustment, over all atoms.  Returns false when the point is screened out.
+static bool ssf_weight(int natoms, int k, const std::vector<double>& rd, const std::vector<double>& dist,
+                       double min_dist, double& weight) {
+  constexpr double a = 0.64;
+  if (!(rd[k] >= 0.5 * (1.0 - a) * min_dist)) return true;
+  for (int j = 0; j < natoms; ++j) {
+    const double nu = (rd[k] - rd[j]) / dist[k + natoms * j];  // j == k: 0/0, compares false
+    if (nu >= a) return false;
+  }
+  double sum = 0.0;
+  for (int i = 0; i < natoms; ++i) {
+    double cell = 1.0;
+    for (int j = 0; j < natoms; ++j) {
+      if (i == j) continue;
+      double nu = (rd[i] - rd[j]) / dist[i + natoms * j];
+      if (nu <= -a) continue;
+      if (nu >= a) {
+        cell = 0.0;
+        break;
+      }
+      nu /= a;
+      const double n3 = nu * nu * nu;
+      const double poly = (-5.0 * n3 * n3 * nu + 21.0 * n3 * nu * nu - 35.0 * n3 + 35.0 * nu) / 16.0;
+      cell *= 0.5 * (1 - poly);
+    }
+    if (i == k) weight *= cell;
+    sum += cell;
+  }
+  weight /= sum;
+  return true;
+}
+
 long becke_grid(int natoms, const int* Z, const double* xyz, int n_rad, int n_ang, int acc, double wthr, int smoothing,
-                int sort, const char* lebedev_path, std::vector<double>& outp, std::vector<double>& outw) {
+                int sort, const char* lebedev_path, std::vector<double>& outp, std::vector<double>& outw, int partition) {
   Lebedev leb(lebedev_path);
   std::vector<double> dist(natoms * natoms);
   for (int i = 0; i < natoms; ++i)
@@ -404,8 +439,11 @@ long becke_grid(int natoms, const int* Z, const double* xyz, int n_rad, int n_an
     std::vector<double> rp, rw;
     atom_grid(leb, Z[k], n_rad, n_ang, acc, rp, rw);
     std::vector<int> sig;
-    for (int l = 0; l < natoms; ++l)
+    double min_dist = 999999999.9;
+    for (int l = 0; l < natoms; ++l) {
       if (dist[l + natoms * k] < 40.0) sig.push_back(l);
+      if (l != k) min_dist = std::min(min_dist, dist[l + natoms * k]);
+    }
     std::vector<double> rd(natoms);
     for (size_t i = 0; i < rw.size(); ++i) {
       const double g[3] = {rp[3 * i] + xyz[3 * k], rp[3 * i + 1] + xyz[3 * k + 1], rp[3 * i + 2] + xyz[3 * k + 2]};
@@ -415,19 +453,23 @@ long becke_grid(int natoms, const int* Z, const double* xyz, int n_rad, int n_an
         for (int c = 0; c < 3; ++c) s += (xyz[3 * l + c] - g[c]) * (xyz[3 * l + c] - g[c]);
         rd[l] = std::sqrt(s);
       }
-      double sum = 0.0;
-      for (int l : sig) {
-        double cell = 1.0;
-        for (int j : sig) {
-          if (l == j) continue;
-          const double mu = (rd[l] - rd[j]) / dist[l + natoms * j];
-          const double nu = mu + a[j + natoms * l] * (1.0 - mu * mu);
-          cell *= 0.5 * (1 - becke_p(nu, smoothing));
+      if (partition == 1) {
+        if (!ssf_weight(natoms, k, rd, dist, min_dist, weight)) continue;
+      } else {
+        double sum = 0.0;
+        for (int l : sig) {
+          double cell = 1.0;
+          for (int j : sig) {
+            if (l == j) continue;
+            const double mu = (rd[l] - rd[j]) / dist[l + natoms * j];
+            const double nu = mu + a[j + natoms * l] * (1.0 - mu * mu);
+            cell *= 0.5 * (1 - becke_p(nu, smoothing));
+          }
+          if (l == k) weight *= cell;
+          sum += cell;
         }
-        if (l == k) weight *= cell;
-        sum += cell;
+        weight /= sum;
       }
-      weight /= sum;
       if (weight > wthr) {
         aw[k].push_back(weight);
         apts[k].insert(apts[k].end(), g, g + 3);
@@ -467,9 +509,10 @@ int orc_block_on_grid(const void* basis, const double* xyz, int npts, double thr
 
 long orc_becke_grid(int natoms, const int* Z, const double* xyz, int n_rad, int n_ang, int accuracy,
                     double weight_threshold, int smoothing, int sort, const char* lebedev_path, double* out_xyz,
-                    double* out_w, long capacity) {
+                    double* out_w, long capacity, int partition) {
   std::vector<double> p, w;
-  long n = orc::becke_grid(natoms, Z, xyz, n_rad, n_ang, accuracy, weight_threshold, smoothing, sort, lebedev_path, p, w);
+  long n = orc::becke_grid(natoms, Z, xyz, n_rad, n_ang, accuracy, weight_threshold, smoothing, sort, lebedev_path, p, w,
+                           partition);
   if (n > capacity) return -1;
   std::memcpy(out_xyz, p.data(), sizeof(double) * 3 * n);
   std::memcpy(out_w, w.data(), sizeof(double) * n);

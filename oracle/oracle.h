@@ -85,7 +85,7 @@ int orc_vxc(const void* basis, const double* xyz, const double* w, long npts, in
  * the node table.  Returns the number of points written (<= capacity), or -1. */
 long orc_becke_grid(int natoms, const int* Z, const double* xyz, int n_rad, int n_ang, int accuracy,
                     double weight_threshold, int smoothing, int sort, const char* lebedev_path, double* out_xyz,
-                    double* out_w, long capacity);
+                    double* out_w, long capacity, int partition /* 0 Becke, 1 SSF */);
 
 /* Ahlrichs M3 radial rule (AtomGridFactory.cpp:238-260). */
 void orc_ahlrichs_radial(double alpha, int n, double* r, double* w);

@@ -51,7 +51,7 @@ def lib():
         L.orc_becke_grid.restype = ctypes.c_long
         L.orc_becke_grid.argtypes = [ctypes.c_int, _ip, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, _dp, _dp,
-                                     ctypes.c_long]
+                                     ctypes.c_long, ctypes.c_int]
         L.orc_ahlrichs_radial.argtypes = [ctypes.c_double, ctypes.c_int, _dp, _dp]
         L.orc_solid_harmonics.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp]
         _lib = L
@@ -147,8 +147,11 @@ def functional(func, rho, grad=None, max_block=0):
     return epuv, dr.reshape(nspin, n), (dg.reshape(nspin, 3, n) if gga else None)
 
 
+PARTITION = {"becke": 0, "ssf": 1}
+
+
 def becke_grid(Z, xyz_bohr, n_rad=0, n_ang=0, accuracy=0, weight_threshold=1e-14, smoothing=3, sort=True,
-               lebedev_path=None):
+               lebedev_path=None, partition="becke"):
     from serenity_gb300.basis import LEBEDEV_TABLE
     Z = np.ascontiguousarray(Z, dtype=np.int32)
     xyz = np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1)
@@ -157,7 +160,7 @@ def becke_grid(Z, xyz_bohr, n_rad=0, n_ang=0, accuracy=0, weight_threshold=1e-14
     out_w = np.zeros(cap)
     path = (lebedev_path or LEBEDEV_TABLE).encode()
     n = lib().orc_becke_grid(len(Z), Z, xyz, n_rad, n_ang, accuracy, weight_threshold, smoothing, int(sort), path,
-                             out_x, out_w, cap)
+                             out_x, out_w, cap, PARTITION[partition])
     if n < 0:
         raise RuntimeError("grid capacity exceeded")
     return out_x[:3 * n].reshape(n, 3).copy(), out_w[:n].copy()
@@ -173,3 +176,29 @@ def solid_harmonics(l, x, y, z):
     out = np.zeros(2 * l + 1)
     lib().orc_solid_harmonics(l, x, y, z, out)
     return out
+
+
+def nadd_vxc(active, envs, xyz, w, func, P_active, P_envs, max_block=128, thr=1e-9, ave_thr=1e-11):
+    """Non-additive XC potential and energy of subsystem DFT, composed from the oracle's
+    density, functional and adder as NAddFuncPotential<M>::getMatrix does
+    (NAddFuncPotential.cpp:189-243; the supersystem density is the plain sum of the
+    subsystem densities, SupersystemDensityOnGridController.cpp:101-187):
+        V = adder_active(dF/drho[rho_tot] - dF/drho[rho_act], dF/dgrad[tot] - dF/dgrad[act])
+        E = E_xc[rho_tot] - E_xc[rho_act] - sum_env E_xc[rho_env]
+    active, envs: Basis objects; P_*: [nbf, nbf] or [nspin, nbf, nbf].  Returns (V, E)."""
+    w = np.asarray(w, dtype=np.float64)
+    gga = bool(lib().orc_functional_is_gga(FUNC[func] if isinstance(func, str) else int(func)))
+    rA, gA = active.density(xyz, P_active, max_block, thr, grad=gga)
+    rT = rA.copy()
+    gT = gA.copy() if gga else None
+    e_env = 0.0
+    for B, P in zip(envs, P_envs):
+        r, g = B.density(xyz, P, max_block, thr, grad=gga)
+        rT += r
+        if gga:
+            gT += g
+        e_env += float(w @ functional(func, r, g, max_block)[0])
+    eT, vT, gvT = functional(func, rT, gT, max_block)
+    eA, vA, gvA = functional(func, rA, gA, max_block)
+    V = active.add_scalar(xyz, w, vT - vA, (gvT - gvA) if gga else None, max_block, thr, ave_thr)
+    return V, float(w @ eT) - float(w @ eA) - e_env

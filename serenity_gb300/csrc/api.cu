@@ -888,6 +888,141 @@ xcgpu_status xcgpu_vxc_batch(xcgpu_ctx* c, const xcgpu_request* reqs, uint32_t n
   return XCGPU_OK;
 }
 
+xcgpu_status xcgpu_nadd_vxc(xcgpu_plan* A, xcgpu_plan* const* env, uint32_t n_env, int func, int nspin,
+                            int precision, double thr, const double* P_active, const double* const* P_env, double* V,
+                            double* E_nadd, int mem) {
+  if (!A) return XCGPU_ERR_INVALID;
+  Ctx* c = A->ctx;
+  if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "nadd: unknown functional");
+  if ((nspin != 1 && nspin != 2) || !P_active || !V || (n_env > 0 && (!env || !P_env)))
+    return c->fail(XCGPU_ERR_INVALID, "nadd: bad arguments");
+  if (precision != XCGPU_PREC_FP64 && precision != XCGPU_PREC_MIXED)
+    return c->fail(XCGPU_ERR_INVALID, "nadd: unknown precision");
+  std::vector<xcgpu_plan*> plans(1, A);
+  std::vector<const double*> Psrc(1, P_active);
+  for (uint32_t i = 0; i < n_env; ++i) {
+    if (!env[i] || !P_env[i]) return c->fail(XCGPU_ERR_INVALID, "nadd: null environment plan or density matrix");
+    if (env[i]->ctx != c) return c->fail(XCGPU_ERR_INVALID, "nadd: environment plan of another context");
+    if (env[i]->grid != A->grid)  // SupersystemDensityOnGridController.cpp:49 (isDefinedOnSameGrid)
+      return c->fail(XCGPU_ERR_INVALID, "nadd: all subsystem densities must live on the active system's grid");
+    for (auto* q : plans)
+      if (q == env[i]) return c->fail(XCGPU_ERR_INVALID, "nadd: one plan per subsystem (a plan appears twice)");
+    plans.push_back(env[i]);
+    Psrc.push_back(P_env[i]);
+  }
+  cudaSetDevice(c->device);
+  const bool gga = xc::is_gga(func), mixed = precision == XCGPU_PREC_MIXED;
+  const long n = A->grid->n;
+  const int nbfA = A->basis->nbf;
+  for (auto* q : plans) XC_TRY(ensure_work(q, nspin, gga, mixed));
+  std::vector<const double*> Pd(plans.size());
+  for (size_t i = 0; i < plans.size(); ++i) {
+    const size_t cnt = (size_t)nspin * plans[i]->basis->nbf * plans[i]->basis->nbf;
+    if (mem == XCGPU_MEM_HOST) {
+      XC_TRY(upload(c, plans[i]->w_P, Psrc[i], cnt));
+      Pd[i] = plans[i]->w_P.as<double>();
+    } else {
+      Pd[i] = Psrc[i];
+    }
+  }
+  int* counter = nullptr;
+  XC_TRY(c->aux(&counter));
+  int* err = counter + 2;
+  XC_TRY(c->cuda(cudaMemsetAsync(counter, 0, 4 * sizeof(int), c->stream), "memset aux"));
+  // 1. every subsystem's density on the shared grid (one batched launch in mixed precision)
+  if (mixed) {
+    std::vector<MixedWork> work;
+    for (size_t i = 0; i < plans.size(); ++i) {
+      xcgpu_plan* q = plans[i];
+      XC_TRY(mixed_split(c, Pd[i], q->w_psplit.as<float>(), (long)nspin * q->basis->nbf * q->basis->nbf));
+      work.push_back(MixedWork{&q->basis->dev, &q->dev, nspin, q->w_psplit.as<float>(), q->w_rho.as<double>(),
+                               gga ? q->w_grad.as<double>() : nullptr, nullptr, nullptr, nullptr, nullptr});
+    }
+    XC_TRY(mixed_density_batch(c, work, counter, err));
+  } else {
+    for (size_t i = 0; i < plans.size(); ++i)
+      XC_TRY(stage_density(plans[i], nspin, Pd[i], plans[i]->w_rho.as<double>(),
+                           gga ? plans[i]->w_grad.as<double>() : nullptr));
+  }
+  // 2. supersystem density: the sum of the subsystem densities
+  //    (SupersystemDensityOnGridController.cpp:101-187)
+  XC_TRY(A->n_rho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  XC_TRY(A->n_epuv.alloc(c, (size_t)n * sizeof(double)));
+  XC_TRY(A->n_dfdrho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  if (gga) {
+    XC_TRY(A->n_grad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+    XC_TRY(A->n_dfdgrad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+  }
+  XC_TRY(A->n_partials.alloc(c, 2 * ((n + 127) / 128) * sizeof(double) + 16));
+  XC_TRY(A->n_fskip.alloc(c, (size_t)(n + kSkipBlock - 1) / kSkipBlock + 1));
+  XC_TRY(A->n_sums.alloc(c, 2 * (plans.size() + 1) * sizeof(double)));
+  XC_TRY(c->cuda(cudaMemcpyAsync(A->n_rho.p, A->w_rho.p, (size_t)nspin * n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 c->stream), "supersystem density"));
+  if (gga)
+    XC_TRY(c->cuda(cudaMemcpyAsync(A->n_grad.p, A->w_grad.p, (size_t)nspin * 3 * n * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, c->stream), "supersystem gradient"));
+  for (size_t i = 1; i < plans.size(); ++i) {
+    XC_TRY(launch_axpy(c, (long)nspin * n, plans[i]->w_rho.as<double>(), A->n_rho.as<double>()));
+    if (gga) XC_TRY(launch_axpy(c, (long)nspin * 3 * n, plans[i]->w_grad.as<double>(), A->n_grad.as<double>()));
+  }
+  // 3. functional of the supersystem, of the active and of every environment density;
+  //    sums: [E, N] of the supersystem, of the active system, of environment i
+  double* sums = A->n_sums.as<double>();
+  auto functional = [&](const double* rho, const double* grad, double* epuv, double* dfdrho, double* dfdgrad,
+                        double* partials, unsigned char* fskip, double* out) -> xcgpu_status {
+    int nparts = 0;
+    xcgpu_status st = launch_functional(c, func, nspin, n, kSkipBlock, rho, gga ? grad : nullptr, epuv, dfdrho,
+                                        gga ? dfdgrad : nullptr, A->dev.w, partials, &nparts, fskip);
+    if (st) return st;
+    if (nparts) return launch_sum_partials(c, partials, nparts, 2, out);
+    return c->cuda(cudaMemsetAsync(out, 0, 2 * sizeof(double), c->stream), "memset sums");
+  };
+  XC_TRY(functional(A->n_rho.as<double>(), A->n_grad.as<double>(), A->n_epuv.as<double>(), A->n_dfdrho.as<double>(),
+                    A->n_dfdgrad.as<double>(), A->n_partials.as<double>(), A->n_fskip.as<unsigned char>(), sums));
+  for (size_t i = 0; i < plans.size(); ++i) {
+    xcgpu_plan* q = plans[i];
+    XC_TRY(functional(q->w_rho.as<double>(), q->w_grad.as<double>(), q->w_epuv.as<double>(), q->w_dfdrho.as<double>(),
+                      q->w_dfdgrad.as<double>(), q->w_partials.as<double>(), q->w_fskip.as<unsigned char>(),
+                      sums + 2 * (i + 1)));
+  }
+  // 4. potential difference on the grid (NAddFuncPotential.cpp:213-225)
+  XC_TRY(launch_scale_add(c, (long)nspin * n, -1.0, A->w_dfdrho.as<double>(), A->n_dfdrho.as<double>()));
+  if (gga) XC_TRY(launch_scale_add(c, (long)nspin * 3 * n, -1.0, A->w_dfdgrad.as<double>(), A->n_dfdgrad.as<double>()));
+  // 5. adder on the active basis
+  double* Vd = V;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(A->w_V.alloc(c, (size_t)nspin * nbfA * nbfA * sizeof(double)));
+    Vd = A->w_V.as<double>();
+  }
+  XC_TRY(c->cuda(cudaMemsetAsync(Vd, 0, (size_t)nspin * nbfA * nbfA * sizeof(double), c->stream), "memset V"));
+  const double* gv = gga ? A->n_dfdgrad.as<double>() : nullptr;
+  if (mixed) {
+    XC_TRY(launch_block_skip_flags(c, A->dev, nspin, A->n_dfdrho.as<double>(), gv, thr, A->w_skip.as<unsigned char>()));
+    std::vector<MixedWork> work(1);
+    work[0] = MixedWork{&A->basis->dev, &A->dev, nspin, nullptr, nullptr, nullptr, A->n_dfdrho.as<double>(), gv,
+                        A->w_skip.as<unsigned char>(), Vd};
+    XC_TRY(mixed_adder_batch(c, work, counter + 1, err));
+  } else {
+    XC_TRY(stage_adder(A, nspin, A->n_dfdrho.as<double>(), gv, thr, Vd));
+  }
+  std::vector<double> hs(2 * (plans.size() + 1));
+  int herr = 0;
+  XC_TRY(c->cuda(cudaMemcpyAsync(hs.data(), sums, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                 "sums"));
+  XC_TRY(c->cuda(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
+  if (mem == XCGPU_MEM_HOST)
+    XC_TRY(c->cuda(cudaMemcpyAsync(V, Vd, (size_t)nspin * nbfA * nbfA * sizeof(double), cudaMemcpyDeviceToHost,
+                                   c->stream), "V"));
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "nadd"));
+  if (herr) return device_error(c, herr, "nadd");
+  if (E_nadd) {
+    double e = hs[0] - hs[2];  // E_xc[rho_tot] - E_xc[rho_active]
+    for (size_t i = 1; i < plans.size(); ++i) e -= hs[2 * (i + 1)];
+    *E_nadd = e;
+  }
+  return XCGPU_OK;
+}
+
 xcgpu_status xcgpu_check_async(xcgpu_ctx* c) {
   if (!c) return XCGPU_ERR_INVALID;
   int herr = 0;

@@ -105,6 +105,57 @@ __global__ void becke_kernel(int natoms, const double* __restrict__ A, const dou
   wout[i] = weight / sum;
 }
 
+// Stratmann-Scuseria-Frisch weight of candidate point i (GridFactory.cpp:209-268): the
+// reference weight stays inside 0.5 (1 - a) of the owner's nearest-neighbour distance;
+// a point with some nu_kj >= a is dropped (NaN marker, removed by the weight cut);
+// otherwise the cell products with the SSF polynomial, a = 0.64, over all atoms.
+__global__ void ssf_kernel(int natoms, const double* __restrict__ A, const double* __restrict__ dist,
+                           const double* __restrict__ min_dist, long npts, const double* __restrict__ pts,
+                           const int* __restrict__ owner, const double* __restrict__ wref, double* __restrict__ wout) {
+  constexpr double a = 0.64;
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npts) return;
+  const double gx = pts[3 * i], gy = pts[3 * i + 1], gz = pts[3 * i + 2];
+  const int k = owner[i];
+  auto r = [&](int l) {
+    const double dx = A[3 * l] - gx, dy = A[3 * l + 1] - gy, dz = A[3 * l + 2] - gz;
+    return sqrt(dx * dx + dy * dy + dz * dz);
+  };
+  double weight = wref[i];
+  const double rk = r(k);
+  if (!(rk >= 0.5 * (1.0 - a) * min_dist[k])) {
+    wout[i] = weight;
+    return;
+  }
+  for (int j = 0; j < natoms; ++j) {
+    if ((rk - r(j)) / dist[k + (long)natoms * j] >= a) {  // j == k: 0/0 compares false
+      wout[i] = nan("");
+      return;
+    }
+  }
+  double sum = 0.0;
+  for (int l = 0; l < natoms; ++l) {
+    const double rl = r(l);
+    double cell = 1.0;
+    for (int j = 0; j < natoms; ++j) {
+      if (j == l) continue;
+      double nu = (rl - r(j)) / dist[l + (long)natoms * j];
+      if (nu <= -a) continue;
+      if (nu >= a) {
+        cell = 0.0;
+        break;
+      }
+      nu /= a;
+      const double n3 = nu * nu * nu;
+      const double poly = (-5.0 * n3 * n3 * nu + 21.0 * n3 * nu * nu - 35.0 * n3 + 35.0 * nu) / 16.0;
+      cell *= 0.5 * (1 - poly);
+    }
+    if (l == k) weight *= cell;
+    sum += cell;
+  }
+  wout[i] = weight / sum;
+}
+
 static void hilbert_order(const std::vector<double>& pts, std::vector<long>& order) {
   const long n = (long)pts.size() / 3;
   long length = 2, nvert = 8;
@@ -162,7 +213,16 @@ using namespace xcgpu;
 extern "C" xcgpu_status xcgpu_grid_build(xcgpu_ctx* c, int natoms, const int* Z, const double* xyz, int n_rad,
                                          int n_ang, int acc, double wthr, int smoothing, int sort, const char* table,
                                          xcgpu_grid** out) {
+  return xcgpu_grid_build_partition(c, natoms, Z, xyz, n_rad, n_ang, acc, wthr, XCGPU_PARTITION_BECKE, smoothing, sort,
+                                    table, out);
+}
+
+extern "C" xcgpu_status xcgpu_grid_build_partition(xcgpu_ctx* c, int natoms, const int* Z, const double* xyz,
+                                                   int n_rad, int n_ang, int acc, double wthr, int partition,
+                                                   int smoothing, int sort, const char* table, xcgpu_grid** out) {
   if (!c || !out || natoms <= 0 || !Z || !xyz || !table) return c ? c->fail(XCGPU_ERR_INVALID, "grid_build: bad arguments") : XCGPU_ERR_INVALID;
+  if (partition != XCGPU_PARTITION_BECKE && partition != XCGPU_PARTITION_SSF)
+    return c->fail(XCGPU_ERR_INVALID, "grid_build: unknown partition");
   if (acc < 0 || acc > 7) return c->fail(XCGPU_ERR_INVALID, "Invalid accuracy level chosen, must be between [1,7].");
   std::map<int, std::vector<double>> leb;
   if (!read_lebedev(table, leb)) return c->fail(XCGPU_ERR_IO, std::string("cannot read Lebedev table ") + table);
@@ -217,6 +277,10 @@ extern "C" xcgpu_status xcgpu_grid_build(xcgpu_ctx* c, int natoms, const int* Z,
       const double u = (chi - 1) / (chi + 1);
       adj[j + (size_t)natoms * i] = std::min(0.5, std::max(-0.5, u / (u * u - 1)));
     }
+  std::vector<double> min_dist(natoms, 999999999.9);
+  for (int k = 0; k < natoms; ++k)
+    for (int l = 0; l < natoms; ++l)
+      if (l != k) min_dist[k] = std::min(min_dist[k], dist[l + (size_t)natoms * k]);
   std::vector<int> sig_off(1, 0), sig_list;
   for (int k = 0; k < natoms; ++k) {
     for (int l = 0; l < natoms; ++l)
@@ -224,7 +288,7 @@ extern "C" xcgpu_status xcgpu_grid_build(xcgpu_ctx* c, int natoms, const int* Z,
     sig_off.push_back((int)sig_list.size());
   }
   const long nc = (long)wref.size();
-  DevBuf dA, dD, dAdj, dSo, dSl, dP, dO, dW, dWo;
+  DevBuf dA, dD, dAdj, dSo, dSl, dP, dO, dW, dWo, dDist, dMin;
   std::vector<double> A(xyz, xyz + 3 * natoms);
   auto up = [&](DevBuf& b, const void* src, size_t bytes) -> xcgpu_status {
     xcgpu_status st = b.alloc(c, bytes);
@@ -241,10 +305,19 @@ extern "C" xcgpu_status xcgpu_grid_build(xcgpu_ctx* c, int natoms, const int* Z,
   if (!st) st = up(dW, wref.data(), wref.size() * 8);
   if (!st) st = dWo.alloc(c, nc * 8);
   if (st) return st;
-  becke_kernel<<<(unsigned)((nc + 127) / 128), 128, 0, c->stream>>>(
-      natoms, dA.as<double>(), dD.as<double>(), dAdj.as<double>(), dSo.as<int>(), dSl.as<int>(), nc, dP.as<double>(),
-      dO.as<int>(), dW.as<double>(), smoothing, dWo.as<double>());
-  if ((st = c->check_launch("becke_kernel"))) return st;
+  if (partition == XCGPU_PARTITION_SSF) {
+    if (!st) st = up(dDist, dist.data(), dist.size() * 8);
+    if (!st) st = up(dMin, min_dist.data(), min_dist.size() * 8);
+    if (st) return st;
+    ssf_kernel<<<(unsigned)((nc + 127) / 128), 128, 0, c->stream>>>(natoms, dA.as<double>(), dDist.as<double>(),
+                                                                    dMin.as<double>(), nc, dP.as<double>(),
+                                                                    dO.as<int>(), dW.as<double>(), dWo.as<double>());
+  } else {
+    becke_kernel<<<(unsigned)((nc + 127) / 128), 128, 0, c->stream>>>(
+        natoms, dA.as<double>(), dD.as<double>(), dAdj.as<double>(), dSo.as<int>(), dSl.as<int>(), nc, dP.as<double>(),
+        dO.as<int>(), dW.as<double>(), smoothing, dWo.as<double>());
+  }
+  if ((st = c->check_launch("grid partition kernel"))) return st;
   std::vector<double> w(nc);
   if ((st = c->cuda(cudaMemcpyAsync(w.data(), dWo.p, nc * 8, cudaMemcpyDeviceToHost, c->stream), "grid weights")))
     return st;

@@ -197,6 +197,8 @@ struct xcgpu_plan {
   std::vector<int> chunk_bounds;
   long chunk_max_doubles = 0;
   xcgpu::DevBuf w_fskip, w_psplit, w_slab, w_P, w_V, w_rho, w_grad, w_epuv, w_dfdrho, w_dfdgrad, w_partials, w_sums, w_skip, w_aux;
+  // supersystem quantities of a non-additive build whose active subsystem is this plan
+  xcgpu::DevBuf n_rho, n_grad, n_epuv, n_dfdrho, n_dfdgrad, n_partials, n_fskip, n_sums;
 };
 
 namespace xcgpu {
@@ -224,6 +226,7 @@ xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0
                               const long* slab_off, const double* scratch, int nspin, const double* v,
                               const double* g, const unsigned char* skip, double* F);
 xcgpu_status launch_axpy(Ctx* c, long n, const double* x, double* y);  // y += x
+xcgpu_status launch_scale_add(Ctx* c, long n, double a, const double* x, double* y);  // y += a x
 xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out /*device*/);
 // mixed precision (tcgen05, 3xTF32): one persistent launch per stage over the blocks of
 // every build in `work`; density writes rho / grad rho (FP64), the adder accumulates

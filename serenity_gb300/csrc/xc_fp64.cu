@@ -556,6 +556,18 @@ xcgpu_status launch_axpy(Ctx* c, long n, const double* x, double* y) {
   return c->check_launch("axpy_kernel");
 }
 
+__global__ void scale_add_kernel(long n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a * x[i];
+}
+
+xcgpu_status launch_scale_add(Ctx* c, long n, double a, const double* x, double* y) {
+  if (n == 0) return XCGPU_OK;
+  KernelTimer kt(c, kOther);
+  scale_add_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, a, x, y);
+  return c->check_launch("scale_add_kernel");
+}
+
 xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out) {
   KernelTimer kt(c, kOther);
   sum_partials_kernel<<<1, 256, 0, c->stream>>>(partials, nparts, ncomp, out);

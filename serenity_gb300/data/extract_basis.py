@@ -18,11 +18,12 @@ import re
 import sys
 
 # element blocks needed by the workloads (water clusters), the H2 end-to-end
-# test system and the spherical-normalisation test (Sc up to l = 6)
+# test systems and the spherical-normalisation test (Sc up to l = 6)
 WANTED = {
     "DEF2-SVP": ["h", "c", "n", "o"],
     "DEF2-TZVP": ["h", "c", "n", "o"],
     "CC-PV5Z": ["sc"],
+    "6-31GS": ["h"],  # the embedding (FDE) H2 test systems
 }
 
 

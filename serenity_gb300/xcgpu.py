@@ -78,6 +78,8 @@ def library(build_if_needed=True):
     L.xcgpu_kernel_launches.restype = ctypes.c_uint64
     L.xcgpu_grid_create.argtypes = [vp, vp, vp, ctypes.c_uint64, ctypes.POINTER(vp)]
     L.xcgpu_grid_build.argtypes = [vp, S, vp, vp, S, S, S, ctypes.c_double, S, S, ctypes.c_char_p, ctypes.POINTER(vp)]
+    L.xcgpu_grid_build_partition.argtypes = [vp, S, vp, vp, S, S, S, ctypes.c_double, S, S, S, ctypes.c_char_p,
+                                             ctypes.POINTER(vp)]
     L.xcgpu_grid_npoints.argtypes = [vp]
     L.xcgpu_grid_npoints.restype = ctypes.c_uint64
     L.xcgpu_grid_copy.argtypes = [vp, vp, vp]
@@ -99,6 +101,8 @@ def library(build_if_needed=True):
     L.xcgpu_add_scalar.argtypes = [vp, ctypes.c_double, S, vp, vp, vp, S, S]
     L.xcgpu_vxc.argtypes = [vp, S, S, S, ctypes.c_double, vp, vp, dp, dp, S]
     L.xcgpu_vxc_batch.argtypes = [vp, ctypes.POINTER(Request), ctypes.c_uint32, S, S]
+    L.xcgpu_nadd_vxc.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_uint32, S, S, S, ctypes.c_double, vp,
+                                 ctypes.POINTER(vp), vp, dp, S]
     L.xcgpu_check_async.argtypes = [vp]
     L.xcgpu_graph_begin.argtypes = [vp]
     L.xcgpu_graph_end.argtypes = [vp, ctypes.POINTER(vp)]
@@ -106,11 +110,11 @@ def library(build_if_needed=True):
     L.xcgpu_graph_destroy.argtypes = [vp]
     L.xcgpu_set_timing.argtypes = [vp, S]
     L.xcgpu_get_timing.argtypes = [vp, vp, vp]
-    for name in ["xcgpu_vxc_batch", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
+    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
                  "xcgpu_graph_launch", "xcgpu_set_timing", "xcgpu_get_timing"]:
         getattr(L, name).restype = S
     for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
-                 "xcgpu_grid_copy", "xcgpu_basis_create", "xcgpu_basis_coefs", "xcgpu_plan_create",
+                 "xcgpu_grid_build_partition", "xcgpu_grid_copy", "xcgpu_basis_create", "xcgpu_basis_coefs", "xcgpu_plan_create",
                  "xcgpu_plan_get_stats", "xcgpu_block_on_grid", "xcgpu_density", "xcgpu_functional",
                  "xcgpu_add_scalar", "xcgpu_vxc"]:
         getattr(L, name).restype = S
@@ -222,6 +226,9 @@ class Context:
         return epuv, dr, dg
 
 
+PARTITION = {"becke": 0, "ssf": 1}
+
+
 class Grid:
     def __init__(self, ctx, xyz=None, w=None, handle=None):
         self.ctx = ctx
@@ -236,14 +243,15 @@ class Grid:
 
     @staticmethod
     def build(ctx, Z, xyz_bohr, n_rad=0, n_ang=0, accuracy=0, weight_threshold=1e-14, smoothing=3, sort=True,
-              lebedev_table=None):
+              lebedev_table=None, partition="becke"):
+        """Atom-centred grid; partition "becke" or "ssf" (the reference's GRIDTYPE)."""
         from .basis import LEBEDEV_TABLE
         Z = np.ascontiguousarray(Z, dtype=np.int32)
         xyz = np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1)
         h = vp()
-        ctx.check(ctx.L.xcgpu_grid_build(ctx.h, len(Z), _ptr(Z), _ptr(xyz), n_rad, n_ang, accuracy, weight_threshold,
-                                         smoothing, int(sort), (lebedev_table or LEBEDEV_TABLE).encode(),
-                                         ctypes.byref(h)))
+        ctx.check(ctx.L.xcgpu_grid_build_partition(ctx.h, len(Z), _ptr(Z), _ptr(xyz), n_rad, n_ang, accuracy,
+                                                   weight_threshold, PARTITION[partition], smoothing, int(sort),
+                                                   (lebedev_table or LEBEDEV_TABLE).encode(), ctypes.byref(h)))
         return Grid(ctx, handle=h)
 
     def points(self):
@@ -368,6 +376,27 @@ class Plan:
         self.ctx.check(self.ctx.L.xcgpu_vxc(self.h, fid, nspin, precision, block_ave_threshold, _ptr(Pc), _ptr(V),
                                             ctypes.byref(exc), ctypes.byref(nel), MEM_HOST))
         return V.transpose(0, 2, 1), exc.value, nel.value
+
+    def nadd_vxc(self, func, P, env, precision=PREC_FP64, block_ave_threshold=1e-11):
+        """Non-additive XC potential of this (active) subsystem in the field of the
+        environment subsystems env = [(plan, P_env), ...] on the same grid
+        (NAddFuncPotential<M>::getMatrix).  P host arrays [nbf,nbf] / [nspin,nbf,nbf].
+        Returns (V [nspin, nbf, nbf] of this plan's basis, E_nadd)."""
+        fid = FUNC[func] if isinstance(func, str) else int(func)
+        P = np.asarray(P, dtype=np.float64)
+        nspin = 1 if P.ndim == 2 else P.shape[0]
+
+        def colmajor(M, nbf):
+            return np.ascontiguousarray(np.stack([m.T for m in np.asarray(M, dtype=np.float64).reshape(nspin, nbf, nbf)]))
+        Pc = colmajor(P, self.nbf)
+        envc = [colmajor(Pe, pl.nbf) for pl, Pe in env]
+        plans = (vp * max(1, len(env)))(*[pl.h for pl, _ in env])
+        ptrs = (vp * max(1, len(env)))(*[e.ctypes.data for e in envc])
+        V = np.zeros((nspin, self.nbf, self.nbf))
+        e = ctypes.c_double()
+        self.ctx.check(self.ctx.L.xcgpu_nadd_vxc(self.h, plans, len(env), fid, nspin, precision, block_ave_threshold,
+                                                 _ptr(Pc), ptrs, _ptr(V), ctypes.byref(e), MEM_HOST))
+        return V.transpose(0, 2, 1), e.value
 
     def __del__(self):
         if getattr(self, "h", None) and self.ctx.h:

@@ -10,6 +10,12 @@
 
 using namespace Serenity;
 
+// every member of the class templates compiles against the C ABI
+template class Serenity::NAddFuncPotential<RESTRICTED>;
+template class Serenity::NAddFuncPotential<UNRESTRICTED>;
+template class Serenity::FuncPotential<RESTRICTED>;
+template class Serenity::FuncPotential<UNRESTRICTED>;
+
 static std::vector<ShellData> small_mixed() {
   return {{0, false, {0.0, 0.0, 0.0}, {1.0, 2.0}, {1.0, 0.1}},
           {1, false, {1.0, 0.0, 0.0}, {1.0, 2.0}, {1.0, 0.1}},

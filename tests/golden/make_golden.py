@@ -15,6 +15,11 @@ Sources (paths inside the reference project):
   Fock matrices, restricted and unrestricted (1e-6), with the density matrices
   read from ``data/testresources/TestSystem_H2_DEF2_TZVP/*.dmat.{res,unres}.h5``
   -> ``funcpot_h2.json``
+* ``src/potentials/NAddFuncPotential_test.cpp:58-120`` -- non-additive LDA
+  potential of an active H2 next to an environment H2 (6-31G*, SSF grid), restricted
+  and unrestricted (1e-5), with the density matrices read from
+  ``data/testresources/TestSystem_H2_6_31Gs_{ACTIVE,ENVIRONMENT}_FDE/*.dmat.*.h5``
+  -> ``nadd_h2.json``
 * ``src/data/grid/BasisFunctionOnGridController.cpp:455-1062`` -- the
   reference's real solid harmonics Y_lm, l = 0..6, evaluated at fixed points by
   reading its formulas as text -> ``solid_harmonics.json``
@@ -229,6 +234,60 @@ def funcpot_fixture():
     }
 
 
+def _expect_entries(body, name):
+    """EXPECT_NEAR(<name>(i, j), value, tol) lines of a test body -> [[i, j, value]], tol."""
+    out, tol = [], None
+    for m in re.finditer(r"EXPECT_NEAR\(%s\((\d+), (\d+)\), ([-+0-9.eE]+), ([-+0-9.eE]+)\)" % re.escape(name), body):
+        out.append([int(m.group(1)), int(m.group(2)), float(m.group(3))])
+        tol = float(m.group(4))
+    return out, tol
+
+
+def _plausible_density(a):
+    return bool(np.all(np.isfinite(a)) and np.abs(a).max() < 10 and np.allclose(a, a.T, rtol=0, atol=1e-14)
+                and np.all(np.diag(a) > 1e-4))
+
+
+def nadd_fixture():
+    """Non-additive XC potential of the FDE H2 pair (NAddFuncPotential_test.cpp:58-120):
+    active H2 in the field of an environment H2, LDA, 6-31G* (Cartesian), on the active
+    system's SSF grid (accuracy 4); density matrices from the systems' test resources."""
+    text = _src("src/potentials/NAddFuncPotential_test.cpp")
+    res_body = text[text.index("TEST_F(NAddFuncPotentialTest, H2Dimer_FockMatrix_LDA)"):]
+    res_body = res_body[:res_body.index("TEST_F", 10)]
+    unres_body = text[text.index("TEST_F(NAddFuncPotentialTest, H2Dimer_FockMatrix_LDA_UNRES)"):]
+    unres_body = unres_body[:unres_body.index("TEST_F", 10)]
+    F, tol = _expect_entries(res_body, "F")
+    Fa, _ = _expect_entries(unres_body, "F.alpha")
+    Fb, _ = _expect_entries(unres_body, "F.beta")
+    systems = {}
+    for role, name in [("active", "TestSystem_H2_6_31Gs_ACTIVE_FDE"), ("environment", "TestSystem_H2_6_31Gs_ENVIRONMENT_FDE")]:
+        base = os.path.join(REF, "data/testresources", name, name)
+        res = _symmetric_blocks(base + ".dmat.res.h5", 4)
+        raw = open(base + ".dmat.unres.h5", "rb").read()
+        # the unrestricted file holds alpha and beta back to back, 128 bytes apart, at the
+        # first offset where a symmetric 4x4 block with positive diagonal starts
+        ua = next(o for o in range(0, len(raw) - 255, 8)
+                  if _plausible_density(np.frombuffer(raw[o:o + 128], dtype="<f8").reshape(4, 4)))
+        Pa = np.frombuffer(raw[ua:ua + 128], dtype="<f8").reshape(4, 4)
+        Pb = np.frombuffer(raw[ua + 128:ua + 256], dtype="<f8").reshape(4, 4)
+        assert np.allclose(Pa, Pa.T) and np.allclose(Pb, Pb.T)
+        settings = open(base + ".settings").read()
+        grid = dict(re.findall(r"^(\w+) (\S+)$", settings[settings.index("+grid"):settings.index("-grid")], re.M))
+        xyz = [ln.split() for ln in open(base + ".xyz").read().strip().split("\n")[2:]]
+        res = [(o, a) for o, a in res if np.all(np.diag(a) > 1e-4)]
+        assert len(res) == 1, [o for o, _ in res]
+        systems[role] = {"atoms_angstrom": [[a[0], float(a[1]), float(a[2]), float(a[3])] for a in xyz],
+                         "grid_settings": grid, "P": res[0][1].tolist(), "P_offset": res[0][0],
+                         "Pa": Pa.tolist(), "Pb": Pb.tolist(), "Pab_offsets": [ua, ua + 128]}
+    return {
+        "source": "src/potentials/NAddFuncPotential_test.cpp:58-120; data/testresources/TestSystem_H2_6_31Gs_{ACTIVE,ENVIRONMENT}_FDE",
+        "tolerance": tol, "basis": "6-31GS", "spherical": False, "functional": "LDA",
+        "systems": systems,
+        "F": F, "Fa": Fa, "Fb": Fb,
+    }
+
+
 def solid_harmonics_fixture():
     """Evaluate the reference's Y[m] (value formulas only) for l = 0..6 at fixed points."""
     text = _src("src/data/grid/BasisFunctionOnGridController.cpp")
@@ -260,6 +319,7 @@ def main():
         "adder_very_small.json": adder_fixture(),
         "funcpot_h2.json": funcpot_fixture(),
         "solid_harmonics.json": solid_harmonics_fixture(),
+        "nadd_h2.json": nadd_fixture(),
     }
     for name, obj in fixtures.items():
         with open(os.path.join(OUT, name), "w") as f:

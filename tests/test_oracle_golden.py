@@ -66,3 +66,49 @@ def test_h2_lda_fock_matrix_end_to_end(golden, unrestricted):
     for s in range(V.shape[0]):
         np.testing.assert_allclose(V[s], F, rtol=0, atol=d["tolerance"])
     assert abs(nel - 2.0) < 1e-5
+
+
+def _nadd_pair(golden):
+    """Active and environment H2 of the reference's FDE test systems on the active
+    system's SSF grid."""
+    d = golden("nadd_h2.json")
+    out = {}
+    for role in ["active", "environment"]:
+        s = d["systems"][role]
+        sym = [a[0] for a in s["atoms_angstrom"]]
+        xyz = np.array([a[1:] for a in s["atoms_angstrom"]]) * ANGSTROM_TO_BOHR
+        out[role] = (sym, xyz, po.Basis(Shells.for_atoms(sym, xyz, d["basis"], spherical=d["spherical"])))
+    sym, xyz, _ = out["active"]
+    gs = d["systems"]["active"]["grid_settings"]
+    assert gs["GRIDTYPE"] == "SSF"
+    pts, w = po.becke_grid([atomic_number(s) for s in sym], xyz, accuracy=int(gs["ACCURACY"]),
+                           weight_threshold=float(gs["WEIGHTTHRESHOLD"]), smoothing=int(gs["SMOOTHING"]),
+                           partition="ssf")
+    return d, out, pts, w
+
+
+def test_nadd_lda_fock_matrix_matches_reference(golden):
+    """NAddFuncPotential_test.cpp:58-84 (restricted LDA, 1e-5): pins the SSF partition,
+    the 6-31G* basis and the non-additive composition."""
+    d, sysd, pts, w = _nadd_pair(golden)
+    A, E = d["systems"]["active"], d["systems"]["environment"]
+    V, _ = po.nadd_vxc(sysd["active"][2], [sysd["environment"][2]], pts, w, d["functional"], np.array(A["P"]),
+                       [np.array(E["P"])])
+    for i, j, v in d["F"]:
+        assert abs(V[0][i, j] - v) <= d["tolerance"], (i, j, V[0][i, j], v)
+
+
+def test_nadd_unrestricted_split_equals_restricted(golden):
+    """Unrestricted input with P_alpha = P_beta = P / 2 gives the restricted potential
+    in both spin channels and the same energy (the reference's unrestricted golden values
+    of NAddFuncPotential_test.cpp:87-120 need density matrices its test resources do not
+    pin, see the fixture)."""
+    d, sysd, pts, w = _nadd_pair(golden)
+    A, E = np.array(d["systems"]["active"]["P"]), np.array(d["systems"]["environment"]["P"])
+    for func in ["LDA", "PBE"]:
+        Vr, er = po.nadd_vxc(sysd["active"][2], [sysd["environment"][2]], pts, w, func, A, [E])
+        Vu, eu = po.nadd_vxc(sysd["active"][2], [sysd["environment"][2]], pts, w, func, np.stack([A / 2, A / 2]),
+                             [np.stack([E / 2, E / 2])])
+        np.testing.assert_allclose(Vu[0], Vr[0], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(Vu[1], Vr[0], rtol=0, atol=1e-12)
+        assert abs(eu - er) <= 1e-12
