@@ -214,6 +214,17 @@ xcgpu_status xcgpu_nadd_vxc(xcgpu_plan* active, xcgpu_plan* const* env, uint32_t
                             int precision, double block_ave_threshold, const double* P_active,
                             const double* const* P_env, double* V, double* E_nadd, int mem);
 
+/* Every subsystem's non-additive potential at once (a Jacobi freeze-and-thaw cycle, or
+ * the final energy evaluation of FreezeAndThawTask.cpp:151-411): with one set of
+ * subsystem densities on the supersystem grid, V[i] = adder_i(dF[rho_tot] - dF[rho_i])
+ * for every i, E_nadd = E_xc[rho_tot] - sum_i E_xc[rho_i] (the same for all i).  Equals
+ * n_sub calls of xcgpu_nadd_vxc, each with the others as environment, with each density
+ * formed once instead of n_sub times; the densities and the adders of all subsystems run
+ * as one batched launch each in mixed precision.  P[i], V[i] as in xcgpu_nadd_vxc. */
+xcgpu_status xcgpu_nadd_vxc_all(xcgpu_plan* const* plans, uint32_t n_sub, int func, int nspin, int precision,
+                                double block_ave_threshold, const double* const* P, double* const* V, double* E_nadd,
+                                int mem);
+
 /* ---- batched builds (many subsystems, e.g. a freeze-and-thaw step) -------------------
  * All requests run as one persistent launch per heavy stage (mixed precision) on the
  * context stream, without host synchronisation unless XCGPU_BATCH_SYNC is set; P, V and

@@ -1023,6 +1023,148 @@ xcgpu_status xcgpu_nadd_vxc(xcgpu_plan* A, xcgpu_plan* const* env, uint32_t n_en
   return XCGPU_OK;
 }
 
+xcgpu_status xcgpu_nadd_vxc_all(xcgpu_plan* const* plans, uint32_t n_sub, int func, int nspin, int precision,
+                                double thr, const double* const* P, double* const* V, double* E_nadd, int mem) {
+  if (!plans || n_sub == 0 || !plans[0]) return XCGPU_ERR_INVALID;
+  xcgpu_plan* A = plans[0];
+  Ctx* c = A->ctx;
+  if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "nadd_all: unknown functional");
+  if ((nspin != 1 && nspin != 2) || !P || !V) return c->fail(XCGPU_ERR_INVALID, "nadd_all: bad arguments");
+  if (precision != XCGPU_PREC_FP64 && precision != XCGPU_PREC_MIXED)
+    return c->fail(XCGPU_ERR_INVALID, "nadd_all: unknown precision");
+  for (uint32_t i = 0; i < n_sub; ++i) {
+    if (!plans[i] || !P[i] || !V[i]) return c->fail(XCGPU_ERR_INVALID, "nadd_all: null plan, density or output");
+    if (plans[i]->ctx != c) return c->fail(XCGPU_ERR_INVALID, "nadd_all: plan of another context");
+    if (plans[i]->grid != A->grid)
+      return c->fail(XCGPU_ERR_INVALID, "nadd_all: all subsystem densities must live on one (supersystem) grid");
+    for (uint32_t j = 0; j < i; ++j)
+      if (plans[j] == plans[i]) return c->fail(XCGPU_ERR_INVALID, "nadd_all: one plan per subsystem");
+  }
+  cudaSetDevice(c->device);
+  const bool gga = xc::is_gga(func), mixed = precision == XCGPU_PREC_MIXED;
+  const long n = A->grid->n;
+  for (uint32_t i = 0; i < n_sub; ++i) XC_TRY(ensure_work(plans[i], nspin, gga, mixed));
+  std::vector<const double*> Pd(n_sub);
+  std::vector<double*> Vd(n_sub);
+  for (uint32_t i = 0; i < n_sub; ++i) {
+    xcgpu_plan* q = plans[i];
+    const size_t cnt = (size_t)nspin * q->basis->nbf * q->basis->nbf;
+    if (mem == XCGPU_MEM_HOST) {
+      XC_TRY(upload(c, q->w_P, P[i], cnt));
+      XC_TRY(q->w_V.alloc(c, cnt * sizeof(double)));
+      Pd[i] = q->w_P.as<double>();
+      Vd[i] = q->w_V.as<double>();
+    } else {
+      Pd[i] = P[i];
+      Vd[i] = V[i];
+    }
+    XC_TRY(q->n_dfdrho.alloc(c, (size_t)nspin * n * sizeof(double)));
+    if (gga) XC_TRY(q->n_dfdgrad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+  }
+  int* counter = nullptr;
+  XC_TRY(c->aux(&counter));
+  int* err = counter + 2;
+  XC_TRY(c->cuda(cudaMemsetAsync(counter, 0, 4 * sizeof(int), c->stream), "memset aux"));
+  // 1. all subsystem densities (one batched launch in mixed precision)
+  std::vector<MixedWork> work;
+  for (uint32_t i = 0; i < n_sub; ++i) {
+    xcgpu_plan* q = plans[i];
+    double* grad = gga ? q->w_grad.as<double>() : nullptr;
+    if (mixed) {
+      XC_TRY(mixed_split(c, Pd[i], q->w_psplit.as<float>(), (long)nspin * q->basis->nbf * q->basis->nbf));
+      work.push_back(MixedWork{&q->basis->dev, &q->dev, nspin, q->w_psplit.as<float>(), q->w_rho.as<double>(), grad,
+                               q->n_dfdrho.as<double>(), gga ? q->n_dfdgrad.as<double>() : nullptr,
+                               q->w_skip.as<unsigned char>(), Vd[i]});
+    } else {
+      XC_TRY(stage_density(q, nspin, Pd[i], q->w_rho.as<double>(), grad));
+    }
+  }
+  if (mixed) XC_TRY(mixed_density_batch(c, work, counter, err));
+  // 2. supersystem density in the first plan's buffers
+  XC_TRY(A->n_rho.alloc(c, (size_t)nspin * n * sizeof(double)));
+  XC_TRY(A->n_epuv.alloc(c, (size_t)n * sizeof(double)));
+  if (gga) XC_TRY(A->n_grad.alloc(c, (size_t)nspin * 3 * n * sizeof(double)));
+  XC_TRY(A->n_partials.alloc(c, 2 * ((n + 127) / 128) * sizeof(double) + 16));
+  XC_TRY(A->n_fskip.alloc(c, (size_t)(n + kSkipBlock - 1) / kSkipBlock + 1));
+  XC_TRY(A->n_sums.alloc(c, 2 * (n_sub + 1) * sizeof(double)));
+  XC_TRY(c->cuda(cudaMemcpyAsync(A->n_rho.p, A->w_rho.p, (size_t)nspin * n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 c->stream), "supersystem density"));
+  if (gga)
+    XC_TRY(c->cuda(cudaMemcpyAsync(A->n_grad.p, A->w_grad.p, (size_t)nspin * 3 * n * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, c->stream), "supersystem gradient"));
+  for (uint32_t i = 1; i < n_sub; ++i) {
+    XC_TRY(launch_axpy(c, (long)nspin * n, plans[i]->w_rho.as<double>(), A->n_rho.as<double>()));
+    if (gga) XC_TRY(launch_axpy(c, (long)nspin * 3 * n, plans[i]->w_grad.as<double>(), A->n_grad.as<double>()));
+  }
+  // 3. functionals: the supersystem's into the first plan's difference buffers (it is
+  //    subtracted last), each subsystem's into its own work buffers
+  double* sums = A->n_sums.as<double>();
+  auto functional = [&](const double* rho, const double* grad, double* epuv, double* dfdrho, double* dfdgrad,
+                        double* partials, unsigned char* fskip, double* out) -> xcgpu_status {
+    int nparts = 0;
+    xcgpu_status st = launch_functional(c, func, nspin, n, kSkipBlock, rho, gga ? grad : nullptr, epuv, dfdrho,
+                                        gga ? dfdgrad : nullptr, A->dev.w, partials, &nparts, fskip);
+    if (st) return st;
+    if (nparts) return launch_sum_partials(c, partials, nparts, 2, out);
+    return c->cuda(cudaMemsetAsync(out, 0, 2 * sizeof(double), c->stream), "memset sums");
+  };
+  XC_TRY(functional(A->n_rho.as<double>(), A->n_grad.as<double>(), A->n_epuv.as<double>(), A->n_dfdrho.as<double>(),
+                    A->n_dfdgrad.as<double>(), A->n_partials.as<double>(), A->n_fskip.as<unsigned char>(), sums));
+  for (uint32_t i = 0; i < n_sub; ++i) {
+    xcgpu_plan* q = plans[i];
+    XC_TRY(functional(q->w_rho.as<double>(), q->w_grad.as<double>(), q->w_epuv.as<double>(), q->w_dfdrho.as<double>(),
+                      q->w_dfdgrad.as<double>(), q->w_partials.as<double>(), q->w_fskip.as<unsigned char>(),
+                      sums + 2 * (i + 1)));
+  }
+  // 4. per subsystem: dF[rho_tot] - dF[rho_i] (the first plan's buffers hold dF[rho_tot])
+  for (uint32_t k = 0; k < n_sub; ++k) {
+    const uint32_t i = (k + 1) % n_sub;  // the first subsystem last
+    xcgpu_plan* q = plans[i];
+    if (i != 0) {
+      XC_TRY(c->cuda(cudaMemcpyAsync(q->n_dfdrho.p, A->n_dfdrho.p, (size_t)nspin * n * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, c->stream), "copy potential"));
+      if (gga)
+        XC_TRY(c->cuda(cudaMemcpyAsync(q->n_dfdgrad.p, A->n_dfdgrad.p, (size_t)nspin * 3 * n * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, c->stream), "copy potential gradient"));
+    }
+    XC_TRY(launch_scale_add(c, (long)nspin * n, -1.0, q->w_dfdrho.as<double>(), q->n_dfdrho.as<double>()));
+    if (gga)
+      XC_TRY(launch_scale_add(c, (long)nspin * 3 * n, -1.0, q->w_dfdgrad.as<double>(), q->n_dfdgrad.as<double>()));
+  }
+  // 5. every subsystem's adder (one batched launch in mixed precision)
+  for (uint32_t i = 0; i < n_sub; ++i) {
+    xcgpu_plan* q = plans[i];
+    const int nbf = q->basis->nbf;
+    const double* gv = gga ? q->n_dfdgrad.as<double>() : nullptr;
+    XC_TRY(c->cuda(cudaMemsetAsync(Vd[i], 0, (size_t)nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
+    if (mixed)
+      XC_TRY(launch_block_skip_flags(c, q->dev, nspin, q->n_dfdrho.as<double>(), gv, thr,
+                                     q->w_skip.as<unsigned char>()));
+    else
+      XC_TRY(stage_adder(q, nspin, q->n_dfdrho.as<double>(), gv, thr, Vd[i]));
+  }
+  if (mixed) XC_TRY(mixed_adder_batch(c, work, counter + 1, err));
+  std::vector<double> hs(2 * (n_sub + 1));
+  int herr = 0;
+  XC_TRY(c->cuda(cudaMemcpyAsync(hs.data(), sums, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                 "sums"));
+  XC_TRY(c->cuda(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
+  if (mem == XCGPU_MEM_HOST)
+    for (uint32_t i = 0; i < n_sub; ++i) {
+      const int nbf = plans[i]->basis->nbf;
+      XC_TRY(c->cuda(cudaMemcpyAsync(V[i], Vd[i], (size_t)nspin * nbf * nbf * sizeof(double), cudaMemcpyDeviceToHost,
+                                     c->stream), "V"));
+    }
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "nadd_all"));
+  if (herr) return device_error(c, herr, "nadd_all");
+  if (E_nadd) {
+    double e = hs[0];  // E_xc[rho_tot] - sum_i E_xc[rho_i]
+    for (uint32_t i = 0; i < n_sub; ++i) e -= hs[2 * (i + 1)];
+    *E_nadd = e;
+  }
+  return XCGPU_OK;
+}
+
 xcgpu_status xcgpu_check_async(xcgpu_ctx* c) {
   if (!c) return XCGPU_ERR_INVALID;
   int herr = 0;

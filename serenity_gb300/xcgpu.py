@@ -103,6 +103,8 @@ def library(build_if_needed=True):
     L.xcgpu_vxc_batch.argtypes = [vp, ctypes.POINTER(Request), ctypes.c_uint32, S, S]
     L.xcgpu_nadd_vxc.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_uint32, S, S, S, ctypes.c_double, vp,
                                  ctypes.POINTER(vp), vp, dp, S]
+    L.xcgpu_nadd_vxc_all.argtypes = [ctypes.POINTER(vp), ctypes.c_uint32, S, S, S, ctypes.c_double,
+                                     ctypes.POINTER(vp), ctypes.POINTER(vp), dp, S]
     L.xcgpu_check_async.argtypes = [vp]
     L.xcgpu_graph_begin.argtypes = [vp]
     L.xcgpu_graph_end.argtypes = [vp, ctypes.POINTER(vp)]
@@ -110,7 +112,7 @@ def library(build_if_needed=True):
     L.xcgpu_graph_destroy.argtypes = [vp]
     L.xcgpu_set_timing.argtypes = [vp, S]
     L.xcgpu_get_timing.argtypes = [vp, vp, vp]
-    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
+    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_nadd_vxc_all", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
                  "xcgpu_graph_launch", "xcgpu_set_timing", "xcgpu_get_timing"]:
         getattr(L, name).restype = S
     for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
@@ -224,6 +226,31 @@ class Context:
         self.check(self.L.xcgpu_functional(self.h, fid, nspin, n, skip_block, _ptr(rho), _ptr(g), _ptr(epuv), _ptr(dr),
                                            _ptr(dg), MEM_HOST))
         return epuv, dr, dg
+
+
+def nadd_vxc_all(subsystems, func, precision=PREC_FP64, block_ave_threshold=1e-11):
+    """Every subsystem's non-additive XC potential from one set of densities on a shared
+    (supersystem) grid: subsystems = [(plan, P), ...] with host P [nbf,nbf] or
+    [nspin,nbf,nbf].  Returns ([V_i [nspin, nbf_i, nbf_i]], E_nadd)."""
+    if not subsystems:
+        raise ValueError("nadd_vxc_all: no subsystems")
+    ctx = subsystems[0][0].ctx
+    fid = FUNC[func] if isinstance(func, str) else int(func)
+    P0 = np.asarray(subsystems[0][1], dtype=np.float64)
+    nspin = 1 if P0.ndim == 2 else P0.shape[0]
+    Ps, Vs = [], []
+    for plan, P in subsystems:
+        M = np.asarray(P, dtype=np.float64).reshape(nspin, plan.nbf, plan.nbf)
+        Ps.append(np.ascontiguousarray(np.stack([m.T for m in M])))
+        Vs.append(np.zeros((nspin, plan.nbf, plan.nbf)))
+    k = len(subsystems)
+    plans = (vp * k)(*[pl.h for pl, _ in subsystems])
+    pp = (vp * k)(*[x.ctypes.data for x in Ps])
+    vv = (vp * k)(*[x.ctypes.data for x in Vs])
+    e = ctypes.c_double()
+    ctx.check(ctx.L.xcgpu_nadd_vxc_all(plans, k, fid, nspin, precision, block_ave_threshold, pp, vv, ctypes.byref(e),
+                                       MEM_HOST))
+    return [V.transpose(0, 2, 1) for V in Vs], e.value
 
 
 PARTITION = {"becke": 0, "ssf": 1}

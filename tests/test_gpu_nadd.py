@@ -136,3 +136,17 @@ def test_nadd_without_environment_is_zero_and_grid_mismatch_is_rejected(ctx):
     pB = xcgpu.Plan(ctx, other, xcgpu.Basis(ctx, subs[1][0].shells), 128, 1e-9)
     with pytest.raises(xcgpu.XcgpuError):
         pA.nadd_vxc("PBE", PA, [(pB, subs[1][2])])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_nadd_all_equals_one_call_per_subsystem(ctx, precision):
+    """xcgpu_nadd_vxc_all = one xcgpu_nadd_vxc per subsystem with the others as
+    environment (each density formed once instead of once per call)."""
+    from serenity_gb300 import xcgpu
+    grid, subs = _water_in_waters(ctx)
+    Vs, e = xcgpu.nadd_vxc_all([(p, P) for _, p, P in subs], "PBE", precision=precision)
+    for i, (_, p, P) in enumerate(subs):
+        others = [(q, Q) for j, (_, q, Q) in enumerate(subs) if j != i]
+        V1, e1 = p.nadd_vxc("PBE", P, others, precision=precision)
+        np.testing.assert_allclose(Vs[i], V1, rtol=0, atol=1e-12)
+        assert abs(e - e1) <= 1e-12
