@@ -199,6 +199,17 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* plan, double block_ave_threshold, int 
 xcgpu_status xcgpu_vxc(xcgpu_plan* plan, int func, int nspin, int precision, double block_ave_threshold,
                        const double* P, double* V, double* Exc, double* Nel, int mem);
 
+/* ---- XC part of the nuclear gradient ------------------------------------------------
+ * FuncPotential<M>::getGeomGradients (FuncPotential.cpp:113-241): for every pair of active
+ * functions of a block, the atom of nu collects -2 P_mu,nu sum_p w [v phi_mu d_k phi_nu +
+ * sum_j g_j (phi_mu d_j d_k phi_nu + d_j phi_mu d_k phi_nu)] (second basis derivatives for
+ * GGA), summed over spins; no grid-weight derivatives, as in the reference.  FP64.
+ * shell_atom[s] = atom index of shell s (BasisController::getAtomIndicesOfBasis); G is
+ * natoms x 3 column-major (the reference's Eigen::MatrixXd), overwritten; P and G in
+ * `mem` space. */
+xcgpu_status xcgpu_xc_gradient(xcgpu_plan* plan, int func, int nspin, const double* P, const int* shell_atom,
+                               int natoms, double* G, int mem);
+
 /* ---- non-additive XC potential of subsystem DFT (frozen-density embedding) -----------
  * NAddFuncPotential<M>::getMatrix / getEnergy (NAddFuncPotential.cpp:189-243, 297-318) with
  * the supersystem density of SupersystemDensityOnGridController.cpp:101-187: every

@@ -92,6 +92,12 @@ void orc_ahlrichs_radial(double alpha, int n, double* r, double* w);
 /* Real solid harmonic values at a point, m = -l..l (the reference's order). */
 void orc_solid_harmonics(int l, double x, double y, double z, double* out);
 
+/* XC part of the nuclear gradient (FuncPotential<M>::getGeomGradients,
+ * FuncPotential.cpp:113-241): shell_atom[s] = atom index of shell s; P column-major per
+ * spin (restricted: total); out natoms x 3 column-major.  No grid-weight derivatives. */
+int orc_xc_gradient(const void* basis, const int* shell_atom, int natoms, const double* xyz, const double* w,
+                    long npts, int max_block, double thr, int func, int nspin, const double* P, double* out);
+
 #ifdef __cplusplus
 }
 #endif

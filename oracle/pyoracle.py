@@ -202,3 +202,22 @@ def nadd_vxc(active, envs, xyz, w, func, P_active, P_envs, max_block=128, thr=1e
     eA, vA, gvA = functional(func, rA, gA, max_block)
     V = active.add_scalar(xyz, w, vT - vA, (gvT - gvA) if gga else None, max_block, thr, ave_thr)
     return V, float(w @ eT) - float(w @ eA) - e_env
+
+
+def xc_gradient(basis, shell_atom, natoms, xyz, w, func, P, max_block=128, thr=1e-9):
+    """XC part of the nuclear gradient (FuncPotential<M>::getGeomGradients): natoms x 3.
+    shell_atom[s] = atom index of shell s; P [nbf, nbf] (restricted total) or
+    [nspin, nbf, nbf]."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+    n = xyz.size // 3
+    P = np.asarray(P, dtype=np.float64)
+    nspin = 1 if P.ndim == 2 else P.shape[0]
+    Pc = np.ascontiguousarray(np.stack([m.T for m in P.reshape(nspin, basis.nbf, basis.nbf)]).reshape(-1))
+    out = np.zeros(3 * natoms)
+    L = lib()
+    L.orc_xc_gradient.argtypes = [ctypes.c_void_p, _ip, ctypes.c_int, _dp, _dp, ctypes.c_long, ctypes.c_int,
+                                  ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp]
+    L.orc_xc_gradient(basis.h, np.ascontiguousarray(shell_atom, dtype=np.int32), natoms, xyz,
+                      np.ascontiguousarray(w, dtype=np.float64), n, max_block, thr, FUNC[func] if isinstance(func, str)
+                      else int(func), nspin, Pc, out)
+    return out.reshape(3, natoms).T

@@ -254,6 +254,81 @@ static void functional(int func, int nspin, long npts, int maxb, const double* r
   }
 }
 
+// XC contribution to the nuclear gradient, FuncPotential<M>::getGeomGradients
+// (FuncPotential.cpp:113-241), loop for loop: per block and pair (mu, nu) of
+// non-negligible functions, the atom of nu collects
+//   -2 P_mu,nu sum_p w v phi_mu d_k phi_nu
+//   -2 P_mu,nu sum_p w sum_j g_j (phi_mu d_j d_k phi_nu + d_j phi_mu d_k phi_nu)   (GGA)
+// per spin (restricted: the total density and its potential).  No weight derivatives,
+// as in the reference.  out: natoms x 3, column-major (atom + natoms * k).
+static void xc_gradient(const Basis& B, const int* shell_atom, int natoms, const double* xyz, const double* w,
+                        long npts, int maxb, double thr, int func, int nspin, const double* P, double* out) {
+  const int nbf = B.nbf;
+  const bool gga = functional_is_gga(func);
+  std::vector<int> fatom(nbf);
+  for (size_t s = 0; s < B.shells.size(); ++s)
+    for (int f = 0; f < B.shells[s].nfunc; ++f) fatom[B.shells[s].first + f] = shell_atom[s];
+  std::vector<double> rho((size_t)nspin * npts), grad(gga ? (size_t)nspin * 3 * npts : 0);
+  density(B, xyz, npts, maxb, thr, nspin, P, rho.data(), gga ? grad.data() : nullptr);
+  std::vector<double> epuv(npts), v((size_t)nspin * npts), g(gga ? (size_t)nspin * 3 * npts : 0);
+  functional(func, nspin, npts, 128, rho.data(), gga ? grad.data() : nullptr, epuv.data(), v.data(),
+             gga ? g.data() : nullptr);
+  const long nblocks = (npts + maxb - 1) / maxb;
+  const int nthreads = omp_get_max_threads();
+  std::vector<std::vector<double>> Gt(nthreads, std::vector<double>((size_t)3 * natoms, 0.0));
+#pragma omp parallel
+  {
+    std::vector<double> val, gr, he;
+    std::vector<int> negl(nbf);
+    double* G = Gt[omp_get_thread_num()].data();
+#pragma omp for schedule(dynamic)
+    for (long b = 0; b < nblocks; ++b) {
+      const long first = b * maxb;
+      const int n = block_size(b, nblocks, npts, maxb);
+      val.assign((size_t)n * nbf, 0.0);
+      gr.assign((size_t)3 * n * nbf, 0.0);
+      he.assign(gga ? (size_t)6 * n * nbf : 0, 0.0);
+      block_on_grid(B, xyz + 3 * first, n, thr, gga ? 2 : 1, val.data(), gr.data(), gga ? he.data() : nullptr,
+                    negl.data());
+      auto phi = [&](int mu, int p) { return val[(size_t)mu * n + p]; };
+      auto d = [&](int k, int mu, int p) { return gr[(size_t)k * n * nbf + (size_t)mu * n + p]; };
+      // Hessian component of the pair (j, k): xx xy xz yy yz zz
+      static const int hc[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+      auto dd = [&](int j, int k, int mu, int p) { return he[(size_t)hc[j][k] * n * nbf + (size_t)mu * n + p]; };
+      for (int s = 0; s < nspin; ++s) {
+        const double* Ps = P + (size_t)s * nbf * nbf;
+        for (int mu = 0; mu < nbf; ++mu) {
+          if (negl[mu]) continue;
+          for (int nu = 0; nu < nbf; ++nu) {
+            if (negl[nu]) continue;
+            const double pref = 2.0 * Ps[(size_t)nu * nbf + mu];  // P(mu, nu), column-major
+            const int A = fatom[nu];
+            for (int k = 0; k < 3; ++k) {
+              double t = 0.0;
+              for (int p = 0; p < n; ++p) t += w[first + p] * v[s * npts + first + p] * phi(mu, p) * d(k, nu, p);
+              G[A + natoms * k] -= pref * t;
+            }
+            if (gga) {
+              for (int k = 0; k < 3; ++k) {
+                double t = 0.0;
+                for (int j = 0; j < 3; ++j)
+                  for (int p = 0; p < n; ++p)
+                    t += w[first + p] * g[((size_t)s * 3 + j) * npts + first + p] *
+                         (phi(mu, p) * dd(j, k, nu, p) + d(j, mu, p) * d(k, nu, p));
+                G[A + natoms * k] -= pref * t;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  for (int i = 0; i < 3 * natoms; ++i) {
+    out[i] = 0.0;
+    for (auto& t : Gt) out[i] += t[i];
+  }
+}
+
 }  // namespace orc
 
 extern "C" {
@@ -308,3 +383,11 @@ int orc_vxc(const void* basis, const double* xyz, const double* w, long npts, in
 }
 
 }  // extern "C"
+
+extern "C" int orc_xc_gradient(const void* basis, const int* shell_atom, int natoms, const double* xyz,
+                               const double* w, long npts, int max_block, double thr, int func, int nspin,
+                               const double* P, double* out) {
+  orc::xc_gradient(*static_cast<const orc::Basis*>(basis), shell_atom, natoms, xyz, w, npts, max_block, thr, func,
+                   nspin, P, out);
+  return 0;
+}

@@ -101,6 +101,12 @@ class Shells:
                                "coef": coefs})
         return Shells(shells)
 
+    def atom_indices(self, coords_bohr):
+        """Atom index of every shell: the atom at the shell's centre."""
+        xyz = np.asarray(coords_bohr, dtype=np.float64).reshape(-1, 3)
+        c = np.asarray(self.centers, dtype=np.float64).reshape(-1, 3)
+        return np.argmin(((c[:, None, :] - xyz[None, :, :]) ** 2).sum(-1), axis=1).astype(np.int32)
+
     def as_list(self):
         out, off = [], 0
         for i in range(self.nshell):

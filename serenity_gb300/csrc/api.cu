@@ -1023,6 +1023,75 @@ xcgpu_status xcgpu_nadd_vxc(xcgpu_plan* A, xcgpu_plan* const* env, uint32_t n_en
   return XCGPU_OK;
 }
 
+xcgpu_status xcgpu_xc_gradient(xcgpu_plan* P, int func, int nspin, const double* Pm, const int* shell_atom, int natoms,
+                               double* G, int mem) {
+  if (!P) return XCGPU_ERR_INVALID;
+  Ctx* c = P->ctx;
+  if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "xc_gradient: unknown functional");
+  if ((nspin != 1 && nspin != 2) || !Pm || !shell_atom || natoms <= 0 || !G)
+    return c->fail(XCGPU_ERR_INVALID, "xc_gradient: bad arguments");
+  const xcgpu_basis* B = P->basis;
+  std::vector<int> fatom(B->nbf);
+  for (int sh = 0; sh < B->nshell; ++sh) {
+    if (shell_atom[sh] < 0 || shell_atom[sh] >= natoms)
+      return c->fail(XCGPU_ERR_INVALID, "xc_gradient: shell atom index out of range");
+    const int nf = B->pure[sh] ? 2 * B->l[sh] + 1 : ncart(B->l[sh]);
+    for (int f = 0; f < nf; ++f) fatom[B->first[sh] + f] = shell_atom[sh];
+  }
+  cudaSetDevice(c->device);
+  const bool gga = xc::is_gga(func);
+  const long n = P->grid->n;
+  const int nbf = B->nbf;
+  XC_TRY(ensure_work(P, nspin, gga, false));
+  const double* Pd = Pm;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(upload(c, P->w_P, Pm, (size_t)nspin * nbf * nbf));
+    Pd = P->w_P.as<double>();
+  }
+  // rho, grad rho and the potential of the functional (FuncPotential.cpp:115-116)
+  double* grad = gga ? P->w_grad.as<double>() : nullptr;
+  XC_TRY(stage_density(P, nspin, Pd, P->w_rho.as<double>(), grad));
+  int nparts = 0;
+  XC_TRY(launch_functional(c, func, nspin, n, kSkipBlock, P->w_rho.as<double>(), grad, P->w_epuv.as<double>(),
+                           P->w_dfdrho.as<double>(), gga ? P->w_dfdgrad.as<double>() : nullptr, P->dev.w,
+                           P->w_partials.as<double>(), &nparts, P->w_fskip.as<unsigned char>()));
+  // chunks of blocks whose slabs (4 planes, 10 with Hessians) fit the scratch cap
+  const int planes = gga ? 10 : 4;
+  const long cap = std::max<long>((long)(c->scratch_cap / sizeof(double)),
+                                  (long)planes * kBlockPoints * std::max(P->max_active, 1));
+  std::vector<long> off(P->nblocks);
+  std::vector<int> bounds(1, 0);
+  long cur = 0, mx = 0;
+  for (int b = 0; b < P->nblocks; ++b) {
+    const long need = (long)planes * kBlockPoints * (P->fn_off[b + 1] - P->fn_off[b]);
+    if (cur + need > cap && cur > 0) {
+      bounds.push_back(b);
+      mx = std::max(mx, cur);
+      cur = 0;
+    }
+    off[b] = cur;
+    cur += need;
+  }
+  mx = std::max(mx, cur);
+  bounds.push_back(P->nblocks);
+  DevBuf d_off, d_fatom, d_G;
+  XC_TRY(upload(c, d_off, off.data(), off.size()));
+  XC_TRY(upload(c, d_fatom, fatom.data(), fatom.size()));
+  XC_TRY(d_G.alloc(c, (size_t)3 * natoms * sizeof(double)));
+  XC_TRY(c->cuda(cudaMemsetAsync(d_G.p, 0, (size_t)3 * natoms * sizeof(double), c->stream), "memset G"));
+  XC_TRY(c->scratch2.alloc(c, std::max<long>(mx, 1) * sizeof(double)));
+  for (size_t k = 0; k + 1 < bounds.size(); ++k) {
+    const int b0 = bounds[k], b1 = bounds[k + 1];
+    XC_TRY(fp64_xc_gradient_chunk(c, B->dev, P->dev, b0, b1, d_off.as<long>() + b0, c->scratch2.as<double>(), gga,
+                                  nspin, Pd, P->w_dfdrho.as<double>(), gga ? P->w_dfdgrad.as<double>() : nullptr,
+                                  d_fatom.as<int>(), natoms, d_G.as<double>()));
+  }
+  XC_TRY(c->cuda(cudaMemcpyAsync(G, d_G.p, (size_t)3 * natoms * sizeof(double),
+                                 mem == XCGPU_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, c->stream),
+                 "G"));
+  return c->cuda(cudaStreamSynchronize(c->stream), "xc_gradient");
+}
+
 xcgpu_status xcgpu_nadd_vxc_all(xcgpu_plan* const* plans, uint32_t n_sub, int func, int nspin, int precision,
                                 double thr, const double* const* P, double* const* V, double* E_nadd, int mem) {
   if (!plans || n_sub == 0 || !plans[0]) return XCGPU_ERR_INVALID;

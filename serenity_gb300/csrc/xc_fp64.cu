@@ -251,6 +251,151 @@ xcgpu_status fp64_density_chunk(Ctx* c, const DevPlan& P, int b0, int b1, const 
 }
 
 // ------------------------------------------------------------------------------------
+// XC contribution to the nuclear gradient (FuncPotential<M>::getGeomGradients,
+// FuncPotential.cpp:113-241).  The reference's pair loop
+//   G[atom(nu)][k] -= 2 P_mu,nu sum_p w [ v phi_mu d_k phi_nu
+//                       + sum_j g_j (phi_mu d_j d_k phi_nu + d_j phi_mu d_k phi_nu) ]
+// is regrouped around two contractions with the block's density matrix,
+//   X_p,nu = sum_mu phi_mu(p) P_mu,nu,   Y_p,nu = sum_mu (w g . grad phi_mu)(p) P_mu,nu,
+// so that  G[atom(nu)][k] -= 2 sum_p [ X (w v d_k phi_nu + w g_j d_j d_k phi_nu) + Y d_k phi_nu ].
+// Slabs hold [value, x, y, z (, xx, xy, xz, yy, yz, zz)][function][128 points].
+
+// Values, gradients and Hessians of the active functions of blocks [b0, b1) (10 planes).
+__global__ void __launch_bounds__(128) fp64_eval_hess_kernel(DevBasis B, DevPlan P, int b0,
+                                                             const long* __restrict__ slab_off,
+                                                             double* __restrict__ scratch) {
+  const int b = b0 + blockIdx.x;
+  const long first = (long)b * P.max_block;
+  const int n = (int)min((long)P.max_block, P.npoints - first);
+  const int nact = P.fn_off[b + 1] - P.fn_off[b];
+  double* slab = scratch + slab_off[blockIdx.x];
+  const int p = threadIdx.x;
+  if (p < n) {
+    const double* q = P.xyz + 3 * (first + p);
+    eval_point<double, 2>(B, P, b, q[0], q[1], q[2], [&](int f, double v, double gx, double gy, double gz, const double* h) {
+      slab[(long)f * kBlockPoints + p] = v;
+      slab[(long)(nact + f) * kBlockPoints + p] = gx;
+      slab[(long)(2 * nact + f) * kBlockPoints + p] = gy;
+      slab[(long)(3 * nact + f) * kBlockPoints + p] = gz;
+      for (int c = 0; c < 6; ++c) slab[(long)((4 + c) * nact + f) * kBlockPoints + p] = h[c];
+    });
+  } else {
+    for (int f = 0; f < 10 * nact; ++f) slab[(long)f * kBlockPoints + p] = 0.0;
+  }
+}
+
+template <bool GGA>
+__global__ void __launch_bounds__(128) fp64_xc_gradient_kernel(DevPlan P, int b0, const long* __restrict__ slab_off,
+                                                               const double* __restrict__ scratch, int nspin,
+                                                               const double* __restrict__ Pm,
+                                                               const double* __restrict__ v,
+                                                               const double* __restrict__ g,
+                                                               const int* __restrict__ fatom, int natoms,
+                                                               double* __restrict__ G) {
+  const int b = b0 + blockIdx.x;
+  const long first = (long)b * P.max_block;
+  const int n = (int)min((long)P.max_block, P.npoints - first);
+  const int nact = P.fn_off[b + 1] - P.fn_off[b];
+  const int* fn = P.fn_list + P.fn_off[b];
+  const double* slab = scratch + slab_off[blockIdx.x];
+  const int p = threadIdx.x, lane = p & 31, warp = p >> 5;
+  const int nbf = P.nbf;
+  const bool live = p < n;
+  __shared__ double Ps[kDMu][kDNu];
+  __shared__ double red[4][kDNu][3];
+  // Hessian plane of the pair (j, k): xx xy xz yy yz zz
+  constexpr int hc[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  const double w = live ? P.w[first + p] : 0.0;
+  for (int s = 0; s < nspin; ++s) {
+    const double* Pmat = Pm + (long)s * nbf * nbf;
+    const double wv = live ? w * v[(long)s * P.npoints + first + p] : 0.0;
+    double wg[3] = {0.0, 0.0, 0.0};
+    if (GGA && live)
+      for (int j = 0; j < 3; ++j) wg[j] = w * g[((long)s * 3 + j) * P.npoints + first + p];
+    for (int nu0 = 0; nu0 < nact; nu0 += kDNu) {
+      double ax[kDNu], ay[kDNu];
+#pragma unroll
+      for (int j = 0; j < kDNu; ++j) ax[j] = ay[j] = 0.0;
+      for (int mu0 = 0; mu0 < nact; mu0 += kDMu) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kDMu * kDNu; e += blockDim.x) {
+          const int i = e / kDNu, j = e % kDNu;
+          const int mu = mu0 + i, nu = nu0 + j;
+          Ps[i][j] = (mu < nact && nu < nact) ? Pmat[(long)fn[nu] * nbf + fn[mu]] : 0.0;
+        }
+        __syncthreads();
+        const int mlim = min(kDMu, nact - mu0);
+        for (int i = 0; i < mlim; ++i) {
+          const int mu = mu0 + i;
+          const double ph = slab[(long)mu * kBlockPoints + p];
+          double psi = 0.0;
+          if (GGA)
+            psi = wg[0] * slab[(long)(nact + mu) * kBlockPoints + p] + wg[1] * slab[(long)(2 * nact + mu) * kBlockPoints + p] +
+                  wg[2] * slab[(long)(3 * nact + mu) * kBlockPoints + p];
+#pragma unroll
+          for (int j = 0; j < kDNu; ++j) {
+            ax[j] = fma(ph, Ps[i][j], ax[j]);
+            if (GGA) ay[j] = fma(psi, Ps[i][j], ay[j]);
+          }
+        }
+      }
+      // per-function contributions of this point, summed over the warp's 32 points
+#pragma unroll
+      for (int j = 0; j < kDNu; ++j) {
+        const int nu = nu0 + j;
+        double c[3] = {0.0, 0.0, 0.0};
+        if (nu < nact && live) {
+          double d[3];
+          for (int k = 0; k < 3; ++k) d[k] = slab[(long)((1 + k) * nact + nu) * kBlockPoints + p];
+          for (int k = 0; k < 3; ++k) c[k] = ax[j] * wv * d[k];
+          if (GGA) {
+            for (int k = 0; k < 3; ++k) {
+              double t = 0.0;
+              for (int jj = 0; jj < 3; ++jj) t += wg[jj] * slab[(long)((4 + hc[jj][k]) * nact + nu) * kBlockPoints + p];
+              c[k] += ax[j] * t + ay[j] * d[k];
+            }
+          }
+        }
+        for (int k = 0; k < 3; ++k) {
+          double x = c[k];
+          for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+          if (lane == 0) red[warp][j][k] = x;
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x < 3 * kDNu) {
+        const int j = threadIdx.x / 3, k = threadIdx.x % 3, nu = nu0 + j;
+        if (nu < nact) {
+          const double t = red[0][j][k] + red[1][j][k] + red[2][j][k] + red[3][j][k];
+          atomicAdd(&G[fatom[fn[nu]] + (long)natoms * k], -2.0 * t);
+        }
+      }
+    }
+  }
+}
+
+xcgpu_status fp64_xc_gradient_chunk(Ctx* c, const DevBasis& B, const DevPlan& P, int b0, int b1, const long* slab_off,
+                                    double* scratch, bool gga, int nspin, const double* Pm, const double* v,
+                                    const double* g, const int* fatom, int natoms, double* G) {
+  if (b1 <= b0) return XCGPU_OK;
+  xcgpu_status st;
+  {
+    KernelTimer kt(c, kEval);
+    if (gga) fp64_eval_hess_kernel<<<b1 - b0, kBlockPoints, 0, c->stream>>>(B, P, b0, slab_off, scratch);
+    else fp64_eval_kernel<<<b1 - b0, kBlockPoints, 0, c->stream>>>(B, P, b0, slab_off, scratch);
+    if ((st = c->check_launch("gradient basis kernel"))) return st;
+  }
+  KernelTimer kt(c, kOther);
+  if (gga)
+    fp64_xc_gradient_kernel<true><<<b1 - b0, kBlockPoints, 0, c->stream>>>(P, b0, slab_off, scratch, nspin, Pm, v, g,
+                                                                             fatom, natoms, G);
+  else
+    fp64_xc_gradient_kernel<false><<<b1 - b0, kBlockPoints, 0, c->stream>>>(P, b0, slab_off, scratch, nspin, Pm, v, g,
+                                                                              fatom, natoms, G);
+  return c->check_launch("fp64_xc_gradient_kernel");
+}
+
+// ------------------------------------------------------------------------------------
 // Functional on points.  Block skip (XCFun.cpp:136-140): a block of skip_block points
 // whose sum |rho_s| < n * 1e-12 for every spin gives zero outputs.
 __global__ void __launch_bounds__(128) skip_flags_kernel(long n, int skip_block, int nspin,

@@ -103,6 +103,7 @@ def library(build_if_needed=True):
     L.xcgpu_vxc_batch.argtypes = [vp, ctypes.POINTER(Request), ctypes.c_uint32, S, S]
     L.xcgpu_nadd_vxc.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_uint32, S, S, S, ctypes.c_double, vp,
                                  ctypes.POINTER(vp), vp, dp, S]
+    L.xcgpu_xc_gradient.argtypes = [vp, S, S, vp, vp, S, vp, S]
     L.xcgpu_nadd_vxc_all.argtypes = [ctypes.POINTER(vp), ctypes.c_uint32, S, S, S, ctypes.c_double,
                                      ctypes.POINTER(vp), ctypes.POINTER(vp), dp, S]
     L.xcgpu_check_async.argtypes = [vp]
@@ -112,7 +113,7 @@ def library(build_if_needed=True):
     L.xcgpu_graph_destroy.argtypes = [vp]
     L.xcgpu_set_timing.argtypes = [vp, S]
     L.xcgpu_get_timing.argtypes = [vp, vp, vp]
-    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_nadd_vxc_all", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
+    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_nadd_vxc_all", "xcgpu_xc_gradient", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
                  "xcgpu_graph_launch", "xcgpu_set_timing", "xcgpu_get_timing"]:
         getattr(L, name).restype = S
     for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
@@ -403,6 +404,18 @@ class Plan:
         self.ctx.check(self.ctx.L.xcgpu_vxc(self.h, fid, nspin, precision, block_ave_threshold, _ptr(Pc), _ptr(V),
                                             ctypes.byref(exc), ctypes.byref(nel), MEM_HOST))
         return V.transpose(0, 2, 1), exc.value, nel.value
+
+    def xc_gradient(self, func, P, shell_atom, natoms):
+        """XC part of the nuclear gradient (FuncPotential<M>::getGeomGradients), FP64:
+        natoms x 3.  shell_atom[s] = atom of shell s; P host [nbf,nbf] or [nspin,nbf,nbf]."""
+        fid = FUNC[func] if isinstance(func, str) else int(func)
+        P = np.asarray(P, dtype=np.float64)
+        nspin = 1 if P.ndim == 2 else P.shape[0]
+        Pc = np.ascontiguousarray(np.stack([m.T for m in P.reshape(nspin, self.nbf, self.nbf)]))
+        sa = np.ascontiguousarray(shell_atom, dtype=np.int32)
+        G = np.zeros(3 * natoms)
+        self.ctx.check(self.ctx.L.xcgpu_xc_gradient(self.h, fid, nspin, _ptr(Pc), _ptr(sa), natoms, _ptr(G), MEM_HOST))
+        return G.reshape(3, natoms).T
 
     def nadd_vxc(self, func, P, env, precision=PREC_FP64, block_ave_threshold=1e-11):
         """Non-additive XC potential of this (active) subsystem in the field of the

@@ -112,3 +112,26 @@ def test_nadd_unrestricted_split_equals_restricted(golden):
         np.testing.assert_allclose(Vu[0], Vr[0], rtol=0, atol=1e-12)
         np.testing.assert_allclose(Vu[1], Vr[0], rtol=0, atol=1e-12)
         assert abs(eu - er) <= 1e-12
+
+
+@pytest.mark.parametrize("func,unrestricted", [("LDA", False), ("PBE", False), ("BLYP", True)])
+def test_xc_gradient_is_the_fixed_grid_derivative(func, unrestricted):
+    """FuncPotential::getGeomGradients (no grid-weight derivatives) is the exact derivative
+    of E_xc on a fixed grid with P fixed and the basis moving with the atom: central
+    finite differences agree to O(h^2) (the reference's gradient golden vectors,
+    FuncPotential_test.cpp:234-330, need SCF densities its test resources do not hold)."""
+    from serenity_gb300 import workload as wl
+    sym, xyz = wl.water_cluster(1, 2, jitter=0.1)
+    w = wl.Workload(sym, xyz, "DEF2-SVP", func, (5, 4) if unrestricted else 5, 30, 110, 3)
+    P = w.density()
+    pts, wts = po.becke_grid(w.Z, xyz, n_rad=30, n_ang=110)
+    sa = w.shells.atom_indices(xyz)
+    G = po.xc_gradient(po.Basis(w.shells), sa, 3, pts, wts, func, P, thr=0.0)
+    h = 1e-4
+    for atom, k in [(0, 0), (1, 2), (2, 1)]:
+        def E(dx):
+            x2 = xyz.copy()
+            x2[atom, k] += dx
+            return po.Basis(Shells.for_atoms(sym, x2, "DEF2-SVP")).vxc(pts, wts, func, P, thr=0.0, ave_thr=0.0)[1]
+        fd = (E(h) - E(-h)) / (2 * h)
+        assert abs(G[atom, k] - fd) <= 2e-8, (atom, k, G[atom, k], fd)
