@@ -199,6 +199,18 @@ xcgpu_status xcgpu_add_scalar(xcgpu_plan* plan, double block_ave_threshold, int 
 xcgpu_status xcgpu_vxc(xcgpu_plan* plan, int func, int nspin, int precision, double block_ave_threshold,
                        const double* P, double* V, double* Exc, double* Nel, int mem);
 
+/* ---- linear-response XC kernel (TDDFT / TDA sigma vectors) --------------------------
+ * KernelSigmavector<RESTRICTED>::calcF (KernelSigmavector.cpp:128-392), singlet: for each
+ * trial matrix D[t] (column-major n_bf x n_bf), the density of (D + D^T)/2 and its
+ * gradient are contracted with the second functional derivatives at the ground-state
+ * density of P0 (total), v1 = F_nn rho1 + F_n,sigma sigma1, g1 = 2 (F_sigma,n rho1 +
+ * F_sigma,sigma sigma1) grad n + 2 F_sigma grad rho1, and integrated like a potential:
+ * F[t] = phi^T w (v1/2 phi + g1 . grad phi) + transpose, overwritten.  The reference's
+ * per-element screening of D and of the integration (at 1e-11) is replaced by the
+ * adder's block skip.  All matrices in `mem` space. */
+xcgpu_status xcgpu_lr_kernel(xcgpu_plan* plan, int func, const double* P0, uint32_t ntrial, const double* const* D,
+                             double* const* F, int precision, double block_ave_threshold, int mem);
+
 /* ---- XC part of the nuclear gradient ------------------------------------------------
  * FuncPotential<M>::getGeomGradients (FuncPotential.cpp:113-241): for every pair of active
  * functions of a block, the atom of nu collects -2 P_mu,nu sum_p w [v phi_mu d_k phi_nu +

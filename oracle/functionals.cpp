@@ -100,6 +100,105 @@ template <int N> D<N> xasinhx_of_sq(const D<N>& u) {
 }
 template <int N> double val(const D<N>& a) { return a.v; }
 
+// Second-order forward-mode numbers (value, gradient, Hessian over N variables), for
+// the second functional derivatives of the linear-response kernel.
+template <int N>
+struct H {
+  double v;
+  double d[N];
+  double h[N][N];
+  H(double x = 0.0) : v(x) {
+    for (int i = 0; i < N; ++i) {
+      d[i] = 0.0;
+      for (int j = 0; j < N; ++j) h[i][j] = 0.0;
+    }
+  }
+  static H var(double x, int i) {
+    H r(x);
+    r.d[i] = 1.0;
+    return r;
+  }
+};
+template <int N>
+H<N> chain2(const H<N>& a, double f, double df, double ddf) {
+  H<N> r(f);
+  for (int i = 0; i < N; ++i) {
+    r.d[i] = df * a.d[i];
+    for (int j = 0; j < N; ++j) r.h[i][j] = df * a.h[i][j] + ddf * a.d[i] * a.d[j];
+  }
+  return r;
+}
+template <int N>
+H<N> operator+(const H<N>& a, const H<N>& b) {
+  H<N> r(a.v + b.v);
+  for (int i = 0; i < N; ++i) {
+    r.d[i] = a.d[i] + b.d[i];
+    for (int j = 0; j < N; ++j) r.h[i][j] = a.h[i][j] + b.h[i][j];
+  }
+  return r;
+}
+template <int N> H<N> operator-(const H<N>& a) { return chain2(a, -a.v, -1.0, 0.0); }
+template <int N> H<N> operator-(const H<N>& a, const H<N>& b) { return a + (-b); }
+template <int N>
+H<N> operator*(const H<N>& a, const H<N>& b) {
+  H<N> r(a.v * b.v);
+  for (int i = 0; i < N; ++i) {
+    r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    for (int j = 0; j < N; ++j)
+      r.h[i][j] = a.h[i][j] * b.v + a.d[i] * b.d[j] + a.d[j] * b.d[i] + a.v * b.h[i][j];
+  }
+  return r;
+}
+template <int N> H<N> inv(const H<N>& b) {
+  const double q = 1.0 / b.v;
+  return chain2(b, q, -q * q, 2.0 * q * q * q);
+}
+template <int N> H<N> operator/(const H<N>& a, const H<N>& b) { return a * inv(b); }
+template <int N> H<N> operator+(const H<N>& a, double b) { return a + H<N>(b); }
+template <int N> H<N> operator+(double a, const H<N>& b) { return H<N>(a) + b; }
+template <int N> H<N> operator-(const H<N>& a, double b) { return a - H<N>(b); }
+template <int N> H<N> operator-(double a, const H<N>& b) { return H<N>(a) - b; }
+template <int N> H<N> operator*(const H<N>& a, double b) { return chain2(a, a.v * b, b, 0.0); }
+template <int N> H<N> operator*(double a, const H<N>& b) { return chain2(b, a * b.v, a, 0.0); }
+template <int N> H<N> operator/(const H<N>& a, double b) { return chain2(a, a.v / b, 1.0 / b, 0.0); }
+template <int N> H<N> operator/(double a, const H<N>& b) { return a * inv(b); }
+template <int N> H<N> sqrt(const H<N>& a) {
+  const double s = std::sqrt(a.v);
+  return chain2(a, s, 0.5 / s, -0.25 / (s * s * s));
+}
+template <int N> H<N> cbrt(const H<N>& a) {
+  const double s = std::cbrt(a.v);
+  return chain2(a, s, s / (3.0 * a.v), -2.0 * s / (9.0 * a.v * a.v));
+}
+template <int N> H<N> pow(const H<N>& a, double p) {
+  return chain2(a, std::pow(a.v, p), p * std::pow(a.v, p - 1.0), p * (p - 1.0) * std::pow(a.v, p - 2.0));
+}
+template <int N> H<N> exp(const H<N>& a) {
+  const double e = std::exp(a.v);
+  return chain2(a, e, e, e);
+}
+template <int N> H<N> log(const H<N>& a) { return chain2(a, std::log(a.v), 1.0 / a.v, -1.0 / (a.v * a.v)); }
+template <int N> H<N> atan(const H<N>& a) {
+  const double q = 1.0 / (1.0 + a.v * a.v);
+  return chain2(a, std::atan(a.v), q, -2.0 * a.v * q * q);
+}
+// x asinh(x) of u = x^2: f'(u) = (asinh x / x + 1/sqrt(1+u)) / 2,
+// f''(u) = (1 / (2u sqrt(1+u)) - asinh x / (2 u x) - (1+u)^(-3/2) / 2) / 2; series below 1e-4
+template <int N> H<N> xasinhx_of_sq(const H<N>& u) {
+  const double x = std::sqrt(u.v);
+  const double f = x * std::asinh(x);
+  double df, ddf;
+  if (u.v < 1e-4) {
+    df = 1.0 - u.v / 3.0 + 9.0 * u.v * u.v / 40.0;
+    ddf = -1.0 / 3.0 + 9.0 * u.v / 20.0;
+  } else {
+    const double sq = std::sqrt(1.0 + u.v);
+    df = 0.5 * (std::asinh(x) / x + 1.0 / sq);
+    ddf = 0.5 * (1.0 / (2.0 * u.v * sq) - std::asinh(x) / (2.0 * u.v * x) - 0.5 / (sq * sq * sq));
+  }
+  return chain2(u, f, df, ddf);
+}
+
 static const double kDensTiny = 1e-14;
 static const double kZetaMax = 1.0 - 1e-12;
 
@@ -261,6 +360,32 @@ bool functional_is_gga(int func) {
       return true;
   }
   return false;
+}
+
+// Restricted linear-response kernel contracted with a perturbed density (the pp, pg, gg
+// kernel products of KernelSigmavector.cpp:363-392 with p = rho1, g = grad rho1, weights
+// left to the adder): with F(n, sigma) and sigma1 = 2 grad n . grad rho1,
+//   v1 = F_nn rho1 + F_n,sigma sigma1,
+//   g1 = 2 (F_sigma,n rho1 + F_sigma,sigma sigma1) grad n + 2 F_sigma grad rho1.
+void lr_kernel_point(int func, double n0, const double* g0, double n1, const double* g1, double* v1, double* gg1) {
+  const bool gga = functional_is_gga(func);
+  *v1 = 0.0;
+  if (gga)
+    for (int k = 0; k < 3; ++k) gg1[k] = 0.0;
+  if (!(n0 >= kDensTiny)) return;
+  double sig0 = 0.0, sig1 = 0.0;
+  if (gga)
+    for (int k = 0; k < 3; ++k) {
+      sig0 += g0[k] * g0[k];
+      sig1 += 2.0 * g0[k] * g1[k];
+    }
+  typedef H<2> T;
+  T n = T::var(n0, 0), s = T::var(sig0, 1);
+  T half = 0.5 * n, q = 0.25 * s;
+  T e = energy(func, half, half, q, q, q);
+  *v1 = e.h[0][0] * n1 + e.h[0][1] * sig1;
+  if (gga)
+    for (int k = 0; k < 3; ++k) gg1[k] = 2.0 * (e.h[1][0] * n1 + e.h[1][1] * sig1) * g0[k] + 2.0 * e.d[1] * g1[k];
 }
 
 void functional_point(int func, int nspin, const double* in, double* out) {

@@ -98,6 +98,14 @@ void orc_solid_harmonics(int l, double x, double y, double z, double* out);
 int orc_xc_gradient(const void* basis, const int* shell_atom, int natoms, const double* xyz, const double* w,
                     long npts, int max_block, double thr, int func, int nspin, const double* P, double* out);
 
+/* Restricted (singlet) linear-response XC kernel contracted with a perturbed density:
+ * v1 = F_nn rho1 + F_n,sigma sigma1, g1 = 2 (F_sigma,n rho1 + F_sigma,sigma sigma1) grad n +
+ * 2 F_sigma grad rho1 (sigma1 = 2 grad n . grad rho1), second derivatives by second-order
+ * forward-mode differentiation of the energy expressions; block skip of 128 points on
+ * rho0 as the functional data.  grad arrays [3][npts] (GGA). */
+int orc_lr_kernel(int func, long npts, const double* rho0, const double* grad0, const double* rho1,
+                  const double* grad1, double* v1, double* g1);
+
 #ifdef __cplusplus
 }
 #endif

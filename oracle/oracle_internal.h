@@ -35,6 +35,8 @@ void block_on_grid(const Basis& B, const double* xyz, int npts, double thr, int 
  *               out = {e, dF/dna, dF/dnb, dF/dga(3), dF/dgb(3)} */
 void functional_point(int func, int nspin, const double* in, double* out);
 bool functional_is_gga(int func);
+/* restricted linear-response kernel contracted with (rho1, grad rho1): v1, g1[3] */
+void lr_kernel_point(int func, double n0, const double* g0, double n1, const double* g1, double* v1, double* gg1);
 
 }  // namespace orc
 #endif

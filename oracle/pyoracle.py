@@ -221,3 +221,38 @@ def xc_gradient(basis, shell_atom, natoms, xyz, w, func, P, max_block=128, thr=1
                       np.ascontiguousarray(w, dtype=np.float64), n, max_block, thr, FUNC[func] if isinstance(func, str)
                       else int(func), nspin, Pc, out)
     return out.reshape(3, natoms).T
+
+
+def lr_kernel(func, rho0, grad0, rho1, grad1):
+    """Restricted linear-response kernel contracted with (rho1, grad rho1) on points:
+    (v1 [n], g1 [3, n] or None).  rho [n], grad [3, n]."""
+    fid = FUNC[func] if isinstance(func, str) else int(func)
+    gga = bool(lib().orc_functional_is_gga(fid))
+    rho0 = np.ascontiguousarray(rho0, dtype=np.float64).reshape(-1)
+    n = rho0.size
+    rho1 = np.ascontiguousarray(rho1, dtype=np.float64).reshape(-1)
+    g0 = np.ascontiguousarray(grad0, dtype=np.float64).reshape(-1) if gga else None
+    g1 = np.ascontiguousarray(grad1, dtype=np.float64).reshape(-1) if gga else None
+    v1 = np.zeros(n)
+    go = np.zeros(3 * n) if gga else None
+    L = lib()
+    L.orc_lr_kernel.argtypes = [ctypes.c_int, ctypes.c_long, _dp, ctypes.c_void_p, _dp, ctypes.c_void_p, _dp,
+                                ctypes.c_void_p]
+    L.orc_lr_kernel(fid, n, rho0, _ptr(g0), rho1, _ptr(g1), v1, _ptr(go))
+    return v1, (go.reshape(3, n) if gga else None)
+
+
+def lr_fock(basis, xyz, w, func, P0, D, max_block=128, thr=1e-9, ave_thr=1e-11):
+    """XC-kernel part of a restricted (singlet) linear-response sigma vector
+    (KernelSigmavector<RESTRICTED>::calcF, KernelSigmavector.cpp:128-253): the trial matrix
+    D is symmetrised, its density rho1 = phi^T D phi and gradient are contracted with the
+    ground-state kernel, and the result goes through the adder (F + F^T).  No per-element
+    screening (the reference screens D_ij avg_i avg_j and the integration by block
+    averages at 1e-11; here only the adder's block skip applies)."""
+    D = np.asarray(D, dtype=np.float64)
+    Ds = 0.5 * (D + D.T)
+    gga = bool(lib().orc_functional_is_gga(FUNC[func] if isinstance(func, str) else int(func)))
+    r0, g0 = basis.density(xyz, P0, max_block, thr, grad=gga)
+    r1, g1 = basis.density(xyz, Ds, max_block, thr, grad=gga)
+    v1, gv1 = lr_kernel(func, r0[0], g0[0] if gga else None, r1[0], g1[0] if gga else None)
+    return basis.add_scalar(xyz, w, v1, gv1.reshape(1, 3, -1) if gga else None, max_block, thr, ave_thr)[0]

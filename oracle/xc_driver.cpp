@@ -391,3 +391,36 @@ extern "C" int orc_xc_gradient(const void* basis, const int* shell_atom, int nat
                    nspin, P, out);
   return 0;
 }
+
+// Restricted linear-response kernel on points (KernelSigmavector<RESTRICTED> singlet
+// contraction before the numerical integration): blocks of 128 points whose ground-state
+// density sums below 128e-12 give zero (the functional data's block skip); grad0/grad1
+// are [3][npts] (GGA only), g1 [3][npts].
+extern "C" int orc_lr_kernel(int func, long npts, const double* rho0, const double* grad0, const double* rho1,
+                             const double* grad1, double* v1, double* g1) {
+  const bool gga = orc::functional_is_gga(func);
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < (npts + 127) / 128; ++b) {
+    const long first = b * 128, n = std::min<long>(128, npts - first);
+    double sum = 0.0;
+    for (long p = first; p < first + n; ++p) sum += std::fabs(rho0[p]);
+    const bool skip = sum < n * 1e-12;
+    for (long p = first; p < first + n; ++p) {
+      double a0[3] = {0, 0, 0}, a1[3] = {0, 0, 0}, out[3] = {0, 0, 0};
+      double v = 0.0;
+      if (!skip) {
+        if (gga)
+          for (int k = 0; k < 3; ++k) {
+            a0[k] = grad0[k * npts + p];
+            a1[k] = grad1[k * npts + p];
+          }
+        orc::lr_kernel_point(func, rho0[p], a0, rho1[p], a1, &v, out);
+      }
+      v1[p] = v;
+      if (gga)
+        for (int k = 0; k < 3; ++k) g1[k * npts + p] = out[k];
+    }
+  }
+  return 0;
+}
+

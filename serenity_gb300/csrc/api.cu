@@ -1092,6 +1092,88 @@ xcgpu_status xcgpu_xc_gradient(xcgpu_plan* P, int func, int nspin, const double*
   return c->cuda(cudaStreamSynchronize(c->stream), "xc_gradient");
 }
 
+xcgpu_status xcgpu_lr_kernel(xcgpu_plan* P, int func, const double* P0, uint32_t ntrial, const double* const* D,
+                             double* const* F, int precision, double thr, int mem) {
+  if (!P) return XCGPU_ERR_INVALID;
+  Ctx* c = P->ctx;
+  if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "lr_kernel: unknown functional");
+  if (!P0 || (ntrial > 0 && (!D || !F))) return c->fail(XCGPU_ERR_INVALID, "lr_kernel: bad arguments");
+  if (precision != XCGPU_PREC_FP64 && precision != XCGPU_PREC_MIXED)
+    return c->fail(XCGPU_ERR_INVALID, "lr_kernel: unknown precision");
+  for (uint32_t t = 0; t < ntrial; ++t)
+    if (!D[t] || !F[t]) return c->fail(XCGPU_ERR_INVALID, "lr_kernel: null trial or output matrix");
+  cudaSetDevice(c->device);
+  const bool gga = xc::is_gga(func), mixed = precision == XCGPU_PREC_MIXED;
+  const long n = P->grid->n;
+  const int nbf = P->basis->nbf;
+  const size_t nn = (size_t)nbf * nbf;
+  XC_TRY(ensure_work(P, 1, gga, mixed));
+  XC_TRY(P->n_rho.alloc(c, (size_t)n * sizeof(double)));
+  XC_TRY(P->n_dfdrho.alloc(c, (size_t)n * sizeof(double)));
+  if (gga) {
+    XC_TRY(P->n_grad.alloc(c, (size_t)3 * n * sizeof(double)));
+    XC_TRY(P->n_dfdgrad.alloc(c, (size_t)3 * n * sizeof(double)));
+  }
+  const double* P0d = P0;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(upload(c, P->w_P, P0, nn));
+    P0d = P->w_P.as<double>();
+  }
+  DevBuf dD, dS, dF;
+  XC_TRY(dS.alloc(c, nn * sizeof(double)));
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(dD.alloc(c, nn * sizeof(double)));
+    XC_TRY(dF.alloc(c, nn * sizeof(double)));
+  }
+  int* counter = nullptr;
+  XC_TRY(c->aux(&counter));
+  int* err = counter + 2;
+  XC_TRY(c->cuda(cudaMemsetAsync(counter, 0, 4 * sizeof(int), c->stream), "memset aux"));
+  // density of a symmetric matrix M into (rho, grad)
+  auto density = [&](const double* M, double* rho, double* grad) -> xcgpu_status {
+    if (!mixed) return stage_density(P, 1, M, rho, grad);
+    xcgpu_status st = mixed_split(c, M, P->w_psplit.as<float>(), (long)nn);
+    if (st) return st;
+    std::vector<MixedWork> work(1);
+    work[0] = MixedWork{&P->basis->dev, &P->dev, 1, P->w_psplit.as<float>(), rho, grad, nullptr, nullptr, nullptr, nullptr};
+    return mixed_density_batch(c, work, counter, err);
+  };
+  // ground state (the kernel's expansion point)
+  XC_TRY(density(P0d, P->w_rho.as<double>(), gga ? P->w_grad.as<double>() : nullptr));
+  for (uint32_t t = 0; t < ntrial; ++t) {
+    const double* Dd = D[t];
+    double* Fd = F[t];
+    if (mem == XCGPU_MEM_HOST) {
+      XC_TRY(c->cuda(cudaMemcpyAsync(dD.p, D[t], nn * sizeof(double), cudaMemcpyHostToDevice, c->stream), "trial"));
+      Dd = dD.as<double>();
+      Fd = dF.as<double>();
+    }
+    // perturbed density of (D + D^T) / 2 (KernelSigmavector.cpp:227-233 symmetrises D)
+    XC_TRY(launch_symmetrise_half(c, Dd, dS.as<double>(), nbf));
+    XC_TRY(density(dS.as<double>(), P->n_rho.as<double>(), gga ? P->n_grad.as<double>() : nullptr));
+    XC_TRY(launch_lr_kernel(c, func, n, P->w_rho.as<double>(), gga ? P->w_grad.as<double>() : nullptr,
+                            P->n_rho.as<double>(), gga ? P->n_grad.as<double>() : nullptr, P->n_dfdrho.as<double>(),
+                            gga ? P->n_dfdgrad.as<double>() : nullptr));
+    XC_TRY(c->cuda(cudaMemsetAsync(Fd, 0, nn * sizeof(double), c->stream), "memset F"));
+    const double* gv = gga ? P->n_dfdgrad.as<double>() : nullptr;
+    if (mixed) {
+      XC_TRY(launch_block_skip_flags(c, P->dev, 1, P->n_dfdrho.as<double>(), gv, thr, P->w_skip.as<unsigned char>()));
+      std::vector<MixedWork> work(1);
+      work[0] = MixedWork{&P->basis->dev, &P->dev, 1, nullptr, nullptr, nullptr, P->n_dfdrho.as<double>(), gv,
+                          P->w_skip.as<unsigned char>(), Fd};
+      XC_TRY(mixed_adder_batch(c, work, counter + 1, err));
+    } else {
+      XC_TRY(stage_adder(P, 1, P->n_dfdrho.as<double>(), gv, thr, Fd));
+    }
+    if (mem == XCGPU_MEM_HOST)
+      XC_TRY(c->cuda(cudaMemcpyAsync(F[t], Fd, nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "F"));
+  }
+  int herr = 0;
+  XC_TRY(c->cuda(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "lr_kernel"));
+  return device_error(c, herr, "lr_kernel");
+}
+
 xcgpu_status xcgpu_nadd_vxc_all(xcgpu_plan* const* plans, uint32_t n_sub, int func, int nspin, int precision,
                                 double thr, const double* const* P, double* const* V, double* E_nadd, int mem) {
   if (!plans || n_sub == 0 || !plans[0]) return XCGPU_ERR_INVALID;

@@ -104,6 +104,8 @@ def library(build_if_needed=True):
     L.xcgpu_nadd_vxc.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_uint32, S, S, S, ctypes.c_double, vp,
                                  ctypes.POINTER(vp), vp, dp, S]
     L.xcgpu_xc_gradient.argtypes = [vp, S, S, vp, vp, S, vp, S]
+    L.xcgpu_lr_kernel.argtypes = [vp, S, vp, ctypes.c_uint32, ctypes.POINTER(vp), ctypes.POINTER(vp), S,
+                                  ctypes.c_double, S]
     L.xcgpu_nadd_vxc_all.argtypes = [ctypes.POINTER(vp), ctypes.c_uint32, S, S, S, ctypes.c_double,
                                      ctypes.POINTER(vp), ctypes.POINTER(vp), dp, S]
     L.xcgpu_check_async.argtypes = [vp]
@@ -113,7 +115,7 @@ def library(build_if_needed=True):
     L.xcgpu_graph_destroy.argtypes = [vp]
     L.xcgpu_set_timing.argtypes = [vp, S]
     L.xcgpu_get_timing.argtypes = [vp, vp, vp]
-    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_nadd_vxc_all", "xcgpu_xc_gradient", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
+    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_nadd_vxc_all", "xcgpu_xc_gradient", "xcgpu_lr_kernel", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
                  "xcgpu_graph_launch", "xcgpu_set_timing", "xcgpu_get_timing"]:
         getattr(L, name).restype = S
     for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
@@ -404,6 +406,21 @@ class Plan:
         self.ctx.check(self.ctx.L.xcgpu_vxc(self.h, fid, nspin, precision, block_ave_threshold, _ptr(Pc), _ptr(V),
                                             ctypes.byref(exc), ctypes.byref(nel), MEM_HOST))
         return V.transpose(0, 2, 1), exc.value, nel.value
+
+    def lr_kernel(self, func, P0, trials, precision=PREC_FP64, block_ave_threshold=1e-11):
+        """XC kernel part of restricted (singlet) linear-response sigma vectors: for each
+        trial matrix D (host [nbf, nbf]) the matrix F (KernelSigmavector<RESTRICTED>::calcF).
+        P0: ground-state total density matrix."""
+        fid = FUNC[func] if isinstance(func, str) else int(func)
+        P0c = np.ascontiguousarray(np.asarray(P0, dtype=np.float64).T)
+        Ds = [np.ascontiguousarray(np.asarray(D, dtype=np.float64).T) for D in trials]
+        Fs = [np.zeros((self.nbf, self.nbf)) for _ in trials]
+        k = len(trials)
+        dp = (vp * max(1, k))(*[x.ctypes.data for x in Ds])
+        fp = (vp * max(1, k))(*[x.ctypes.data for x in Fs])
+        self.ctx.check(self.ctx.L.xcgpu_lr_kernel(self.h, fid, _ptr(P0c), k, dp, fp, precision, block_ave_threshold,
+                                                  MEM_HOST))
+        return [F.T for F in Fs]
 
     def xc_gradient(self, func, P, shell_atom, natoms):
         """XC part of the nuclear gradient (FuncPotential<M>::getGeomGradients), FP64:

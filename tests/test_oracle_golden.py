@@ -135,3 +135,26 @@ def test_xc_gradient_is_the_fixed_grid_derivative(func, unrestricted):
             return po.Basis(Shells.for_atoms(sym, x2, "DEF2-SVP")).vxc(pts, wts, func, P, thr=0.0, ave_thr=0.0)[1]
         fd = (E(h) - E(-h)) / (2 * h)
         assert abs(G[atom, k] - fd) <= 2e-8, (atom, k, G[atom, k], fd)
+
+
+@pytest.mark.parametrize("func", ["LDA", "PBE", "BLYP"])
+def test_lr_kernel_is_the_derivative_of_the_xc_matrix(func):
+    """The restricted linear-response kernel contraction (KernelSigmavector<RESTRICTED>
+    singlet, second functional derivatives by second-order forward-mode differentiation)
+    is the derivative of the XC matrix along the trial density: F(D) = d/de Vxc[P0 + e D]
+    for symmetric D (the reference's tests of this path need LRSCF solver runs)."""
+    from serenity_gb300 import workload as wl
+    sym, xyz = wl.water_cluster(1, 5, jitter=0.1)
+    w = wl.Workload(sym, xyz, "DEF2-SVP", func, 5, 30, 110, 6)
+    P0 = w.density()
+    rng = np.random.default_rng(8)
+    D = rng.standard_normal(P0.shape) * 0.05
+    D = D + D.T
+    pts, wts = po.becke_grid(w.Z, xyz, n_rad=30, n_ang=110)
+    B = po.Basis(w.shells)
+    F = po.lr_fock(B, pts, wts, func, P0, D, thr=0.0, ave_thr=0.0)
+    h = 1e-5
+    Vp = B.vxc(pts, wts, func, P0 + h * D, thr=0.0, ave_thr=0.0)[0][0]
+    Vm = B.vxc(pts, wts, func, P0 - h * D, thr=0.0, ave_thr=0.0)[0][0]
+    fd = (Vp - Vm) / (2 * h)
+    assert np.abs(F - fd).max() <= 1e-6 * max(1.0, np.abs(fd).max()), np.abs(F - fd).max()
