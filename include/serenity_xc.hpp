@@ -8,6 +8,8 @@
  *   ScalarOperatorToMatrixAdder<M>    src/data/grid/ScalarOperatorToMatrixAdder.h:56-93
  *   FuncPotential<M> (getMatrix, getEnergy)  src/potentials/FuncPotential.h
  *   NAddFuncPotential<M> (getMatrix, getEnergy)  src/potentials/NAddFuncPotential.h
+ *   FuncPotential<M>::getGeomGradients           src/potentials/FuncPotential.cpp:113-241
+ *   KernelSigmavector (restricted singlet calcF)  src/postHF/LRSCF/Sigmavectors/KernelSigmavector.h
  *
  * Errors are thrown as SerenityError, as in the reference.  Matrices and grid data are
  * plain column-major containers with the memory layout of Eigen's defaults
@@ -438,6 +440,17 @@ class FuncPotential {
   }
   double getEnergy() const { return energy_; }
   double getNumberOfElectrons() const { return nel_; }
+  // getGeomGradients (FuncPotential.cpp:113-241): natoms x 3; shellAtoms[s] = atom of shell s
+  // (BasisController::getAtomIndicesOfBasis).  FP64.
+  Matrix getGeomGradients(const DensityMatrix<M>& P, const std::vector<int>& shellAtoms, int natoms) {
+    const int ns = detail::nspin<M>();
+    std::vector<double> Pv;
+    detail::pack(P, Pv);
+    Matrix G(natoms, 3);
+    detail::check(bfog_->ctx(), xcgpu_xc_gradient(bfog_->handle(), (int)f_, ns, Pv.data(), shellAtoms.data(), natoms,
+                                                  G.data(), XCGPU_MEM_HOST));
+    return G;
+  }
 
  private:
   std::shared_ptr<BasisFunctionOnGridController> bfog_;
@@ -445,6 +458,36 @@ class FuncPotential {
   double thr_;
   int precision_;
   double energy_ = 0.0, nel_ = 0.0;
+};
+
+// The XC kernel part of restricted (singlet) linear-response sigma vectors
+// (KernelSigmavector<RESTRICTED>::calcF, src/postHF/LRSCF/Sigmavectors/KernelSigmavector.cpp:128-392):
+// calcF(P0, trials) returns one matrix per trial matrix.
+class KernelSigmavector {
+ public:
+  KernelSigmavector(std::shared_ptr<BasisFunctionOnGridController> bfog, Functional f,
+                    double blockAveThreshold = 1e-11, int precision = XCGPU_PREC_FP64)
+      : bfog_(bfog), f_(f), thr_(blockAveThreshold), precision_(precision) {}
+  std::vector<Matrix> calcF(const Matrix& P0, const std::vector<Matrix>& trials) {
+    const long nbf = bfog_->getNBasisFunctions();
+    std::vector<Matrix> F(trials.size(), Matrix(nbf, nbf));
+    std::vector<const double*> d;
+    std::vector<double*> f;
+    for (size_t t = 0; t < trials.size(); ++t) {
+      if (trials[t].rows() != nbf || trials[t].cols() != nbf) throw SerenityError("KernelSigmavector: size mismatch");
+      d.push_back(trials[t].data());
+      f.push_back(F[t].data());
+    }
+    detail::check(bfog_->ctx(), xcgpu_lr_kernel(bfog_->handle(), (int)f_, P0.data(), (uint32_t)trials.size(), d.data(),
+                                                f.data(), precision_, thr_, XCGPU_MEM_HOST));
+    return F;
+  }
+
+ private:
+  std::shared_ptr<BasisFunctionOnGridController> bfog_;
+  Functional f_;
+  double thr_;
+  int precision_;
 };
 
 // NAddFuncPotential<M> (src/potentials/NAddFuncPotential.h:93-200): the non-additive XC
