@@ -124,20 +124,25 @@ constexpr int kNT = 128;                      // rows of an operand tile (M, and
 constexpr uint32_t kStageBytes = 4 * kTileA;  // A_hi, A_lo, B_hi, B_lo
 constexpr uint32_t kColsHH0 = 0, kColsHH1 = 128, kColsX0 = 256, kColsX1 = 384;
 constexpr int kTileFloats = 128 * 32;         // one operand tile (hi or lo) in floats
-constexpr int kAdderStages = 3;
+constexpr int kAdderStages = 2;
+constexpr int kDsLd = 129;  // row stride of the adder's transpose tile (conflict-free both ways)
 
 // hi*hi of one 32-wide K chunk into a fresh accumulator, the two cross products into
 // the tile's cross accumulator
 __device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl, int N,
                                             uint32_t hh_cols, uint32_t x_cols, bool first_chunk) {
   const uint32_t idesc = tc::idesc_tf32(128, N);
+  // descriptors of the four operand tiles; a k-slice of 8 TF32 (32 bytes) advances the
+  // start-address field (bits 0-13, in 16-byte units) by 2, without carry since every
+  // address stays below 256 KB
+  const uint64_t dah = tc::smem_desc_sw128(ah), dal = tc::smem_desc_sw128(al);
+  const uint64_t dbh = tc::smem_desc_sw128(bh), dbl = tc::smem_desc_sw128(bl);
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks) {
-    const uint32_t o = ks * 32;
-    tc::mma_tf32(tmem + hh_cols, tc::smem_desc_sw128(ah + o), tc::smem_desc_sw128(bh + o), idesc, ks > 0 ? 1u : 0u);
-    tc::mma_tf32(tmem + x_cols, tc::smem_desc_sw128(ah + o), tc::smem_desc_sw128(bl + o), idesc,
-                 (!first_chunk || ks > 0) ? 1u : 0u);
-    tc::mma_tf32(tmem + x_cols, tc::smem_desc_sw128(al + o), tc::smem_desc_sw128(bh + o), idesc, 1u);
+    const uint64_t o = 2u * ks;
+    tc::mma_tf32(tmem + hh_cols, dah + o, dbh + o, idesc, ks > 0 ? 1u : 0u);
+    tc::mma_tf32(tmem + x_cols, dah + o, dbl + o, idesc, (!first_chunk || ks > 0) ? 1u : 0u);
+    tc::mma_tf32(tmem + x_cols, dal + o, dbh + o, idesc, 1u);
   }
 }
 
@@ -478,6 +483,7 @@ __global__ void __launch_bounds__(kT, 1)
   __shared__ float s_w[2][4][128];  // per spin and point: w v / 2, w g_x, w g_y, w g_z
   const uint32_t base_s = tc::smem_u32(smem_raw);
   uint8_t* sm = smem_raw + ((1024 - (base_s & 1023)) & 1023);
+  float* Ds = reinterpret_cast<float*>(sm + kAdderStages * kStageBytes);  // [128][kDsLd], a product's tile
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
   if (tid == 0) {
@@ -589,64 +595,86 @@ __global__ void __launch_bounds__(kT, 1)
     }
     __syncthreads();
     // ---- 2. tile products ----
+    // F_b = D + D^T with D = Phi^T G is symmetric, so V is accumulated on and above the
+    // diagonal only (a mirror kernel fills the rest): per spin, for every function tile
+    // pair a <= b, the products D(a, b) and (a < b) D(b, a) run back to back; D(a, a) is
+    // folded with its transpose, D(b, a) transposed onto D(a, b), through Ds in shared
+    // memory, and each element goes to V with one FP64 atomic.  Steps run over
+    // (spin, a, b, product, 32-point chunk), chunk fastest; the copy issuer and the MMA
+    // issuer (thread 0) and the drain (all threads) walk them with incremental cursors.
     const int nsteps = __popc(smask) * nft * nft * nkc;
-    // step i -> (spin, m tile, n tile, chunk), chunk fastest
-    auto decode = [&](int i, int& s, int& mt, int& nt, int& kc) {
-      kc = i % nkc;
-      int r = i / nkc;
-      nt = r % nft;
-      r /= nft;
-      mt = r % nft;
-      const int si = r / nft;
-      s = (smask == 2) ? 1 : si;
+    struct Cursor {
+      int si, a, b, ph, kc, prod, st;  // ph: 0 = D(a, b), 1 = D(b, a)
     };
-    auto issue_copy = [&](int i) {
-      int s, mt, nt, kc;
-      decode(i, s, mt, nt, kc);
-      const int st = i % kAdderStages;
-      uint8_t* dst = sm + st * kStageBytes;
+    auto advance = [&](Cursor& c) {
+      c.st = (c.st + 1 == kAdderStages) ? 0 : c.st + 1;
+      if (++c.kc < nkc) return;
+      c.kc = 0;
+      ++c.prod;
+      if (c.ph == 0 && c.a < c.b) {
+        c.ph = 1;
+        return;
+      }
+      c.ph = 0;
+      if (++c.b < nft) return;
+      if (++c.a < nft) {
+        c.b = c.a;
+        return;
+      }
+      c.a = c.b = 0;
+      ++c.si;
+    };
+    auto mt_of = [](const Cursor& c) { return c.ph ? c.b : c.a; };
+    auto nt_of = [](const Cursor& c) { return c.ph ? c.a : c.b; };
+    auto spin_of = [&](const Cursor& c) { return (smask == 2) ? 1 : c.si; };
+    auto issue_copy = [&](const Cursor& c) {
+      uint8_t* dst = sm + c.st * kStageBytes;
+      const int mt = mt_of(c), nt = nt_of(c);
       const int nM = min(128, nact - 128 * mt), nN = min(128, nact - 128 * nt);
       const uint32_t ab = (uint32_t)((nM + 7) & ~7) * 128u, bb = (uint32_t)((nN + 15) & ~15) * 128u;
-      const float* a = my + (long)(mt * 4 + kc) * 2 * kTileFloats;
-      const float* g = my + (long)(1 + s) * opstride + (long)(nt * 4 + kc) * 2 * kTileFloats;
-      tc::mbar_arrive_expect_tx(&full[st], 2 * ab + 2 * bb);
-      tc::bulk_g2s(dst, a, ab, &full[st]);
-      tc::bulk_g2s(dst + kTileA, a + kTileFloats, ab, &full[st]);
-      tc::bulk_g2s(dst + 2 * kTileA, g, bb, &full[st]);
-      tc::bulk_g2s(dst + 3 * kTileA, g + kTileFloats, bb, &full[st]);
+      const float* a = my + (long)(mt * 4 + c.kc) * 2 * kTileFloats;
+      const float* g = my + (long)(1 + spin_of(c)) * opstride + (long)(nt * 4 + c.kc) * 2 * kTileFloats;
+      tc::mbar_arrive_expect_tx(&full[c.st], 2 * ab + 2 * bb);
+      tc::bulk_g2s(dst, a, ab, &full[c.st]);
+      tc::bulk_g2s(dst + kTileA, a + kTileFloats, ab, &full[c.st]);
+      tc::bulk_g2s(dst + 2 * kTileA, g, bb, &full[c.st]);
+      tc::bulk_g2s(dst + 3 * kTileA, g + kTileFloats, bb, &full[c.st]);
     };
+    Cursor cc = {0, 0, 0, 0, 0, 0, 0}, mc = cc, dc = cc;  // copy, MMA, drain
     issued = consumed = committed = drained = 0;
-    float acc[32];  // this thread's 32 columns of one row of the current tile pair
+    float acc[32];  // this thread's 32 columns of one row of the current product
+    const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
     if (tid == 0)
-      for (; issued < min(kAdderStages, nsteps); ++issued) issue_copy(issued);
+      for (; issued < min(kAdderStages, nsteps); ++issued) {
+        issue_copy(cc);
+        advance(cc);
+      }
     for (int i = 0; i <= nsteps; ++i) {
       bool bad = false;
       if (tid == 0 && i < nsteps) {
-        const int st = i % kAdderStages;
-        if (tc::mbar_wait_bounded(&full[st], (fph >> st) & 1u, kWaitLimitNs)) {
-          fph ^= 1u << st;
+        if (tc::mbar_wait_bounded(&full[mc.st], (fph >> mc.st) & 1u, kWaitLimitNs)) {
+          fph ^= 1u << mc.st;
           ++consumed;
           tc::fence_after_sync();
-          int s, mt, nt, kc;
-          decode(i, s, mt, nt, kc);
-          const int N = (min(128, nact - 128 * nt) + 15) & ~15;
-          const uint32_t sa = tc::smem_u32(sm + st * kStageBytes);
+          const int N = (min(128, nact - 128 * nt_of(mc)) + 15) & ~15;
+          const uint32_t sa = tc::smem_u32(sm + mc.st * kStageBytes);
           issue_chunk(tmem, sa, sa + kTileA, sa + 2 * kTileA, sa + 3 * kTileA, N, (i & 1) ? kColsHH1 : kColsHH0,
-                      ((i / nkc) & 1) ? kColsX1 : kColsX0, kc == 0);
-          tc::mma_commit(&mdone[st]);
+                      (mc.prod & 1) ? kColsX1 : kColsX0, mc.kc == 0);
+          tc::mma_commit(&mdone[mc.st]);
           ++committed;
+          advance(mc);
         } else {
           bad = true;
         }
       }
       if (i >= 1) {
-        const int j = i - 1, st = j % kAdderStages;
-        if (tc::mbar_wait_bounded(&mdone[st], (mph >> st) & 1u, kWaitLimitNs)) {
-          mph ^= 1u << st;
+        if (tc::mbar_wait_bounded(&mdone[dc.st], (mph >> dc.st) & 1u, kWaitLimitNs)) {
+          mph ^= 1u << dc.st;
           ++drained;
-          // the MMAs of step j are done with stage st: refill it for step j + 3
-          if (tid == 0 && j + kAdderStages < nsteps) {
-            issue_copy(j + kAdderStages);
+          // the MMAs of step i - 1 are done with its stage: refill it for step i + 1
+          if (tid == 0 && issued < nsteps) {
+            issue_copy(cc);
+            advance(cc);
             ++issued;
           }
         } else {
@@ -659,24 +687,41 @@ __global__ void __launch_bounds__(kT, 1)
       }
       if (i >= 1) {
         tc::fence_after_sync();
-        const int j = i - 1;
-        int s, mt, nt, kc;
-        decode(j, s, mt, nt, kc);
-        const int nN = min(128, nact - 128 * nt);
+        const int mt = mt_of(dc), nt = nt_of(dc);
+        const int nM = min(128, nact - 128 * mt), nN = min(128, nact - 128 * nt);
         const int N = (nN + 15) & ~15;
-        drain_regs(tmem + ((j & 1) ? kColsHH1 : kColsHH0), warp, acc, kc == 0, N);
-        if (kc == nkc - 1) {
-          drain_regs(tmem + (((j / nkc) & 1) ? kColsX1 : kColsX0), warp, acc, false, N);
-          const int nM = min(128, nact - 128 * mt);
-          const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
-          if (row < nM) {
-            double* Vs = I.V + (long)s * nbf * nbf + __ldg(fn + 128 * mt + row);
-            const int* fnn = fn + 128 * nt + c0;
+        drain_regs(tmem + (((i - 1) & 1) ? kColsHH1 : kColsHH0), warp, acc, dc.kc == 0, N);
+        if (dc.kc == nkc - 1) {  // end of a product
+          drain_regs(tmem + ((dc.prod & 1) ? kColsX1 : kColsX0), warp, acc, false, N);
+          if (dc.ph == 0) {
 #pragma unroll
-            for (int c = 0; c < 32; ++c)
-              if (c0 + c < nN) atomicAdd(Vs + (long)__ldg(fnn + c) * nbf, (double)acc[c]);
+            for (int c = 0; c < 32; ++c) Ds[row * kDsLd + c0 + c] = acc[c];
+          } else {  // D(b, a): row n of tile b, columns m of tile a -> Ds[m][n]
+#pragma unroll
+            for (int c = 0; c < 32; ++c) Ds[(c0 + c) * kDsLd + row] += acc[c];
+          }
+          const bool flush = dc.a == dc.b || dc.ph == 1;
+          if (flush) {  // uniform across the CTA
+            __syncthreads();
+            // thread row m of tile a, columns n of tile b: F(m, n) into V(fn_a[m], fn_b[n])
+            const int ma = min(128, nact - 128 * dc.a), nb_ = min(128, nact - 128 * dc.b);
+            if (row < ma) {
+              double* Vs = I.V + (long)spin_of(dc) * nbf * nbf + __ldg(fn + 128 * dc.a + row);
+              const int* fnb = fn + 128 * dc.b + c0;
+              const bool diag = dc.a == dc.b;
+#pragma unroll 8
+              for (int c = 0; c < 32; ++c) {
+                const int n = c0 + c;
+                if (n < nb_ && (!diag || n >= row)) {
+                  const float f = diag ? Ds[row * kDsLd + n] + Ds[n * kDsLd + row] : Ds[row * kDsLd + n];
+                  atomicAdd(Vs + (long)__ldg(fnb + c) * nbf, (double)f);
+                }
+              }
+            }
+            __syncthreads();  // Ds is reused by the next product
           }
         }
+        advance(dc);
         tc::fence_before_sync();
       }
       __syncthreads();
@@ -712,6 +757,19 @@ __global__ void split_p_kernel(const double* __restrict__ P, float* __restrict__
   lo[i] = __uint_as_float(l);
 }
 
+// V holds sum_b F_b on and above the diagonal (row <= column): copy it below
+__global__ void mirror_upper_kernel(double* V, int nbf, int nspin) {
+  const long n2 = (long)nbf * nbf;
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n2 * nspin) return;
+  const int s = (int)(idx / n2);
+  const long e = idx % n2;
+  const int i = (int)(e % nbf), j = (int)(e / nbf);  // row i, column j (column-major)
+  if (i <= j) return;
+  double* M = V + (long)s * n2;
+  M[e] = M[(long)i * nbf + j];
+}
+
 // V <- V + V^T (per spin), turning sum_b D_b into sum_b (D_b + D_b^T)
 __global__ void symmetrize_kernel(double* V, int nbf, int nspin) {
   const long n2 = (long)nbf * nbf;
@@ -732,7 +790,7 @@ __global__ void symmetrize_kernel(double* V, int nbf, int nspin) {
 }
 
 static size_t density_smem() { return 2 * kStageBytes + 128 * (kNT + 1) * sizeof(float) + 1024; }
-static size_t adder_smem() { return kAdderStages * kStageBytes + 1024; }
+static size_t adder_smem() { return kAdderStages * kStageBytes + 128 * kDsLd * sizeof(float) + 1024; }
 
 xcgpu_status mixed_init(Ctx* c) {
   const struct {
@@ -862,8 +920,8 @@ xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* 
   KernelTimer kt2(c, kOther);
   for (const auto& w : work) {
     const long n = (long)w.P->nbf * w.P->nbf * w.nspin;
-    symmetrize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(w.V, w.P->nbf, w.nspin);
-    if ((st = c->check_launch("symmetrize_kernel"))) return st;
+    mirror_upper_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(w.V, w.P->nbf, w.nspin);
+    if ((st = c->check_launch("mirror_upper_kernel"))) return st;
   }
   return XCGPU_OK;
 }
