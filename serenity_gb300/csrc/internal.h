@@ -241,7 +241,7 @@ struct MixedWork {
   const DevBasis* B;
   const DevPlan* P;
   int nspin;
-  float* Psplit;  // 2 * nspin * nbf^2 floats
+  float* Psplit;  // 2 * nspin * nbf^2 floats: TF32 (hi, lo) pairs, interleaved
   double* rho;
   double* grad;
   const double* v;

@@ -184,8 +184,7 @@ struct MxItem {
   DevBasis B;
   DevPlan P;
   int nspin;
-  const float* Phi;  // TF32 split of the density matrices (density kernel)
-  const float* Plo;
+  const float2* Psplit;  // TF32 split (hi, lo) of the density matrices, interleaved (density kernel)
   double* rho;  // outputs of the density kernel
   double* grad;
   const double* v;  // inputs of the adder kernel
@@ -314,8 +313,7 @@ __global__ void __launch_bounds__(kT, 1)
     }
     __syncthreads();
     for (int s = 0; s < nspin; ++s) {
-      const float* __restrict__ Ph = I.Phi + (long)s * nbf * nbf;
-      const float* __restrict__ Pl = I.Plo + (long)s * nbf * nbf;
+      const float2* __restrict__ Pspin = I.Psplit + (long)s * nbf * nbf;
       double r_acc = 0.0, g_acc[3] = {0.0, 0.0, 0.0};
       for (int nu0 = 0; nu0 < nact; nu0 += kNT) {
         const int nnu = min(kNT, nact - nu0);
@@ -347,17 +345,13 @@ __global__ void __launch_bounds__(kT, 1)
             const int mu = mu0 + lane;
             const bool muok = mu < nact;
             const long cmu = muok ? (long)__ldg(fn + mu) : 0;
-#pragma unroll 4
+#pragma unroll 8
             for (int row = warp; row < N; row += kWarps) {
-              float h = 0.f, l = 0.f;
-              if (muok && row < nnu) {
-                const long o = (long)__ldg(fn + nu0 + row) * nbf + cmu;
-                h = __ldg(Ph + o);
-                l = __ldg(Pl + o);
-              }
+              float2 hl = make_float2(0.f, 0.f);
+              if (muok && row < nnu) hl = __ldg(Pspin + (long)__ldg(fn + nu0 + row) * nbf + cmu);
               const uint32_t off = tc::swz_offset(row, lane);
-              *reinterpret_cast<float*>(Bhi + off) = h;
-              *reinterpret_cast<float*>(Blo + off) = l;
+              *reinterpret_cast<float*>(Bhi + off) = hl.x;
+              *reinterpret_cast<float*>(Blo + off) = hl.y;
             }
           }
           tc::fence_async_smem();
@@ -748,13 +742,12 @@ done:
 }
 
 // TF32 split of the density matrices (hi = TF32(P), lo = TF32(P - hi)), once per build
-__global__ void split_p_kernel(const double* __restrict__ P, float* __restrict__ hi, float* __restrict__ lo, long n) {
+__global__ void split_p_kernel(const double* __restrict__ P, float2* __restrict__ out, long n) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t h, l;
   tc::split_tf32(P[i], h, l);
-  hi[i] = __uint_as_float(h);
-  lo[i] = __uint_as_float(l);
+  out[i] = make_float2(__uint_as_float(h), __uint_as_float(l));
 }
 
 // V holds sum_b F_b on and above the diagonal (row <= column): copy it below
@@ -816,8 +809,7 @@ static void fill_item(MxItem& it, const MixedWork& w) {
   it.P = *w.P;
   it.nspin = w.nspin;
   const long n = (long)w.P->nbf * w.P->nbf * w.nspin;
-  it.Phi = w.Psplit;
-  it.Plo = w.Psplit ? w.Psplit + n : nullptr;
+  it.Psplit = reinterpret_cast<const float2*>(w.Psplit);
   it.rho = w.rho;
   it.grad = w.grad;
   it.v = w.v;
@@ -876,7 +868,7 @@ static bool any_gga(const std::vector<MixedWork>& work, size_t i0, size_t i1, bo
 
 xcgpu_status mixed_split(Ctx* c, const double* Pm, float* Psplit, long n) {
   KernelTimer kt(c, kOther);
-  split_p_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(Pm, Psplit, Psplit + n, n);
+  split_p_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(Pm, reinterpret_cast<float2*>(Psplit), n);
   return c->check_launch("split_p_kernel");
 }
 
