@@ -185,6 +185,8 @@ void xcgpu_ctx_destroy(xcgpu_ctx* c) {
   c->batch_items.release();
   c->host_items.release();
   c->aux_by_stream.clear();
+  c->arena_by_stream.clear();
+  c->fp64_by_stream.clear();
   for (auto& pe : c->ev_pending) {
     cudaEventDestroy(pe.second.first);
     cudaEventDestroy(pe.second.second);
@@ -565,33 +567,53 @@ static xcgpu_status prep_chunks(xcgpu_plan* P) {
   return XCGPU_OK;
 }
 
+// the calling stream's FP64 slab scratch, grown to the plan's largest chunk (growth
+// waits for the stream: earlier builds on it may still read the old slabs)
+static xcgpu_status fp64_scratch(xcgpu_plan* P, double** out) {
+  Ctx* c = P->ctx;
+  DevBuf& b = c->on_stream(c->fp64_by_stream);
+  const size_t need = std::max<long>(P->chunk_max_doubles, 1) * sizeof(double);
+  if (b.p && b.bytes < need) XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "fp64 scratch"));
+  XC_TRY(b.alloc(c, need));
+  *out = b.as<double>();
+  return XCGPU_OK;
+}
+
 static xcgpu_status stage_density(xcgpu_plan* P, int nspin, const double* dP, double* rho, double* grad) {
   Ctx* c = P->ctx;
   XC_TRY(prep_chunks(P));
-  XC_TRY(c->scratch.alloc(c, std::max<long>(P->chunk_max_doubles, 1) * sizeof(double)));
+  double* scr = nullptr;
+  XC_TRY(fp64_scratch(P, &scr));
   for (size_t k = 0; k + 1 < P->chunk_bounds.size(); ++k) {
     const int b0 = P->chunk_bounds[k], b1 = P->chunk_bounds[k + 1];
     const long* so = P->w_slab.as<long>() + b0;
-    XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, c->scratch.as<double>(), 1));
-    XC_TRY(fp64_density_chunk(c, P->dev, b0, b1, so, c->scratch.as<double>(), nspin, dP, rho, grad));
+    XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, scr, 1));
+    XC_TRY(fp64_density_chunk(c, P->dev, b0, b1, so, scr, nspin, dP, rho, grad));
+  }
+  return XCGPU_OK;
+}
+
+// skip: nspin * nblocks + 1 bytes of block skip flags (written here)
+static xcgpu_status stage_adder(xcgpu_plan* P, int nspin, const double* v, const double* g, double thr,
+                                unsigned char* skip, double* F) {
+  Ctx* c = P->ctx;
+  XC_TRY(prep_chunks(P));
+  XC_TRY(launch_block_skip_flags(c, P->dev, nspin, v, g, thr, skip));
+  double* scr = nullptr;
+  XC_TRY(fp64_scratch(P, &scr));
+  for (size_t k = 0; k + 1 < P->chunk_bounds.size(); ++k) {
+    const int b0 = P->chunk_bounds[k], b1 = P->chunk_bounds[k + 1];
+    const long* so = P->w_slab.as<long>() + b0;
+    XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, scr, 1));
+    XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, so, scr, nspin, v,
+                            g, skip, F));
   }
   return XCGPU_OK;
 }
 
 static xcgpu_status stage_adder(xcgpu_plan* P, int nspin, const double* v, const double* g, double thr, double* F) {
-  Ctx* c = P->ctx;
-  XC_TRY(prep_chunks(P));
-  XC_TRY(P->w_skip.alloc(c, (size_t)nspin * P->nblocks + 1));
-  XC_TRY(launch_block_skip_flags(c, P->dev, nspin, v, g, thr, P->w_skip.as<unsigned char>()));
-  XC_TRY(c->scratch.alloc(c, std::max<long>(P->chunk_max_doubles, 1) * sizeof(double)));
-  for (size_t k = 0; k + 1 < P->chunk_bounds.size(); ++k) {
-    const int b0 = P->chunk_bounds[k], b1 = P->chunk_bounds[k + 1];
-    const long* so = P->w_slab.as<long>() + b0;
-    XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, c->scratch.as<double>(), 1));
-    XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, so,
-                            c->scratch.as<double>(), nspin, v, g, P->w_skip.as<unsigned char>(), F));
-  }
-  return XCGPU_OK;
+  XC_TRY(P->w_skip.alloc(P->ctx, (size_t)nspin * P->nblocks + 1));
+  return stage_adder(P, nspin, v, g, thr, P->w_skip.as<unsigned char>(), F);
 }
 
 template <class T>
@@ -622,7 +644,8 @@ struct BuildReq {
   double* exc_nel;
 };
 
-// work buffers of one build, allocated on first use and kept in the plan
+// work buffers kept in the plan, for the entry points that run one build at a time on
+// a plan (non-additive potentials, gradients, response kernels)
 static xcgpu_status ensure_work(xcgpu_plan* P, int nspin, bool gga, bool mixed) {
   Ctx* c = P->ctx;
   const long n = P->grid->n;
@@ -641,51 +664,97 @@ static xcgpu_status ensure_work(xcgpu_plan* P, int nspin, bool gga, bool mixed) 
   return XCGPU_OK;
 }
 
+// work buffers of one build (FuncPotential::getMatrix), 256-byte aligned slices of
+// one allocation; with base == nullptr only the size is computed
+struct BuildWork {
+  double *rho = nullptr, *grad = nullptr, *epuv = nullptr, *dfdrho = nullptr, *dfdgrad = nullptr, *partials = nullptr;
+  unsigned char *skip = nullptr, *fskip = nullptr;
+  float* psplit = nullptr;
+};
+
+static size_t layout_work(const BuildReq& r, bool mixed, uint8_t* base, BuildWork& w) {
+  const long n = r.plan->grid->n;
+  const size_t ns = r.nspin, nbf = r.plan->basis->nbf;
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> void* {
+    void* p = base ? base + off : nullptr;
+    off += (bytes + 255) & ~size_t(255);
+    return p;
+  };
+  w = BuildWork();
+  w.rho = static_cast<double*>(take(ns * n * sizeof(double)));
+  w.epuv = static_cast<double*>(take(n * sizeof(double)));
+  w.dfdrho = static_cast<double*>(take(ns * n * sizeof(double)));
+  if (xc::is_gga(r.func)) {
+    w.grad = static_cast<double*>(take(ns * 3 * n * sizeof(double)));
+    w.dfdgrad = static_cast<double*>(take(ns * 3 * n * sizeof(double)));
+  }
+  w.partials = static_cast<double*>(take(2 * ((n + 127) / 128) * sizeof(double) + 16));
+  w.skip = static_cast<unsigned char*>(take(ns * r.plan->nblocks + 1));
+  w.fskip = static_cast<unsigned char*>(take((n + kSkipBlock - 1) / kSkipBlock + 1));
+  if (mixed) w.psplit = static_cast<float*>(take(2 * ns * nbf * nbf * sizeof(float)));
+  return off;
+}
+
+// the work buffers of every request, carved from the calling stream's arena; the arena
+// grows (after the stream's earlier builds have finished with it) and never shrinks, so
+// a repeated batch allocates nothing and can be captured in a graph
+static xcgpu_status carve_work(Ctx* c, const std::vector<BuildReq>& reqs, bool mixed, std::vector<BuildWork>& out) {
+  out.resize(reqs.size());
+  size_t total = 0;
+  for (size_t i = 0; i < reqs.size(); ++i) total += layout_work(reqs[i], mixed, nullptr, out[i]);
+  DevBuf& a = c->on_stream(c->arena_by_stream);
+  if (a.p && a.bytes < total) XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "work arena"));
+  XC_TRY(a.alloc(c, total));
+  uint8_t* base = a.as<uint8_t>();
+  for (size_t i = 0; i < reqs.size(); ++i) base += layout_work(reqs[i], mixed, base, out[i]);
+  return XCGPU_OK;
+}
+
 // Whole builds (FuncPotential::getMatrix) for a list of requests, all on the context
 // stream without host synchronisation: mixed precision runs one persistent launch per
-// heavy stage over the blocks of every request.
+// heavy stage over the blocks of every request.  Plans are only read, so requests may
+// share a plan (several density matrices of one geometry in one batch).
 static xcgpu_status run_builds(Ctx* c, std::vector<BuildReq>& reqs, int precision) {
   const bool mixed = precision == XCGPU_PREC_MIXED;
-  for (auto& r : reqs) XC_TRY(ensure_work(r.plan, r.nspin, xc::is_gga(r.func), mixed));
+  std::vector<BuildWork> bw;
+  XC_TRY(carve_work(c, reqs, mixed, bw));
   int* counter = nullptr;
   XC_TRY(c->aux(&counter));
   int* err = counter + 2;
   XC_TRY(c->cuda(cudaMemsetAsync(counter, 0, 4 * sizeof(int), c->stream), "memset aux"));
   std::vector<MixedWork> work;
   // 1. rho, grad rho
-  for (auto& r : reqs) {
+  for (size_t i = 0; i < reqs.size(); ++i) {
+    const BuildReq& r = reqs[i];
+    const BuildWork& w = bw[i];
     xcgpu_plan* P = r.plan;
-    const bool gga = xc::is_gga(r.func);
-    double* grad = gga ? P->w_grad.as<double>() : nullptr;
     if (mixed) {
-      XC_TRY(mixed_split(c, r.P, P->w_psplit.as<float>(), (long)r.nspin * P->basis->nbf * P->basis->nbf));
-      work.push_back(MixedWork{&P->basis->dev, &P->dev, r.nspin, P->w_psplit.as<float>(), P->w_rho.as<double>(),
-                               grad, P->w_dfdrho.as<double>(), gga ? P->w_dfdgrad.as<double>() : nullptr,
-                               P->w_skip.as<unsigned char>(), r.V});
+      XC_TRY(mixed_split(c, r.P, w.psplit, (long)r.nspin * P->basis->nbf * P->basis->nbf));
+      work.push_back(MixedWork{&P->basis->dev, &P->dev, r.nspin, w.psplit, w.rho, w.grad, w.dfdrho, w.dfdgrad, w.skip,
+                               r.V});
     } else {
-      XC_TRY(stage_density(P, r.nspin, r.P, P->w_rho.as<double>(), grad));
+      XC_TRY(stage_density(P, r.nspin, r.P, w.rho, w.grad));
     }
   }
   if (mixed) XC_TRY(mixed_density_batch(c, work, counter, err));
   // 2. functional, E_xc and N_el, adder skip flags
-  for (auto& r : reqs) {
+  for (size_t i = 0; i < reqs.size(); ++i) {
+    const BuildReq& r = reqs[i];
+    const BuildWork& w = bw[i];
     xcgpu_plan* P = r.plan;
-    const bool gga = xc::is_gga(r.func);
     const long n = P->grid->n;
     int nparts = 0;
-    XC_TRY(launch_functional(c, r.func, r.nspin, n, kSkipBlock, P->w_rho.as<double>(),
-                             gga ? P->w_grad.as<double>() : nullptr, P->w_epuv.as<double>(),
-                             P->w_dfdrho.as<double>(), gga ? P->w_dfdgrad.as<double>() : nullptr, P->dev.w,
-                             P->w_partials.as<double>(), &nparts, P->w_fskip.as<unsigned char>()));
-    if (nparts) XC_TRY(launch_sum_partials(c, P->w_partials.as<double>(), nparts, 2, r.exc_nel));
+    XC_TRY(launch_functional(c, r.func, r.nspin, n, kSkipBlock, w.rho, w.grad, w.epuv, w.dfdrho, w.dfdgrad, P->dev.w,
+                             w.partials, &nparts, w.fskip));
+    if (nparts) XC_TRY(launch_sum_partials(c, w.partials, nparts, 2, r.exc_nel));
     else XC_TRY(c->cuda(cudaMemsetAsync(r.exc_nel, 0, 2 * sizeof(double), c->stream), "memset sums"));
     const int nbf = P->basis->nbf;
     XC_TRY(c->cuda(cudaMemsetAsync(r.V, 0, (size_t)r.nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
     if (mixed)
-      XC_TRY(launch_block_skip_flags(c, P->dev, r.nspin, P->w_dfdrho.as<double>(),
-                                     gga ? P->w_dfdgrad.as<double>() : nullptr, r.thr, P->w_skip.as<unsigned char>()));
+      XC_TRY(launch_block_skip_flags(c, P->dev, r.nspin, w.dfdrho, w.dfdgrad, r.thr, w.skip));
     else
-      XC_TRY(stage_adder(P, r.nspin, P->w_dfdrho.as<double>(), gga ? P->w_dfdgrad.as<double>() : nullptr, r.thr, r.V));
+      XC_TRY(stage_adder(P, r.nspin, w.dfdrho, w.dfdgrad, r.thr, w.skip, r.V));
   }
   // 3. Vxc (mixed: one launch for all requests)
   if (mixed) XC_TRY(mixed_adder_batch(c, work, counter + 1, err));

@@ -114,6 +114,15 @@ struct Ctx {
   std::map<cudaStream_t, std::unique_ptr<DevBuf>> aux_by_stream;
   // per-CTA basis scratch of the mixed-precision kernels, per stream
   std::map<cudaStream_t, std::unique_ptr<DevBuf>> mixed_by_stream;
+  // per stream: the work buffers of the whole builds in flight on it (one arena carved
+  // per request, so plans stay read-only and any number of requests may share one) and
+  // the FP64 basis-value slabs
+  std::map<cudaStream_t, std::unique_ptr<DevBuf>> arena_by_stream, fp64_by_stream;
+  DevBuf& on_stream(std::map<cudaStream_t, std::unique_ptr<DevBuf>>& m) {
+    auto& b = m[stream];
+    if (!b) b.reset(new DevBuf());
+    return *b;
+  }
   xcgpu_status aux(int** out) {
     auto& b = aux_by_stream[stream];
     if (!b) b.reset(new DevBuf());

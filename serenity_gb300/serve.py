@@ -44,28 +44,24 @@ def _work_bytes(npts, nbf, nspin, gga, nblocks):
 
 
 class Resident:
-    """Grid + basis of one geometry and its plan instances (one per concurrent use)."""
+    """Grid, basis and plan of one geometry.  A build only reads its plan (its work
+    buffers come from the stream's arena), so every request on the geometry, in one
+    batch or in batches in flight together, shares the one plan."""
 
     def __init__(self, ctx, w, grid=None):
         self.grid = grid if grid is not None else xcgpu.Grid.build(ctx, w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
         self.basis = xcgpu.Basis(ctx, w.shells)
-        self.plans = []
-        self.busy = set()
+        self.plans = [xcgpu.Plan(ctx, self.grid, self.basis, 128, 1e-9)]
+        self.busy = 0  # requests admitted and not yet retired
         self.ctx = ctx
         self.S = None
 
     def plan(self):
-        for i, p in enumerate(self.plans):
-            if i not in self.busy:
-                self.busy.add(i)
-                return i, p
-        p = xcgpu.Plan(self.ctx, self.grid, self.basis, 128, 1e-9)
-        self.plans.append(p)
-        self.busy.add(len(self.plans) - 1)
-        return len(self.plans) - 1, p
+        self.busy += 1
+        return 0, self.plans[0]
 
     def release(self, i):
-        self.busy.discard(i)
+        self.busy -= 1
 
 
 class Server:
@@ -82,6 +78,7 @@ class Server:
         self.grids = {}  # geometry -> grid, shared by the bases of that geometry
         self.inflight = []
         self.reserved = 0
+        self.residents_built = 0
 
     # -- resident data --------------------------------------------------------------------
     def resident(self, key, w):
@@ -93,6 +90,7 @@ class Server:
                 self.grids[gkey] = xcgpu.Grid.build(self.ctx, w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
             r = Resident(self.ctx, w, self.grids[gkey])
             self.cache[key] = r
+            self.residents_built += 1
         self.cache.move_to_end(key)
         return r
 
@@ -161,6 +159,7 @@ class Server:
         todo = collections.deque(sorted(requests, key=lambda r: r.arrival))
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0  # noqa: E731
+        built0 = self.residents_built
         sidx = 0
         completed = 0
         while todo or pending or self.inflight:
@@ -201,7 +200,8 @@ class Server:
         lat = np.array([r.latency for r in requests])
         return {"requests": len(requests), "wall_s": total, "throughput_req_s": len(requests) / total,
                 "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                "mean_ms": float(lat.mean() * 1e3), "batches": sidx, "resident_geometries": len(self.cache)}
+                "mean_ms": float(lat.mean() * 1e3), "batches": sidx, "resident_geometries": len(self.cache),
+                "residents_built_while_serving": self.residents_built - built0}
 
 
 def density_on_gpu(S_dev, nocc, seed):
@@ -226,10 +226,7 @@ def overlap_on_gpu(ctx, resident, n):
     """Overlap matrix of a resident geometry by grid integration (adder with v = 1)."""
     import torch
     if resident.S is None:
-        plan = resident.plans[0] if resident.plans else xcgpu.Plan(ctx, resident.grid, resident.basis, 128, 1e-9)
-        if not resident.plans:
-            resident.plans.append(plan)
-        S = plan.add_scalar(np.ones(resident.grid.n), block_ave_threshold=0.0, precision=xcgpu.PREC_MIXED)[0]
+        S = resident.plans[0].add_scalar(np.ones(resident.grid.n), block_ave_threshold=0.0, precision=xcgpu.PREC_MIXED)[0]
         resident.S = torch.from_numpy(np.ascontiguousarray(S)).cuda()
     return resident.S
 

@@ -53,17 +53,42 @@ def test_graph_replay_and_loop(ctx):
     b.close()
 
 
-def test_serving_results_same_alone_and_in_the_mix(ctx):
-    from serenity_gb300 import serve, xcgpu
-    server = serve.Server(ctx, hbm_budget=8 << 30, max_batch=4, nstreams=2)
+@pytest.mark.parametrize("precision", [0, 1])
+def test_requests_sharing_one_plan_in_a_batch(ctx, precision):
+    """Several density matrices of one geometry in one batch (plans are read-only; each
+    request's work buffers are its own slice of the stream's arena)."""
+    import torch
+    from serenity_gb300 import xcgpu
+    sym, xyz = wl.water_cluster(3, seed=7, jitter=0.2)
+    ws = [wl.Workload(sym, xyz, "DEF2-SVP", "PBE", 15, 30, 110, seed) for seed in (1, 2, 3)]
+    grid = xcgpu.Grid.build(ctx, ws[0].Z, ws[0].coords, n_rad=30, n_ang=110)
+    plan = xcgpu.Plan(ctx, grid, xcgpu.Basis(ctx, ws[0].shells), 128, 1e-9)
+    items = []
+    for w, func in zip(ws, ["PBE", "LDA", "PBE"]):
+        P = torch.from_numpy(np.ascontiguousarray(np.asarray(w.density()).reshape(1, w.nbf, w.nbf))).cuda()
+        items.append((plan, func, P, torch.empty_like(P), torch.empty(2, dtype=torch.float64, device="cuda")))
+    ctx.vxc_batch(items, precision, sync=True)
+    for (_, func, P, V, en), w in zip(items, ws):
+        Vs, es, ns = plan.vxc(func, np.asarray(w.density()), precision=precision)
+        e = en.cpu().numpy()
+        assert abs(e[0] - es) <= 1e-13 * max(1, abs(es))
+        assert abs(e[1] - ns) <= 1e-13 * ns
+        np.testing.assert_allclose(V.cpu().numpy().reshape(Vs.shape), Vs, rtol=0, atol=1e-12 * max(1.0, np.abs(Vs).max()))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_serving_results_same_alone_and_in_the_mix(ctx, precision):
+    from serenity_gb300 import serve
+    server = serve.Server(ctx, hbm_budget=8 << 30, precision=precision, max_batch=4, nstreams=2)
     reqs, _ = serve.make_requests(server, n=14, rate=2000.0, seed=3, max_waters=6, n_rad=30, n_ang=110)
     stats = server.run(reqs)
     assert stats["requests"] == 14 and stats["batches"] >= 2
+    assert stats["residents_built_while_serving"] == 0
     for rq in reqs:
         rq_plan = server.cache[rq.key].plans[0]
         V_mix = rq.V_dev.cpu().numpy()
         e_mix = rq.en_dev.cpu().numpy()
-        V_alone, e_alone, n_alone = rq_plan.vxc(rq.func, rq.P_dev, precision=xcgpu.PREC_MIXED,
+        V_alone, e_alone, n_alone = rq_plan.vxc(rq.func, rq.P_dev, precision=precision,
                                                 out=rq.V_dev.clone())
         assert abs(e_mix[0] - e_alone) <= 1e-12 * max(1, abs(e_alone))
         assert abs(e_mix[1] - n_alone) <= 1e-12 * n_alone
