@@ -763,25 +763,6 @@ __global__ void mirror_upper_kernel(double* V, int nbf, int nspin) {
   M[e] = M[(long)i * nbf + j];
 }
 
-// V <- V + V^T (per spin), turning sum_b D_b into sum_b (D_b + D_b^T)
-__global__ void symmetrize_kernel(double* V, int nbf, int nspin) {
-  const long n2 = (long)nbf * nbf;
-  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= n2 * nspin) return;
-  const int s = (int)(idx / n2);
-  const long e = idx % n2;
-  const int i = (int)(e % nbf), j = (int)(e / nbf);
-  if (i > j) return;
-  double* M = V + (long)s * n2;
-  if (i == j) {
-    M[e] *= 2.0;
-  } else {
-    const double t = M[(long)j * nbf + i] + M[(long)i * nbf + j];
-    M[(long)j * nbf + i] = t;
-    M[(long)i * nbf + j] = t;
-  }
-}
-
 static size_t density_smem() { return 2 * kStageBytes + 128 * (kNT + 1) * sizeof(float) + 1024; }
 static size_t adder_smem() { return kAdderStages * kStageBytes + 128 * kDsLd * sizeof(float) + 1024; }
 
