@@ -335,12 +335,18 @@ xcgpu_status xcgpu_basis_create(xcgpu_ctx* c, const xcgpu_shell* shells, uint32_
   if (!st) st = upload(c, B->d_cnorm, cnorm.data(), cnorm.size());
   if (!st) st = upload(c, B->d_toff, toff.data(), toff.size());
   if (!st) st = upload(c, B->d_coff, coff.data(), coff.size());
-  std::vector<float> prim2;
+  // FP32 pairs carry the exponents and coefficients to ~2^-48: a single FP32 rounding
+  // of them is the same relative error at every grid point (all atoms of an element
+  // share it), which would bias the density by a few 1e-8
+  std::vector<float> prim4;
   for (size_t i = 0; i < B->alpha.size(); ++i) {
-    prim2.push_back((float)B->alpha[i]);
-    prim2.push_back((float)B->coef[i]);
+    const float ah = (float)B->alpha[i], ch = (float)B->coef[i];
+    prim4.push_back(ah);
+    prim4.push_back(ch);
+    prim4.push_back((float)(B->alpha[i] - (double)ah));
+    prim4.push_back((float)(B->coef[i] - (double)ch));
   }
-  if (!st) st = upload(c, B->d_prim2, prim2.data(), prim2.size());
+  if (!st) st = upload(c, B->d_prim4, prim4.data(), prim4.size());
   if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "basis upload");
   if (st) {
     delete B;
@@ -362,7 +368,7 @@ xcgpu_status xcgpu_basis_create(xcgpu_ctx* c, const xcgpu_shell* shells, uint32_
   d.cnorm = B->d_cnorm.as<double>();
   d.trans_off = B->d_toff.as<int>();
   d.cnorm_off = B->d_coff.as<int>();
-  d.prim2 = B->d_prim2.as<float2>();
+  d.prim4 = B->d_prim4.as<float4>();
   *out = B;
   return XCGPU_OK;
 }
@@ -660,7 +666,7 @@ static xcgpu_status ensure_work(xcgpu_plan* P, int nspin, bool gga, bool mixed) 
   XC_TRY(P->w_partials.alloc(c, 2 * ((n + 127) / 128) * sizeof(double) + 16));
   XC_TRY(P->w_skip.alloc(c, (size_t)nspin * P->nblocks + 1));
   XC_TRY(P->w_fskip.alloc(c, (size_t)(n + kSkipBlock - 1) / kSkipBlock + 1));
-  if (mixed) XC_TRY(P->w_psplit.alloc(c, 2 * (size_t)nspin * nbf * nbf * sizeof(float)));
+  if (mixed) XC_TRY(P->w_psplit.alloc(c, psplit_bytes(nspin, nbf)));
   return XCGPU_OK;
 }
 
@@ -692,7 +698,7 @@ static size_t layout_work(const BuildReq& r, bool mixed, uint8_t* base, BuildWor
   w.partials = static_cast<double*>(take(2 * ((n + 127) / 128) * sizeof(double) + 16));
   w.skip = static_cast<unsigned char*>(take(ns * r.plan->nblocks + 1));
   w.fskip = static_cast<unsigned char*>(take((n + kSkipBlock - 1) / kSkipBlock + 1));
-  if (mixed) w.psplit = static_cast<float*>(take(2 * ns * nbf * nbf * sizeof(float)));
+  if (mixed) w.psplit = static_cast<float*>(take(psplit_bytes((int)ns, (int)nbf)));
   return off;
 }
 
@@ -730,7 +736,7 @@ static xcgpu_status run_builds(Ctx* c, std::vector<BuildReq>& reqs, int precisio
     const BuildWork& w = bw[i];
     xcgpu_plan* P = r.plan;
     if (mixed) {
-      XC_TRY(mixed_split(c, r.P, w.psplit, (long)r.nspin * P->basis->nbf * P->basis->nbf));
+      XC_TRY(mixed_split(c, r.P, r.nspin, P->basis->nbf, w.psplit));
       work.push_back(MixedWork{&P->basis->dev, &P->dev, r.nspin, w.psplit, w.rho, w.grad, w.dfdrho, w.dfdgrad, w.skip,
                                r.V});
     } else {
@@ -790,8 +796,8 @@ xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* r
   if (precision == XCGPU_PREC_MIXED) {
     XC_TRY(P->w_aux.alloc(c, 4 * sizeof(int)));
     XC_TRY(c->cuda(cudaMemsetAsync(P->w_aux.p, 0, 4 * sizeof(int), c->stream), "memset aux"));
-    XC_TRY(P->w_psplit.alloc(c, 2 * (size_t)nspin * nbf * nbf * sizeof(float)));
-    XC_TRY(mixed_split(c, Pd, P->w_psplit.as<float>(), (long)nspin * nbf * nbf));
+    XC_TRY(P->w_psplit.alloc(c, psplit_bytes(nspin, nbf)));
+    XC_TRY(mixed_split(c, Pd, nspin, nbf, P->w_psplit.as<float>()));
     std::vector<MixedWork> work(1);
     work[0] = MixedWork{&P->basis->dev, &P->dev, nspin, P->w_psplit.as<float>(), r, gr, nullptr, nullptr, nullptr,
                         nullptr};
@@ -1003,7 +1009,7 @@ xcgpu_status xcgpu_nadd_vxc(xcgpu_plan* A, xcgpu_plan* const* env, uint32_t n_en
     std::vector<MixedWork> work;
     for (size_t i = 0; i < plans.size(); ++i) {
       xcgpu_plan* q = plans[i];
-      XC_TRY(mixed_split(c, Pd[i], q->w_psplit.as<float>(), (long)nspin * q->basis->nbf * q->basis->nbf));
+      XC_TRY(mixed_split(c, Pd[i], nspin, q->basis->nbf, q->w_psplit.as<float>()));
       work.push_back(MixedWork{&q->basis->dev, &q->dev, nspin, q->w_psplit.as<float>(), q->w_rho.as<double>(),
                                gga ? q->w_grad.as<double>() : nullptr, nullptr, nullptr, nullptr, nullptr});
     }
@@ -1201,7 +1207,7 @@ xcgpu_status xcgpu_lr_kernel(xcgpu_plan* P, int func, const double* P0, uint32_t
   // density of a symmetric matrix M into (rho, grad)
   auto density = [&](const double* M, double* rho, double* grad) -> xcgpu_status {
     if (!mixed) return stage_density(P, 1, M, rho, grad);
-    xcgpu_status st = mixed_split(c, M, P->w_psplit.as<float>(), (long)nn);
+    xcgpu_status st = mixed_split(c, M, 1, P->basis->nbf, P->w_psplit.as<float>());
     if (st) return st;
     std::vector<MixedWork> work(1);
     work[0] = MixedWork{&P->basis->dev, &P->dev, 1, P->w_psplit.as<float>(), rho, grad, nullptr, nullptr, nullptr, nullptr};
@@ -1291,7 +1297,7 @@ xcgpu_status xcgpu_nadd_vxc_all(xcgpu_plan* const* plans, uint32_t n_sub, int fu
     xcgpu_plan* q = plans[i];
     double* grad = gga ? q->w_grad.as<double>() : nullptr;
     if (mixed) {
-      XC_TRY(mixed_split(c, Pd[i], q->w_psplit.as<float>(), (long)nspin * q->basis->nbf * q->basis->nbf));
+      XC_TRY(mixed_split(c, Pd[i], nspin, q->basis->nbf, q->w_psplit.as<float>()));
       work.push_back(MixedWork{&q->basis->dev, &q->dev, nspin, q->w_psplit.as<float>(), q->w_rho.as<double>(), grad,
                                q->n_dfdrho.as<double>(), gga ? q->n_dfdgrad.as<double>() : nullptr,
                                q->w_skip.as<unsigned char>(), Vd[i]});

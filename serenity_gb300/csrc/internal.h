@@ -34,7 +34,7 @@ struct DevBasis {
   const double* cnorm = nullptr;   // per l, ncart(l) Cartesian factors
   const int* trans_off = nullptr;  // [kMaxL+1] offsets into trans
   const int* cnorm_off = nullptr;  // [kMaxL+1] offsets into cnorm
-  const float2* prim2 = nullptr;   // (alpha, normalised coef) in FP32 for the FP32 kernels
+  const float4* prim4 = nullptr;   // FP32 kernels: (alpha_hi, coef_hi, alpha_lo, coef_lo), x = x_hi + x_lo
 };
 
 // Per (block, active shell) record used by the FP32 kernels (32 bytes).  The centre
@@ -45,7 +45,7 @@ struct __align__(16) ShellRec {
   float ah[3];
   float al[3];
   int info;
-  int prim0;  // offset of the shell's (alpha, coef) pairs in DevBasis::prim2
+  int prim0;  // offset of the shell's primitives in DevBasis::prim4
 };
 
 // Device-side block table of a plan.
@@ -182,7 +182,7 @@ struct xcgpu_basis {
   std::vector<int> l, pure, nprim, prim_off, first;
   std::vector<double> center, alpha, coef;
   xcgpu::DevBuf d_l, d_pure, d_nprim, d_prim_off, d_first, d_center, d_alpha, d_coef, d_trans, d_cnorm, d_toff, d_coff,
-      d_prim2;
+      d_prim4;
   xcgpu::DevBasis dev;
 };
 
@@ -250,7 +250,7 @@ struct MixedWork {
   const DevBasis* B;
   const DevPlan* P;
   int nspin;
-  float* Psplit;  // 2 * nspin * nbf^2 floats: TF32 (hi, lo) pairs, interleaved
+  float* Psplit;  // psplit_bytes(nspin, nbf): the density matrices' fixed-point slices and column scales
   double* rho;
   double* grad;
   const double* v;
@@ -259,7 +259,10 @@ struct MixedWork {
   double* V;
 };
 xcgpu_status mixed_init(Ctx* c);
-xcgpu_status mixed_split(Ctx* c, const double* Pm, float* Psplit, long n);
+// bytes of the density kernel's form of nspin density matrices: 8 bytes of FP16
+// slices per element, then one FP32 scale per column
+inline size_t psplit_bytes(int nspin, int nbf) { return (size_t)nspin * nbf * nbf * 8 + (size_t)nspin * nbf * 4; }
+xcgpu_status mixed_split(Ctx* c, const double* Pm, int nspin, int nbf, float* Psplit);
 xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
 xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
 

@@ -15,6 +15,7 @@
 // global counter); one elected thread issues the MMAs; completion is tracked with
 // mbarriers through tcgen05.commit; every wait is bounded in time and reports a
 // timeout through the error word instead of hanging.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -22,6 +23,7 @@
 #include <vector>
 
 #include "basis_eval.cuh"
+#include "exp_tang.cuh"
 #include "internal.h"
 #include "tcgen05.cuh"
 
@@ -55,7 +57,7 @@ __device__ __forceinline__ int rec_f0(int info) { return info >> 14; }
 // Evaluate one shell record at a point in FP32; Emit(f, value, dx, dy, dz).
 // Negligible shells (|R| below the radial threshold) emit zeros.
 template <int DERIV, class Emit>
-__device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float2* __restrict__ prim2, const Pt& q,
+__device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __restrict__ prim4, const Pt& q,
                                              float expthr, float thr, Emit&& emit) {
   const float x = (q.h[0] - r.ah[0]) + (q.l[0] - r.al[0]);
   const float y = (q.h[1] - r.ah[1]) + (q.l[1] - r.al[1]);
@@ -64,13 +66,14 @@ __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float2* __
   const int np = rec_nprim(r.info);
   float Rv = 0.f, dR = 0.f;
   for (int i = 0; i < np; ++i) {
-    const float2 ac = __ldg(prim2 + r.prim0 + i);
-    const float t = ac.x * r2;
+    const float4 ac = __ldg(prim4 + r.prim0 + i);  // alpha = x + z, coef = y + w
+    const float t = fmaf(ac.z, r2, __fmul_rn(ac.x, r2));
     if (t < expthr) {
       // explicit roundings: R comes out bit-identical whether or not dR is formed
-      const float e = __fmul_rn(ac.y, expf(-t));
+      const float E = exp_tang(-t);
+      const float e = fmaf(ac.w, E, __fmul_rn(ac.y, E));
       Rv = __fadd_rn(Rv, e);
-      if (DERIV >= 1) dR = fmaf(-2.f * ac.x, e, dR);
+      if (DERIV >= 1) dR = fmaf(-2.f * ac.z, e, fmaf(-2.f * ac.x, e, dR));
     }
   }
   const int l = rec_l(r.info);
@@ -95,13 +98,6 @@ __device__ __forceinline__ ShellRec load_rec(const ShellRec* p) {
   r.info = __float_as_int(b.z);
   r.prim0 = __float_as_int(b.w);
   return r;
-}
-
-__device__ __forceinline__ void st_tf32_pair(uint8_t* hi, uint8_t* lo, uint32_t off, float v) {
-  uint32_t h, l;
-  tc::split_tf32(v, h, l);
-  *reinterpret_cast<uint32_t*>(hi + off) = h;
-  *reinterpret_cast<uint32_t*>(lo + off) = l;
 }
 
 __device__ __forceinline__ bool wait_or_abort(uint64_t* mbar, uint32_t parity, int* err) {
@@ -146,20 +142,6 @@ __device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t ah, uint32_t
   }
 }
 
-// add (or store) TMEM columns [32 (warp >> 2), +32) of this warp's 32 lanes into S rows
-__device__ __forceinline__ void drain32(uint32_t tmem_cols, int warp, int lane, float* S, int ld, int N, bool store) {
-  const int row = 32 * (warp & 3) + lane, c = 32 * (warp >> 2);
-  if (c >= N) return;  // warp-uniform
-  float v[32];
-  tc::tmem_ld32(tmem_cols + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c, v);
-#pragma unroll
-  for (int i = 0; i < 32; ++i)
-    if (c + i < N) {
-      float* d = S + row * ld + c + i;
-      *d = store ? v[i] : *d + v[i];
-    }
-}
-
 // add (or store) this warp's 32 lanes x 32 columns [32 (warp >> 2), +32) of a TMEM
 // accumulator into registers
 __device__ __forceinline__ void drain_regs(uint32_t tmem_cols, int warp, float* acc, bool store, int N) {
@@ -184,7 +166,8 @@ struct MxItem {
   DevBasis B;
   DevPlan P;
   int nspin;
-  const float2* Psplit;  // TF32 split (hi, lo) of the density matrices, interleaved (density kernel)
+  const uint2* Psl;  // density kernel: FP16 slices (s0 | s1 << 16, s2) of P, per column scaled
+  const float* Pcs;  // by the column's power-of-two scale Pcs[j] (fixed_slices)
   double* rho;  // outputs of the density kernel
   double* grad;
   const double* v;  // inputs of the adder kernel
@@ -221,15 +204,78 @@ __device__ __forceinline__ const MxItem& locate(const MxBatch& bt, int gb, int& 
 }
 
 // =====================================================================================
-// density
+// density, with the leading products accumulated exactly
+//   The tensor core's FP32 accumulation truncates: summing positive products it loses
+//   up to an ulp per accumulation step, always towards zero, which shows as a systematic
+//   density deficit (about -6e-8 relative with 3xTF32 operands).  Here both operands are
+//   fixed point: each row of A = Phi (one point) and each column of B = P (one function
+//   nu) is scaled by a power of two that brings its largest element below 128 and cut
+//   into three 8-bit slices (fixed_slices).  Products of leading slices are integers
+//   below 2^14, so their sums over up to 1024 functions are exact in FP32 whatever the
+//   rounding of the adder tree; the remaining five slice products (at most 2^-7 of the
+//   leading ones, with signs uncorrelated with X) go to a second accumulator.  The
+//   slices are stored pre-scaled as FP16 (exact) and multiplied with kind::f16 MMAs.
 //   1. every active shell of the block is evaluated once (value and, for GGA, gradient)
-//      into the CTA's scratch, FP32, [component][function][128 points];
-//   2. per pass of <= 128 functions nu: X = Phi P_b over K chunks of 32 functions mu,
-//      A = Phi (points x mu) split from the scratch, B = P_b (nu x mu) gathered from the
-//      pre-split density matrix (rows of P_b by symmetry, one warp per row);
-//   3. rho_p += sum_nu X_p,nu phi_nu(p), grad rho_p += 2 sum_nu X_p,nu grad phi_nu(p),
-//      reading phi and grad phi back from the scratch.
+//      into the CTA's scratch, FP32, [component][function][128 points], with the
+//      largest |phi| of each point;
+//   2. per pass of <= 128 functions nu: X = Phi P_b over K chunks of 64 functions mu,
+//      A sliced from the scratch, B gathered from the pre-sliced density matrix; the two
+//      accumulators are read after every window of up to kWinChunks chunks;
+//   3. rho_p += sum_nu X_p,nu phi_nu(p), grad rho_p += 2 sum_nu X_p,nu grad phi_nu(p).
 // =====================================================================================
+constexpr uint32_t kDStageBytes = 6 * kTileA;  // A slices 0-2, B slices 0-2 (64 FP16 wide)
+constexpr int kWinChunks = 8;                  // 512 functions: |sum of leading products| < 2^23
+constexpr uint32_t kColsAcc0 = 0, kColsAccR = 128;
+
+// v in (-128, 128) -> s0 + s1 / 2^8 + s2 / 2^16, s_i integers in [-128, 128], as FP16
+// (s0, s1 / 2^8, s2 / 2^16); every step is exact (each remainder is a multiple of the
+// unit of v) except the rounding of s2, so |v - sum| <= 2^-17
+__device__ __forceinline__ void fixed_slices(float v, uint16_t& h0, uint16_t& h1, uint16_t& h2) {
+  const float s0 = rintf(v);
+  const float r1 = __fmul_rn(__fsub_rn(v, s0), 256.f);
+  const float s1 = rintf(r1);
+  const float s2 = rintf(__fmul_rn(__fsub_rn(r1, s1), 256.f));
+  h0 = __half_as_ushort(__float2half_rn(s0));
+  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, 1.f / 256.f)));
+  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, 1.f / 65536.f)));
+}
+
+// power-of-two scale of a row or column with largest magnitude m: m * inv < 128;
+// rows below 2^-100 count as zero
+__device__ __forceinline__ void fixed_scale(float m, float& scale, float& inv) {
+  int e = 0;
+  frexpf(m, &e);  // m = f 2^e, 0.5 <= f < 1
+  if (!(m > 0.f) || e < -100) {
+    scale = inv = 0.f;
+    return;
+  }
+  scale = ldexpf(1.f, e - 7);
+  inv = ldexpf(1.f, 7 - e);
+}
+
+// the six slice products of one 64-wide K chunk: leading x leading into acc0, the
+// rest into accR
+__device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t stage, int N, bool first) {
+  const uint32_t idesc = tc::idesc_f16(128, N);
+  uint64_t a[3], b[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    a[i] = tc::smem_desc_sw128(stage + i * kTileA);
+    b[i] = tc::smem_desc_sw128(stage + (3 + i) * kTileA);
+  }
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {  // 16 FP16 (32 bytes) per MMA
+    const uint64_t o = 2u * ks;
+    const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+    tc::mma_f16(tmem + kColsAcc0, a[0] + o, b[0] + o, idesc, acc);
+    tc::mma_f16(tmem + kColsAccR, a[0] + o, b[1] + o, idesc, acc);
+    tc::mma_f16(tmem + kColsAccR, a[1] + o, b[0] + o, idesc, 1u);
+    tc::mma_f16(tmem + kColsAccR, a[0] + o, b[2] + o, idesc, 1u);
+    tc::mma_f16(tmem + kColsAccR, a[1] + o, b[1] + o, idesc, 1u);
+    tc::mma_f16(tmem + kColsAccR, a[2] + o, b[0] + o, idesc, 1u);
+  }
+}
+
 template <int DERIV>
 __global__ void __launch_bounds__(kT, 1)
     mx_density_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
@@ -238,13 +284,14 @@ __global__ void __launch_bounds__(kT, 1)
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort;
   __shared__ double s_part[4][kQ - 1][128];
+  __shared__ unsigned s_amax[128];  // per point: largest |phi| (FP32 bits)
+  __shared__ float s_bscale[kNT];   // per function nu of the pass: scale of its column of P
   const uint32_t base_s = tc::smem_u32(smem_raw);
   uint8_t* sm = smem_raw + ((1024 - (base_s & 1023)) & 1023);
-  float* Xs = reinterpret_cast<float*>(sm + 2 * kStageBytes);  // [128][kNT + 1]
-  const int ld = kNT + 1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int p = tid & 127, quarter = tid >> 7;  // point, and which of its kQ threads
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
+  const int p = tid & 127, quarter = tid >> 7;  // point (TMEM lane), and which of its kQ threads
+  const int c0 = 32 * quarter;                  // this thread's 32 accumulator columns
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
   if (tid == 0) {
     tc::mbar_init(&mbar[0], 1);
     tc::mbar_init(&mbar[1], 1);
@@ -255,11 +302,14 @@ __global__ void __launch_bounds__(kT, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
+  const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
   uint32_t phase[2] = {0, 0};
-  int outstanding = -1;  // stage whose commit has not been waited for (-1: none)
+  bool pend[2] = {false, false};  // a commit on the stage's barrier not yet waited for
+  int gc = 0;                     // chunks issued by this CTA (stage = gc & 1)
   float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
 
   for (;;) {
+    if (tid < 128) s_amax[tid] = 0u;
     __syncthreads();
     if (tid == 0) s_block = atomicAdd(counter, 1);
     __syncthreads();
@@ -283,11 +333,12 @@ __global__ void __launch_bounds__(kT, 1)
     }
     const bool live = p < npts;
     const long cs = (long)nact * 128;  // component stride of the scratch
-    // ---- 1. basis values (and gradients) of the block ----
+    // ---- 1. basis values (and gradients) of the block, largest |phi| per point ----
     {
       const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
       const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
       float* const col = my + p;
+      float vmax = 0.f;
       ShellRec next;
       if (s0 + quarter < s1) next = load_rec(P.rec + s0 + quarter);
       for (int si = s0 + quarter; si < s1; si += kQ) {
@@ -297,6 +348,7 @@ __global__ void __launch_bounds__(kT, 1)
         auto put = [&](int f, float v, float dx, float dy, float dz) {
           float* t = t0 + f * 128;
           t[0] = v;
+          vmax = fmaxf(vmax, fabsf(v));
           if (DERIV) {
             t[cs] = dx;
             t[2 * cs] = dy;
@@ -304,123 +356,145 @@ __global__ void __launch_bounds__(kT, 1)
           }
         };
         if (live) {
-          shell_rec_at<DERIV>(r, B.prim2, pt, expthr, thr, put);
+          shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, put);
         } else {
           const int nf = rec_nf(r.info);
           for (int f = 0; f < nf; ++f) put(f, 0.f, 0.f, 0.f, 0.f);
         }
       }
+      atomicMax(&s_amax[p], __float_as_uint(vmax));  // non-negative floats order as integers
     }
     __syncthreads();
+    float sa, inva;  // this point's row scale
+    fixed_scale(__uint_as_float(s_amax[p]), sa, inva);
+    const int nkc = (nact + 63) / 64;
     for (int s = 0; s < nspin; ++s) {
-      const float2* __restrict__ Pspin = I.Psplit + (long)s * nbf * nbf;
+      const uint2* __restrict__ Psl = I.Psl + (long)s * nbf * nbf;
+      const float* __restrict__ Pcs = I.Pcs + (long)s * nbf;
       double r_acc = 0.0, g_acc[3] = {0.0, 0.0, 0.0};
       for (int nu0 = 0; nu0 < nact; nu0 += kNT) {
         const int nnu = min(kNT, nact - nu0);
         const int N = (nnu + 15) & ~15;
-        const int nkc = (nact + 31) / 32;
+        if (tid < nnu) s_bscale[tid] = __ldg(Pcs + __ldg(fn + nu0 + tid));
         for (int kc = 0; kc < nkc; ++kc) {
-          const int st = kc & 1;
-          uint8_t* Ahi = sm + st * kStageBytes;
-          uint8_t* Alo = Ahi + kTileA;
-          uint8_t* Bhi = Alo + kTileA;
-          uint8_t* Blo = Bhi + kTileA;
-          const int mu0 = kc * 32;
-          // ---- A: Phi[p][mu0 + 4q .. + 4) for this thread's 2 quads q, 16-byte stores ----
-#pragma unroll
-          for (int qq = 0; qq < 2; ++qq) {
-            const int q = 2 * quarter + qq;
-            uint32_t h[4], l[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const int mu = mu0 + 4 * q + e;
-              tc::split_tf32(mu < nact ? my[(long)mu * 128 + p] : 0.f, h[e], l[e]);
-            }
-            const uint32_t off = (uint32_t)(p * 128 + ((q ^ (p & 7)) << 4));
-            *reinterpret_cast<uint4*>(Ahi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-            *reinterpret_cast<uint4*>(Alo + off) = make_uint4(l[0], l[1], l[2], l[3]);
-          }
-          // ---- B: P_b[nu][mu0 + lane] = P[fn[mu]][fn[nu]] (symmetric P), one warp per row ----
-          {
-            const int mu = mu0 + lane;
-            const bool muok = mu < nact;
-            const long cmu = muok ? (long)__ldg(fn + mu) : 0;
-#pragma unroll 8
-            for (int row = warp; row < N; row += kWarps) {
-              float2 hl = make_float2(0.f, 0.f);
-              if (muok && row < nnu) hl = __ldg(Pspin + (long)__ldg(fn + nu0 + row) * nbf + cmu);
-              const uint32_t off = tc::swz_offset(row, lane);
-              *reinterpret_cast<float*>(Bhi + off) = hl.x;
-              *reinterpret_cast<float*>(Blo + off) = hl.y;
-            }
-          }
-          tc::fence_async_smem();
-          // ---- drain the previous chunk's hi*hi accumulator ----
-          if (kc > 0) {
-            const int pst = (kc - 1) & 1;
-            const bool ok = wait_or_abort(&mbar[pst], phase[pst], err);
-            phase[pst] ^= 1;
-            outstanding = -1;
+          const int st = gc & 1;
+          if (pend[st]) {  // the MMAs of two chunks ago still read this stage
+            const bool ok = wait_or_abort(&mbar[st], phase[st], err);
+            phase[st] ^= 1;
+            pend[st] = false;
             if (__syncthreads_or(!ok)) {
               if (tid == 0) s_abort = 1;
               goto done;
             }
-            tc::fence_after_sync();
-            drain32(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Xs, ld, N, kc == 1);
-            tc::fence_before_sync();
           }
+          uint8_t* const stage = sm + st * kDStageBytes;
+          const int mu0 = kc * 64;
+          // ---- A: row p, 16-byte chunks j = 2 quarter, 2 quarter + 1 (8 functions each) ----
+#pragma unroll
+          for (int jj = 0; jj < 2; ++jj) {
+            const int j = 2 * quarter + jj;
+            uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+            for (int e = 0; e < 8; e += 2) {
+              uint16_t a0, a1, a2, b0, b1, b2;
+              const int mu = mu0 + 8 * j + e;
+              fixed_slices(mu < nact ? __fmul_rn(my[(long)mu * 128 + p], inva) : 0.f, a0, a1, a2);
+              fixed_slices(mu + 1 < nact ? __fmul_rn(my[(long)(mu + 1) * 128 + p], inva) : 0.f, b0, b1, b2);
+              w0[e >> 1] = (uint32_t)a0 | ((uint32_t)b0 << 16);
+              w1[e >> 1] = (uint32_t)a1 | ((uint32_t)b1 << 16);
+              w2[e >> 1] = (uint32_t)a2 | ((uint32_t)b2 << 16);
+            }
+            const uint32_t off = (uint32_t)(p * 128 + ((j ^ (p & 7)) << 4));
+            *reinterpret_cast<uint4*>(stage + off) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+            *reinterpret_cast<uint4*>(stage + kTileA + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+            *reinterpret_cast<uint4*>(stage + 2 * kTileA + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+          }
+          // ---- B: row nu, elements mu0 + 2 lane, + 1: P[fn[mu]][fn[nu]] (symmetric P) ----
+          {
+            const int k0 = 2 * lane;
+            const int muA = mu0 + k0, muB = muA + 1;
+            const long cA = muA < nact ? (long)__ldg(fn + muA) : -1;
+            const long cB = muB < nact ? (long)__ldg(fn + muB) : -1;
+#pragma unroll 4
+            for (int row = warp; row < N; row += kWarps) {
+              uint2 ea = make_uint2(0u, 0u), eb = make_uint2(0u, 0u);
+              if (row < nnu) {
+                const uint2* prow = Psl + (long)__ldg(fn + nu0 + row) * nbf;
+                if (cA >= 0) ea = __ldg(prow + cA);
+                if (cB >= 0) eb = __ldg(prow + cB);
+              }
+              const uint32_t off = tc::swz_offset_h(row, k0);
+              *reinterpret_cast<uint32_t*>(stage + 3 * kTileA + off) = (ea.x & 0xFFFFu) | (eb.x << 16);
+              *reinterpret_cast<uint32_t*>(stage + 4 * kTileA + off) = (ea.x >> 16) | (eb.x & 0xFFFF0000u);
+              *reinterpret_cast<uint32_t*>(stage + 5 * kTileA + off) = (ea.y & 0xFFFFu) | (eb.y << 16);
+            }
+          }
+          tc::fence_async_smem();
           __syncthreads();
+          const bool wfirst = (kc % kWinChunks) == 0;
           if (tid == 0) {
             tc::fence_after_sync();
-            issue_chunk(tmem, tc::smem_u32(Ahi), tc::smem_u32(Alo), tc::smem_u32(Bhi), tc::smem_u32(Blo), N,
-                        st ? kColsHH1 : kColsHH0, kColsX0, kc == 0);
+            issue_fixed_chunk(tmem, tc::smem_u32(stage), N, wfirst);
             tc::mma_commit(&mbar[st]);
           }
-          outstanding = st;
-        }
-        // ---- last chunk: drain hh, add the cross accumulator ----
-        {
-          const int pst = (nkc - 1) & 1;
-          const bool ok = wait_or_abort(&mbar[pst], phase[pst], err);
-          phase[pst] ^= 1;
-          outstanding = -1;
+          pend[st] = true;
+          ++gc;
+          if ((kc % kWinChunks) != kWinChunks - 1 && kc != nkc - 1) continue;
+          // ---- end of a window: wait for its MMAs (older stage first), read X ----
+          bool ok = true;
+#pragma unroll
+          for (int q = 1; q >= 0; --q) {
+            const int sq = (st + q) & 1;  // q = 1: the other (older) stage
+            if (pend[sq]) {
+              ok = wait_or_abort(&mbar[sq], phase[sq], err) && ok;
+              phase[sq] ^= 1;
+              pend[sq] = false;
+            }
+          }
           if (__syncthreads_or(!ok)) {
             if (tid == 0) s_abort = 1;
             goto done;
           }
           tc::fence_after_sync();
-          drain32(tmem + (pst ? kColsHH1 : kColsHH0), warp, lane, Xs, ld, N, nkc == 1);
-          drain32(tmem + kColsX0, warp, lane, Xs, ld, N, false);
-          tc::fence_before_sync();
-          __syncthreads();
-        }
-        // ---- rho_p += sum_nu X_p,nu phi_nu(p) over this thread's 32 columns, FP32 runs of 8 ----
-        if (live) {
-          const float* xs = Xs + p * ld;
-          const float* t = my + (long)nu0 * 128 + p;
-          const int c1 = min(nnu, 32 * quarter + 32);
-          for (int c8 = 32 * quarter; c8 < c1; c8 += 8) {
-            float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-            const int ce = min(c1, c8 + 8);
-            for (int c = c8; c < ce; ++c) {
-              const float xv = xs[c];
-              const float* tc_ = t + (long)c * 128;
-              rr = fmaf(xv, tc_[0], rr);
-              if (DERIV) {
-                gx = fmaf(xv, tc_[cs], gx);
-                gy = fmaf(xv, tc_[2 * cs], gy);
-                gz = fmaf(xv, tc_[3 * cs], gz);
+          if (c0 < N) {  // warp-uniform
+            const float* t = my + (long)nu0 * 128 + p;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int cb = c0 + 16 * h;
+              float a0[16], ar[16];
+              tc::tmem_ld16(tmem + trow + kColsAcc0 + cb, a0);
+              tc::tmem_ld16(tmem + trow + kColsAccR + cb, ar);
+              if (live) {
+#pragma unroll
+                for (int g8 = 0; g8 < 16; g8 += 8) {
+                  float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+                  for (int c = g8; c < g8 + 8; ++c) {
+                    const int col = cb + c;
+                    if (col < nnu) {
+                      const float xv = __fmul_rn(__fadd_rn(a0[c], ar[c]), __fmul_rn(sa, s_bscale[col]));
+                      const float* tc_ = t + (long)col * 128;
+                      rr = fmaf(xv, tc_[0], rr);
+                      if (DERIV) {
+                        gx = fmaf(xv, tc_[cs], gx);
+                        gy = fmaf(xv, tc_[2 * cs], gy);
+                        gz = fmaf(xv, tc_[3 * cs], gz);
+                      }
+                    }
+                  }
+                  r_acc += (double)rr;
+                  if (DERIV) {
+                    g_acc[0] += (double)gx;
+                    g_acc[1] += (double)gy;
+                    g_acc[2] += (double)gz;
+                  }
+                }
               }
             }
-            r_acc += (double)rr;
-            if (DERIV) {
-              g_acc[0] += (double)gx;
-              g_acc[1] += (double)gy;
-              g_acc[2] += (double)gz;
-            }
           }
+          tc::fence_before_sync();
+          __syncthreads();  // the accumulators and s_bscale are reused
         }
-        __syncthreads();  // Xs and the stages are reused by the next pass
       }
       // combine the kQ partial sums of each point
       if (quarter > 0) {
@@ -449,10 +523,12 @@ __global__ void __launch_bounds__(kT, 1)
     }
   }
 done:
-  if (outstanding >= 0) wait_or_abort(&mbar[outstanding], phase[outstanding], err);
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    if (pend[q]) wait_or_abort(&mbar[q], phase[q], err);
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+  if (warp == 0) tc::tmem_dealloc(tmem, 256);
 }
 
 // =====================================================================================
@@ -578,7 +654,7 @@ __global__ void __launch_bounds__(kT, 1)
             }
           };
           if (live) {
-            shell_rec_at<DERIV>(r, B.prim2, pt, expthr, thr, put);
+            shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, put);
           } else {
             const int nf = rec_nf(r.info);
             for (int f = 0; f < nf; ++f) put(f, 0.f, 0.f, 0.f, 0.f);
@@ -741,13 +817,39 @@ done:
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
-// TF32 split of the density matrices (hi = TF32(P), lo = TF32(P - hi)), once per build
-__global__ void split_p_kernel(const double* __restrict__ P, float2* __restrict__ out, long n) {
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  uint32_t h, l;
-  tc::split_tf32(P[i], h, l);
-  out[i] = make_float2(__uint_as_float(h), __uint_as_float(l));
+// Fixed-point slices of the density matrices, once per build: one CTA per (spin,
+// column j) finds the column's largest |P_ij|, its power-of-two scale (the largest
+// scaled element below 128) and the three FP16 slices of every scaled element (taken
+// from the FP64 value, so P enters to 2^-24 of its column maximum).
+__global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__ P, uint2* __restrict__ out,
+                                                      float* __restrict__ colscale, int nbf) {
+  __shared__ double red[8];
+  const long c = blockIdx.x;  // spin * nbf + j
+  const double* col = P + c * nbf;
+  uint2* o = out + c * nbf;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < nbf; i += blockDim.x) m = fmax(m, fabs(col[i]));
+  for (int d = 16; d > 0; d >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, d));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  m = red[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+  int e = 0;
+  frexp(m, &e);
+  const bool zero = !(m > 0.0) || e < -100;
+  const double inv = zero ? 0.0 : ldexp(1.0, 7 - e);
+  if (threadIdx.x == 0) colscale[c] = zero ? 0.f : ldexpf(1.f, e - 7);
+  for (int i = threadIdx.x; i < nbf; i += blockDim.x) {
+    const double v = col[i] * inv;  // |v| < 128, exact
+    const double s0 = rint(v);
+    const double r1 = (v - s0) * 256.0;
+    const double s1 = rint(r1);
+    const double s2 = rint((r1 - s1) * 256.0);
+    const uint32_t h0 = __half_as_ushort(__float2half_rn((float)s0));
+    const uint32_t h1 = __half_as_ushort(__float2half_rn((float)(s1 * (1.0 / 256.0))));
+    const uint32_t h2 = __half_as_ushort(__float2half_rn((float)(s2 * (1.0 / 65536.0))));
+    o[i] = make_uint2(h0 | (h1 << 16), h2);
+  }
 }
 
 // V holds sum_b F_b on and above the diagonal (row <= column): copy it below
@@ -763,7 +865,7 @@ __global__ void mirror_upper_kernel(double* V, int nbf, int nspin) {
   M[e] = M[(long)i * nbf + j];
 }
 
-static size_t density_smem() { return 2 * kStageBytes + 128 * (kNT + 1) * sizeof(float) + 1024; }
+static size_t density_smem() { return 2 * kDStageBytes + 1024; }
 static size_t adder_smem() { return kAdderStages * kStageBytes + 128 * kDsLd * sizeof(float) + 1024; }
 
 xcgpu_status mixed_init(Ctx* c) {
@@ -789,8 +891,8 @@ static void fill_item(MxItem& it, const MixedWork& w) {
   it.B = *w.B;
   it.P = *w.P;
   it.nspin = w.nspin;
-  const long n = (long)w.P->nbf * w.P->nbf * w.nspin;
-  it.Psplit = reinterpret_cast<const float2*>(w.Psplit);
+  it.Psl = reinterpret_cast<const uint2*>(w.Psplit);
+  it.Pcs = w.Psplit ? reinterpret_cast<const float*>(it.Psl + (long)w.P->nbf * w.P->nbf * w.nspin) : nullptr;
   it.rho = w.rho;
   it.grad = w.grad;
   it.v = w.v;
@@ -847,9 +949,11 @@ static bool any_gga(const std::vector<MixedWork>& work, size_t i0, size_t i1, bo
   return false;
 }
 
-xcgpu_status mixed_split(Ctx* c, const double* Pm, float* Psplit, long n) {
+xcgpu_status mixed_split(Ctx* c, const double* Pm, int nspin, int nbf, float* Psplit) {
   KernelTimer kt(c, kOther);
-  split_p_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(Pm, reinterpret_cast<float2*>(Psplit), n);
+  uint2* sl = reinterpret_cast<uint2*>(Psplit);
+  float* cs = reinterpret_cast<float*>(sl + (long)nspin * nbf * nbf);
+  split_p_kernel<<<(unsigned)(nspin * nbf), 256, 0, c->stream>>>(Pm, sl, cs, nbf);
   return c->check_launch("split_p_kernel");
 }
 
