@@ -303,9 +303,8 @@ __global__ void __launch_bounds__(kT, 1)
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
-  uint32_t phase[2] = {0, 0};
-  bool pend[2] = {false, false};  // a commit on the stage's barrier not yet waited for
-  int gc = 0;                     // chunks issued by this CTA (stage = gc & 1)
+  uint32_t phase = 0, pend = 0;  // per stage (bit): barrier parity; a commit not yet waited for
+  int gc = 0;                    // chunks issued by this CTA (stage = gc & 1)
   float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
 
   for (;;) {
@@ -378,10 +377,10 @@ __global__ void __launch_bounds__(kT, 1)
         if (tid < nnu) s_bscale[tid] = __ldg(Pcs + __ldg(fn + nu0 + tid));
         for (int kc = 0; kc < nkc; ++kc) {
           const int st = gc & 1;
-          if (pend[st]) {  // the MMAs of two chunks ago still read this stage
-            const bool ok = wait_or_abort(&mbar[st], phase[st], err);
-            phase[st] ^= 1;
-            pend[st] = false;
+          if ((pend >> st) & 1u) {  // the MMAs of two chunks ago still read this stage
+            const bool ok = wait_or_abort(&mbar[st], (phase >> st) & 1u, err);
+            phase ^= 1u << st;
+            pend &= ~(1u << st);
             if (__syncthreads_or(!ok)) {
               if (tid == 0) s_abort = 1;
               goto done;
@@ -390,7 +389,7 @@ __global__ void __launch_bounds__(kT, 1)
           uint8_t* const stage = sm + st * kDStageBytes;
           const int mu0 = kc * 64;
           // ---- A: row p, 16-byte chunks j = 2 quarter, 2 quarter + 1 (8 functions each) ----
-#pragma unroll
+#pragma unroll 1
           for (int jj = 0; jj < 2; ++jj) {
             const int j = 2 * quarter + jj;
             uint32_t w0[4], w1[4], w2[4];
@@ -437,7 +436,7 @@ __global__ void __launch_bounds__(kT, 1)
             issue_fixed_chunk(tmem, tc::smem_u32(stage), N, wfirst);
             tc::mma_commit(&mbar[st]);
           }
-          pend[st] = true;
+          pend |= 1u << st;
           ++gc;
           if ((kc % kWinChunks) != kWinChunks - 1 && kc != nkc - 1) continue;
           // ---- end of a window: wait for its MMAs (older stage first), read X ----
@@ -445,10 +444,10 @@ __global__ void __launch_bounds__(kT, 1)
 #pragma unroll
           for (int q = 1; q >= 0; --q) {
             const int sq = (st + q) & 1;  // q = 1: the other (older) stage
-            if (pend[sq]) {
-              ok = wait_or_abort(&mbar[sq], phase[sq], err) && ok;
-              phase[sq] ^= 1;
-              pend[sq] = false;
+            if ((pend >> sq) & 1u) {
+              ok = wait_or_abort(&mbar[sq], (phase >> sq) & 1u, err) && ok;
+              phase ^= 1u << sq;
+              pend &= ~(1u << sq);
             }
           }
           if (__syncthreads_or(!ok)) {
@@ -458,36 +457,32 @@ __global__ void __launch_bounds__(kT, 1)
           tc::fence_after_sync();
           if (c0 < N) {  // warp-uniform
             const float* t = my + (long)nu0 * 128 + p;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const int cb = c0 + 16 * h;
-              float a0[16], ar[16];
-              tc::tmem_ld16(tmem + trow + kColsAcc0 + cb, a0);
-              tc::tmem_ld16(tmem + trow + kColsAccR + cb, ar);
+#pragma unroll 1
+            for (int cb = c0; cb < c0 + 32; cb += 8) {
+              float a0[8], ar[8];
+              tc::tmem_ld8(tmem + trow + kColsAcc0 + cb, a0);
+              tc::tmem_ld8(tmem + trow + kColsAccR + cb, ar);
               if (live) {
+                float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
-                for (int g8 = 0; g8 < 16; g8 += 8) {
-                  float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-#pragma unroll
-                  for (int c = g8; c < g8 + 8; ++c) {
-                    const int col = cb + c;
-                    if (col < nnu) {
-                      const float xv = __fmul_rn(__fadd_rn(a0[c], ar[c]), __fmul_rn(sa, s_bscale[col]));
-                      const float* tc_ = t + (long)col * 128;
-                      rr = fmaf(xv, tc_[0], rr);
-                      if (DERIV) {
-                        gx = fmaf(xv, tc_[cs], gx);
-                        gy = fmaf(xv, tc_[2 * cs], gy);
-                        gz = fmaf(xv, tc_[3 * cs], gz);
-                      }
+                for (int c = 0; c < 8; ++c) {
+                  const int col = cb + c;
+                  if (col < nnu) {
+                    const float xv = __fmul_rn(__fadd_rn(a0[c], ar[c]), __fmul_rn(sa, s_bscale[col]));
+                    const float* tc_ = t + (long)col * 128;
+                    rr = fmaf(xv, tc_[0], rr);
+                    if (DERIV) {
+                      gx = fmaf(xv, tc_[cs], gx);
+                      gy = fmaf(xv, tc_[2 * cs], gy);
+                      gz = fmaf(xv, tc_[3 * cs], gz);
                     }
                   }
-                  r_acc += (double)rr;
-                  if (DERIV) {
-                    g_acc[0] += (double)gx;
-                    g_acc[1] += (double)gy;
-                    g_acc[2] += (double)gz;
-                  }
+                }
+                r_acc += (double)rr;
+                if (DERIV) {
+                  g_acc[0] += (double)gx;
+                  g_acc[1] += (double)gy;
+                  g_acc[2] += (double)gz;
                 }
               }
             }
@@ -525,7 +520,7 @@ __global__ void __launch_bounds__(kT, 1)
 done:
 #pragma unroll
   for (int q = 0; q < 2; ++q)
-    if (pend[q]) wait_or_abort(&mbar[q], phase[q], err);
+    if ((pend >> q) & 1u) wait_or_abort(&mbar[q], (phase >> q) & 1u, err);
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 256);
