@@ -1,17 +1,19 @@
 // Mixed-precision XC build on the sm_103a tensor cores.
 //
-// Basis values and gradients are evaluated in FP32 on the fly (never stored in
-// global memory); the two dense contractions run as 3xTF32 tcgen05 MMAs with FP32
-// accumulation in tensor memory (TMEM):
+// Basis values and gradients are evaluated in FP32 (with an exponential whose errors
+// average to zero); the two dense contractions run as tcgen05 MMAs on fixed-point
+// operands: every row (or column) of an operand is scaled by a power of two and cut
+// into three 8-bit slices held exactly in FP16, so the products of leading slices are
+// integers that the FP32 accumulation in tensor memory (TMEM) sums without rounding,
+// whatever the rounding of the tensor core's adder tree:
 //   density : X = Phi P_b            (M = 128 points, N = active functions, K = functions)
 //             rho = rowsum(X o Phi), grad rho = 2 rowsum(X o grad Phi), summed in FP64
-//   adder   : D = Phi^T G            (M = active functions, N = active functions, K = points)
-//             with G = w (v/2 Phi + g . grad Phi); D goes to V in FP64 (red.add), and
-//             V + V^T at the end gives sum_b (D_b + D_b^T) = sum_b F_b
+//   adder   : F_b = Phi^T G + G^T Phi (M, N = active functions, K = points)
+//             with G = w (v/2 Phi + g . grad Phi); F_b goes to V in FP64 (red.add)
 //             (ScalarOperatorToMatrixAdder.cpp:224-303).
 // The functional, E_xc, N_el and the cross-block Vxc accumulation stay in FP64.
 //
-// Both kernels are persistent (one CTA of 128 threads per SM, blocks taken from a
+// Both kernels are persistent (one CTA of 512 threads per SM, blocks taken from a
 // global counter); one elected thread issues the MMAs; completion is tracked with
 // mbarriers through tcgen05.commit; every wait is bounded in time and reports a
 // timeout through the error word instead of hanging.
@@ -29,7 +31,7 @@
 
 namespace xcgpu {
 
-constexpr uint32_t kTileA = 128 * 128;  // bytes of a 128-row x 32-element operand tile
+constexpr uint32_t kTileA = 128 * 128;  // bytes of a 128-row x 128-byte operand tile
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 constexpr int kErrTimeout = 1;  // error word values (read by the host after a build)
 constexpr int kErrScratch = 2;
@@ -106,60 +108,11 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* mbar, uint32_t parity, i
   return ok;
 }
 
-// Tensor-memory layout (512 columns per CTA): two hi*hi accumulators used in turn by
-// consecutive 32-wide K chunks, and two cross-term accumulators used in turn by
-// consecutive output tiles.  A fresh hi*hi accumulator per chunk keeps every chain of
-// the tensor core's truncating FP32 accumulation at 4 MMAs; the chunk results are then
-// summed in round-to-nearest FP32 on the CUDA cores (one long chain over all K gave a
-// relative density bias of -6e-7).  The cross terms (~2^-11 smaller) stay in one
-// accumulator per tile.
-constexpr int kT = 512;                       // threads per CTA (one CTA per SM)
+constexpr int kT = 512;               // threads per CTA (one CTA per SM)
 constexpr int kWarps = kT / 32;
-constexpr int kQ = kT / 128;                  // threads per point of a 128-point block
-constexpr int kNT = 128;                      // rows of an operand tile (M, and N at most)
-constexpr uint32_t kStageBytes = 4 * kTileA;  // A_hi, A_lo, B_hi, B_lo
-constexpr uint32_t kColsHH0 = 0, kColsHH1 = 128, kColsX0 = 256, kColsX1 = 384;
-constexpr int kTileFloats = 128 * 32;         // one operand tile (hi or lo) in floats
-constexpr int kAdderStages = 2;
-constexpr int kDsLd = 129;  // row stride of the adder's transpose tile (conflict-free both ways)
-
-// hi*hi of one 32-wide K chunk into a fresh accumulator, the two cross products into
-// the tile's cross accumulator
-__device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl, int N,
-                                            uint32_t hh_cols, uint32_t x_cols, bool first_chunk) {
-  const uint32_t idesc = tc::idesc_tf32(128, N);
-  // descriptors of the four operand tiles; a k-slice of 8 TF32 (32 bytes) advances the
-  // start-address field (bits 0-13, in 16-byte units) by 2, without carry since every
-  // address stays below 256 KB
-  const uint64_t dah = tc::smem_desc_sw128(ah), dal = tc::smem_desc_sw128(al);
-  const uint64_t dbh = tc::smem_desc_sw128(bh), dbl = tc::smem_desc_sw128(bl);
-#pragma unroll
-  for (int ks = 0; ks < 4; ++ks) {
-    const uint64_t o = 2u * ks;
-    tc::mma_tf32(tmem + hh_cols, dah + o, dbh + o, idesc, ks > 0 ? 1u : 0u);
-    tc::mma_tf32(tmem + x_cols, dah + o, dbl + o, idesc, (!first_chunk || ks > 0) ? 1u : 0u);
-    tc::mma_tf32(tmem + x_cols, dal + o, dbh + o, idesc, 1u);
-  }
-}
-
-// add (or store) this warp's 32 lanes x 32 columns [32 (warp >> 2), +32) of a TMEM
-// accumulator into registers
-__device__ __forceinline__ void drain_regs(uint32_t tmem_cols, int warp, float* acc, bool store, int N) {
-  const int c0 = 32 * (warp >> 2);
-  if (c0 >= N) return;  // warp-uniform
-  float v[32];
-  tc::tmem_ld32(tmem_cols + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c0, v);
-#pragma unroll
-  for (int i = 0; i < 32; ++i) acc[i] = store ? v[i] : acc[i] + v[i];
-}
-
-// split v into TF32 hi (at t[0]) and lo (at t[kTileFloats])
-__device__ __forceinline__ void st_split(float* t, float v) {
-  uint32_t h, l;
-  tc::split_tf32(v, h, l);
-  t[0] = __uint_as_float(h);
-  t[kTileFloats] = __uint_as_float(l);
-}
+constexpr int kQ = kT / 128;          // threads per point of a 128-point block
+constexpr int kNT = 128;              // rows of an operand tile (M, and N at most)
+constexpr int kTileFloats = 128 * 32;  // one 16 KB operand tile (128 rows x 128 bytes) in floats
 
 // One XC build inside a batched launch: its basis, plan, spin count and buffers.
 struct MxItem {
@@ -527,32 +480,42 @@ done:
 }
 
 // =====================================================================================
-// adder: D = Phi^T G per block, G = w (v/2 Phi + g . grad Phi), V += D (FP64 red.add)
-//   1. every active shell of the block is evaluated once; its functions go to the CTA's
-//      scratch as ready-made operand tiles (TF32 hi and lo, 128 functions x 32 points,
-//      128-byte swizzled K-major, the shared-memory image of the tile): Phi, and G for
-//      each spin.  A warp writes whole 128-byte rows (32 points of one function).
-//   2. the tile products (spin, function tile m, function tile n, 32-point chunk) run as
-//      one pipeline: thread 0 streams the four operand tiles of each step into one of
-//      three shared-memory stages with bulk copies (TMA) two steps ahead and issues the
-//      MMAs; all threads drain the finished step's accumulator into registers; at the
-//      end of a tile pair the sums go to V with FP64 atomics.
+// adder: F_b = Phi^T G + G^T Phi per block, G = w (v/2 Phi + g . grad Phi); V += F_b with
+// FP64 red.add on and above the diagonal (ScalarOperatorToMatrixAdder.cpp:224-303).  The
+// leading slice products are accumulated exactly, as in the density:
+//   1a. every active shell of the block is evaluated once; Phi and G (per spin) go to
+//       the CTA's scratch in FP32, [operand][function][128 points];
+//   1b. one warp per (operand, function) row: the row's largest |value| over the block's
+//       points sets its power-of-two scale (kept in the scratch), and the three FP16
+//       slices of the scaled row go to the scratch as operand tiles (128 functions x 64
+//       points, 128-byte swizzled K-major: the shared-memory image of the tile);
+//   2. per spin and function tile pair a <= b: P1 = Phi_a^T G_b and P2 = G_a^T Phi_b
+//      (= (Phi_b^T G_a)^T, so F(a, b) = P1 + P2 needs no transposition), each over
+//      64-point chunks.  Thread 0 streams the six slice tiles of a step into one of two
+//      shared-memory stages with bulk copies (TMA) and issues the MMAs: leading x leading
+//      into one accumulator, the five other slice products into a second, per product
+//      (all 512 TMEM columns).  After a pair every thread reads its row's 32 columns of
+//      the four accumulators, applies the row and column scales and adds F to V.
+//   Steps are numbered per CTA (J); step J uses stage J & 1 and completes phase
+//   (J >> 1) & 1 of that stage's barriers, so every waiter knows its parity.
 // =====================================================================================
+constexpr int kOpTileFloats = 2 * 3 * kTileFloats;  // one 128-function tile: 2 chunks x 3 slices
+
 template <int DERIV, bool TWO_SPINS>
 __global__ void __launch_bounds__(kT, 1)
     mx_adder_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
+  constexpr int NOPS = TWO_SPINS ? 3 : 2;  // Phi, G per spin
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full[kAdderStages], mdone[kAdderStages];
+  __shared__ uint64_t full[2], mdone[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort;
   __shared__ float s_w[2][4][128];  // per spin and point: w v / 2, w g_x, w g_y, w g_z
   const uint32_t base_s = tc::smem_u32(smem_raw);
   uint8_t* sm = smem_raw + ((1024 - (base_s & 1023)) & 1023);
-  float* Ds = reinterpret_cast<float*>(sm + kAdderStages * kStageBytes);  // [128][kDsLd], a product's tile
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
   if (tid == 0) {
-    for (int i = 0; i < kAdderStages; ++i) {
+    for (int i = 0; i < 2; ++i) {
       tc::mbar_init(&full[i], 1);
       tc::mbar_init(&mdone[i], 1);
     }
@@ -563,10 +526,14 @@ __global__ void __launch_bounds__(kT, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  uint32_t fph = 0, mph = 0;  // phase bit per stage of full (thread 0) and mdone
-  int issued = 0, consumed = 0, committed = 0, drained = 0;  // pipeline steps of the current block
+  const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
+  int J0 = 0;                            // steps of earlier blocks (uniform)
+  int last_copy = -1, last_mma = -1;     // thread 0: highest step copied / issued
   float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
-  const long opstride = (long)bt.ft_max * 4 * 2 * kTileFloats;  // floats per operand (Phi, G_0, G_1)
+  const long rows_pad = (long)bt.ft_max * 128;
+  float* const stg = my;                               // [NOPS][rows_pad][128]
+  float* const tiles = stg + NOPS * rows_pad * 128;    // [NOPS][ft_max][2 chunks][3 slices][4096]
+  float* const scl = tiles + NOPS * bt.ft_max * kOpTileFloats;  // [NOPS][rows_pad]
 
   for (;;) {
     __syncthreads();
@@ -588,9 +555,10 @@ __global__ void __launch_bounds__(kT, 1)
     for (int s = 0; s < nspin; ++s)
       if (!I.skip[(long)s * P.nblocks + b]) smask |= 1 << s;
     if (smask == 0 || nact == 0) continue;
-    const int nft = (nact + 127) >> 7, nkc = (npts + 31) >> 5;
-    if (nft > bt.ft_max || (long)(1 + nspin) * opstride > bt.cta_floats) {  // scratch too small: report, skip
-      if (tid == 0) atomicExch(err, kErrScratch);
+    const int nft = (nact + 127) >> 7, nkc = (npts + 63) >> 6;
+    if (nft > bt.ft_max || nspin > NOPS - 1 ||
+        (long)NOPS * (rows_pad * 128 + bt.ft_max * kOpTileFloats + rows_pad) > bt.cta_floats) {
+      if (tid == 0) atomicExch(err, kErrScratch);  // scratch sized for a smaller block: report, skip
       continue;
     }
     // ---- weights ----
@@ -609,13 +577,12 @@ __global__ void __launch_bounds__(kT, 1)
       for (int c = 0; c < 4; ++c) s_w[s][c][q] = w4[c];
     }
     __syncthreads();
-    // ---- 1. operand tiles of the block ----
+    const bool sp0 = smask & 1, sp1 = TWO_SPINS && ((smask >> 1) & 1);
+    // ---- 1a. Phi and G of the block's points in FP32 (points past npts are masked in 1b) ----
     {
-      const int p = tid & 127;
-      const int kc = p >> 5, k = p & 31;
-      if (kc < nkc) {  // warp-uniform
-        const bool live = p < npts;
-        const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
+      const int p = tid & 127, quarter = tid >> 7;
+      if (p < npts) {
+        const Pt pt = make_pt(P.xyz + 3 * (first + p));
         const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
         constexpr int NS = TWO_SPINS ? 2 : 1;
         float wsp[NS][4];
@@ -623,188 +590,186 @@ __global__ void __launch_bounds__(kT, 1)
         for (int s = 0; s < NS; ++s)
 #pragma unroll
           for (int c = 0; c < 4; ++c) wsp[s][c] = s_w[s][c][p];
-        const bool sp0 = smask & 1, sp1 = TWO_SPINS && ((smask >> 1) & 1);
-        const int kq = k >> 2, kr = k & 3;
-        float* const base = my + kc * 2 * kTileFloats + kr;
-        const int quarter = tid >> 7;
+        float* const col = stg + p;
         ShellRec next;
         if (s0 + quarter < s1) next = load_rec(P.rec + s0 + quarter);
         for (int si = s0 + quarter; si < s1; si += kQ) {
           const ShellRec r = next;
           if (si + kQ < s1) next = load_rec(P.rec + si + kQ);  // in flight while r is evaluated
-          const int f0 = rec_f0(r.info);
+          float* const t0 = col + (long)rec_f0(r.info) * 128;
           auto put = [&](int f, float val, float dx, float dy, float dz) {
-            const int mu = f0 + f, row = mu & 127;
-            float* t = base + (long)(mu >> 7) * 4 * 2 * kTileFloats + row * 32 + (((kq ^ (row & 7)) & 7) << 2);
-            st_split(t, val);
+            float* t = t0 + f * 128;
+            t[0] = val;
             if (sp0) {
               float gv = wsp[0][0] * val;
               if (DERIV) gv += wsp[0][1] * dx + wsp[0][2] * dy + wsp[0][3] * dz;
-              st_split(t + opstride, gv);
+              t[rows_pad * 128] = gv;
             }
             if (TWO_SPINS && sp1) {
               float gv = wsp[NS - 1][0] * val;
               if (DERIV) gv += wsp[NS - 1][1] * dx + wsp[NS - 1][2] * dy + wsp[NS - 1][3] * dz;
-              st_split(t + 2 * opstride, gv);
+              t[2 * rows_pad * 128] = gv;
             }
           };
-          if (live) {
-            shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, put);
-          } else {
-            const int nf = rec_nf(r.info);
-            for (int f = 0; f < nf; ++f) put(f, 0.f, 0.f, 0.f, 0.f);
-          }
+          shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, put);
         }
+      }
+    }
+    __syncthreads();
+    // ---- 1b. row scales and FP16 slice tiles, one warp per (operand, function) row ----
+    {
+      const int nop = 1 + __popc(smask);
+      const int k4 = 4 * lane;  // this lane's 4 points
+      for (int r = warp; r < nop * nact; r += kWarps) {
+        const int oi = r / nact, m = r - oi * nact;
+        const int o = oi == 0 ? 0 : (smask == 2 ? 2 : oi);
+        float4 v = *reinterpret_cast<const float4*>(stg + ((long)o * rows_pad + m) * 128 + k4);
+        if (k4 + 0 >= npts) v.x = 0.f;
+        if (k4 + 1 >= npts) v.y = 0.f;
+        if (k4 + 2 >= npts) v.z = 0.f;
+        if (k4 + 3 >= npts) v.w = 0.f;
+        float mx = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+        float scale, inv;
+        fixed_scale(mx, scale, inv);
+        if (lane == 0) scl[o * rows_pad + m] = scale;
+        uint16_t h[3][4];
+        fixed_slices(__fmul_rn(v.x, inv), h[0][0], h[1][0], h[2][0]);
+        fixed_slices(__fmul_rn(v.y, inv), h[0][1], h[1][1], h[2][1]);
+        fixed_slices(__fmul_rn(v.z, inv), h[0][2], h[1][2], h[2][2]);
+        fixed_slices(__fmul_rn(v.w, inv), h[0][3], h[1][3], h[2][3]);
+        uint8_t* tb = reinterpret_cast<uint8_t*>(tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 *
+                                                            kTileFloats);
+        const uint32_t off = tc::swz_offset_h(m & 127, k4 & 63);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+          *reinterpret_cast<uint2*>(tb + i * kTileA + off) =
+              make_uint2((uint32_t)h[i][0] | ((uint32_t)h[i][1] << 16), (uint32_t)h[i][2] | ((uint32_t)h[i][3] << 16));
       }
       tc::fence_async_global();  // these generic writes are read by the bulk copies below
     }
     __syncthreads();
-    // ---- 2. tile products ----
-    // F_b = D + D^T with D = Phi^T G is symmetric, so V is accumulated on and above the
-    // diagonal only (a mirror kernel fills the rest): per spin, for every function tile
-    // pair a <= b, the products D(a, b) and (a < b) D(b, a) run back to back; D(a, a) is
-    // folded with its transpose, D(b, a) transposed onto D(a, b), through Ds in shared
-    // memory, and each element goes to V with one FP64 atomic.  Steps run over
-    // (spin, a, b, product, 32-point chunk), chunk fastest; the copy issuer and the MMA
-    // issuer (thread 0) and the drain (all threads) walk them with incremental cursors.
-    const int nsteps = __popc(smask) * nft * nft * nkc;
-    struct Cursor {
-      int si, a, b, ph, kc, prod, st;  // ph: 0 = D(a, b), 1 = D(b, a)
-    };
-    auto advance = [&](Cursor& c) {
-      c.st = (c.st + 1 == kAdderStages) ? 0 : c.st + 1;
-      if (++c.kc < nkc) return;
-      c.kc = 0;
-      ++c.prod;
-      if (c.ph == 0 && c.a < c.b) {
-        c.ph = 1;
-        return;
+    // ---- 2. tile pairs ----
+    const int spp = 2 * nkc;                              // steps per pair: 2 products x chunks
+    const int npairs = __popc(smask) * (nft * (nft + 1) / 2);
+    const int nsteps = npairs * spp;
+    // step i of this block -> (spin, a, b, product, chunk); pairs ordered (spin, a, b >= a)
+    auto decode = [&](int i, int& spin, int& a, int& bb, int& ph, int& kc) {
+      kc = i % nkc;
+      ph = (i / nkc) & 1;
+      int q = i / spp;
+      const int per = nft * (nft + 1) / 2;
+      const int si = q / per;
+      q -= si * per;
+      a = 0;
+      while (q >= nft - a) {
+        q -= nft - a;
+        ++a;
       }
-      c.ph = 0;
-      if (++c.b < nft) return;
-      if (++c.a < nft) {
-        c.b = c.a;
-        return;
+      bb = a + q;
+      spin = (smask == 2) ? 1 : si;
+    };
+    auto issue_copy = [&](int i) {
+      int spin, a, bb, ph, kc;
+      decode(i, spin, a, bb, ph, kc);
+      const int J = J0 + i, st = J & 1;
+      uint8_t* dst = sm + st * kDStageBytes;
+      const int oA = ph ? 1 + spin : 0, oB = ph ? 0 : 1 + spin;
+      const int nM = min(128, nact - 128 * a), nN = min(128, nact - 128 * bb);
+      const uint32_t ab = (uint32_t)((nM + 7) & ~7) * 128u, bbytes = (uint32_t)((nN + 7) & ~7) * 128u;
+      const float* ta = tiles + (((long)oA * bt.ft_max + a) * 2 + kc) * 3 * kTileFloats;
+      const float* tb = tiles + (((long)oB * bt.ft_max + bb) * 2 + kc) * 3 * kTileFloats;
+      tc::mbar_arrive_expect_tx(&full[st], 3 * ab + 3 * bbytes);
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        tc::bulk_g2s(dst + s * kTileA, ta + s * kTileFloats, ab, &full[st]);
+        tc::bulk_g2s(dst + (3 + s) * kTileA, tb + s * kTileFloats, bbytes, &full[st]);
       }
-      c.a = c.b = 0;
-      ++c.si;
+      last_copy = J;
     };
-    auto mt_of = [](const Cursor& c) { return c.ph ? c.b : c.a; };
-    auto nt_of = [](const Cursor& c) { return c.ph ? c.a : c.b; };
-    auto spin_of = [&](const Cursor& c) { return (smask == 2) ? 1 : c.si; };
-    auto issue_copy = [&](const Cursor& c) {
-      uint8_t* dst = sm + c.st * kStageBytes;
-      const int mt = mt_of(c), nt = nt_of(c);
-      const int nM = min(128, nact - 128 * mt), nN = min(128, nact - 128 * nt);
-      const uint32_t ab = (uint32_t)((nM + 7) & ~7) * 128u, bb = (uint32_t)((nN + 15) & ~15) * 128u;
-      const float* a = my + (long)(mt * 4 + c.kc) * 2 * kTileFloats;
-      const float* g = my + (long)(1 + spin_of(c)) * opstride + (long)(nt * 4 + c.kc) * 2 * kTileFloats;
-      tc::mbar_arrive_expect_tx(&full[c.st], 2 * ab + 2 * bb);
-      tc::bulk_g2s(dst, a, ab, &full[c.st]);
-      tc::bulk_g2s(dst + kTileA, a + kTileFloats, ab, &full[c.st]);
-      tc::bulk_g2s(dst + 2 * kTileA, g, bb, &full[c.st]);
-      tc::bulk_g2s(dst + 3 * kTileA, g + kTileFloats, bb, &full[c.st]);
-    };
-    Cursor cc = {0, 0, 0, 0, 0, 0, 0}, mc = cc, dc = cc;  // copy, MMA, drain
-    issued = consumed = committed = drained = 0;
-    float acc[32];  // this thread's 32 columns of one row of the current product
-    const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
+    bool ok = true;
     if (tid == 0)
-      for (; issued < min(kAdderStages, nsteps); ++issued) {
-        issue_copy(cc);
-        advance(cc);
-      }
-    for (int i = 0; i <= nsteps; ++i) {
-      bool bad = false;
-      if (tid == 0 && i < nsteps) {
-        if (tc::mbar_wait_bounded(&full[mc.st], (fph >> mc.st) & 1u, kWaitLimitNs)) {
-          fph ^= 1u << mc.st;
-          ++consumed;
-          tc::fence_after_sync();
-          const int N = (min(128, nact - 128 * nt_of(mc)) + 15) & ~15;
-          const uint32_t sa = tc::smem_u32(sm + mc.st * kStageBytes);
-          issue_chunk(tmem, sa, sa + kTileA, sa + 2 * kTileA, sa + 3 * kTileA, N, (i & 1) ? kColsHH1 : kColsHH0,
-                      (mc.prod & 1) ? kColsX1 : kColsX0, mc.kc == 0);
-          tc::mma_commit(&mdone[mc.st]);
-          ++committed;
-          advance(mc);
-        } else {
-          bad = true;
-        }
-      }
-      if (i >= 1) {
-        if (tc::mbar_wait_bounded(&mdone[dc.st], (mph >> dc.st) & 1u, kWaitLimitNs)) {
-          mph ^= 1u << dc.st;
-          ++drained;
-          // the MMAs of step i - 1 are done with its stage: refill it for step i + 1
-          if (tid == 0 && issued < nsteps) {
-            issue_copy(cc);
-            advance(cc);
-            ++issued;
+      for (int i = 0; i < min(2, nsteps); ++i) issue_copy(i);
+    for (int q = 0; q < npairs; ++q) {
+      const int iL = q * spp + spp - 1;  // the pair's last step
+      if (tid == 0 && ok) {
+        for (int i = q * spp; i <= iL; ++i) {
+          const int J = J0 + i, st = J & 1;
+          if (!tc::mbar_wait_bounded(&full[st], (J >> 1) & 1u, kWaitLimitNs)) {
+            ok = false;
+            break;
           }
-        } else {
-          bad = true;
+          tc::fence_after_sync();
+          int spin, a, bb, ph, kc;
+          decode(i, spin, a, bb, ph, kc);
+          const int N = (min(128, nact - 128 * bb) + 15) & ~15;
+          issue_fixed_chunk(tmem + (ph ? 256u : 0u), tc::smem_u32(sm + st * kDStageBytes), N, kc == 0);
+          tc::mma_commit(&mdone[st]);
+          last_mma = J;
+          // the stage of step i - 1 (same pair) is free once its MMAs are done: refill it
+          if (i > q * spp && i + 1 < nsteps) {
+            if (!tc::mbar_wait_bounded(&mdone[(J - 1) & 1], ((J - 1) >> 1) & 1u, kWaitLimitNs)) {
+              ok = false;
+              break;
+            }
+            issue_copy(i + 1);
+          }
         }
       }
-      if (__syncthreads_or(bad)) {
-        if (bad) atomicExch(err, kErrTimeout);
+      // ---- the pair's accumulators -> V ----
+      const int JL = J0 + iL;
+      const bool done_ok = tc::mbar_wait_bounded(&mdone[JL & 1], (JL >> 1) & 1u, kWaitLimitNs);
+      if (tid == 0 && done_ok && ok && iL + 2 < nsteps) issue_copy(iL + 2);  // prefetch during the drain
+      if (__syncthreads_or(!(done_ok && ok))) {
+        if (tid == 0) atomicExch(err, kErrTimeout);
         goto abort;
       }
-      if (i >= 1) {
-        tc::fence_after_sync();
-        const int mt = mt_of(dc), nt = nt_of(dc);
-        const int nM = min(128, nact - 128 * mt), nN = min(128, nact - 128 * nt);
-        const int N = (nN + 15) & ~15;
-        drain_regs(tmem + (((i - 1) & 1) ? kColsHH1 : kColsHH0), warp, acc, dc.kc == 0, N);
-        if (dc.kc == nkc - 1) {  // end of a product
-          drain_regs(tmem + ((dc.prod & 1) ? kColsX1 : kColsX0), warp, acc, false, N);
-          if (dc.ph == 0) {
+      tc::fence_after_sync();
+      {
+        int spin, a, bb, ph, kc;
+        decode(iL, spin, a, bb, ph, kc);
+        const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
+        const int ma = min(128, nact - 128 * a), nb = min(128, nact - 128 * bb);
+        const int N = (nb + 15) & ~15;
+        const bool rok = row < ma;
+        const int m = 128 * a + row;
+        const float sPm = rok ? scl[m] : 0.f, sGm = rok ? scl[(1 + spin) * rows_pad + m] : 0.f;
+        double* Vrow = I.V + (long)spin * nbf * nbf + (rok ? __ldg(fn + m) : 0);
+        const float* sPn = scl + 128 * bb;
+        const float* sGn = scl + (1 + spin) * rows_pad + 128 * bb;
+        if (c0 < N) {  // warp-uniform
+#pragma unroll 1
+          for (int cb = c0; cb < c0 + 32; cb += 8) {
+            float p0[8], pr[8], q0[8], qr[8];
+            tc::tmem_ld8(tmem + trow + 0 + cb, p0);
+            tc::tmem_ld8(tmem + trow + 128 + cb, pr);
+            tc::tmem_ld8(tmem + trow + 256 + cb, q0);
+            tc::tmem_ld8(tmem + trow + 384 + cb, qr);
 #pragma unroll
-            for (int c = 0; c < 32; ++c) Ds[row * kDsLd + c0 + c] = acc[c];
-          } else {  // D(b, a): row n of tile b, columns m of tile a -> Ds[m][n]
-#pragma unroll
-            for (int c = 0; c < 32; ++c) Ds[(c0 + c) * kDsLd + row] += acc[c];
-          }
-          const bool flush = dc.a == dc.b || dc.ph == 1;
-          if (flush) {  // uniform across the CTA
-            __syncthreads();
-            // thread row m of tile a, columns n of tile b: F(m, n) into V(fn_a[m], fn_b[n])
-            const int ma = min(128, nact - 128 * dc.a), nb_ = min(128, nact - 128 * dc.b);
-            if (row < ma) {
-              double* Vs = I.V + (long)spin_of(dc) * nbf * nbf + __ldg(fn + 128 * dc.a + row);
-              const int* fnb = fn + 128 * dc.b + c0;
-              const bool diag = dc.a == dc.b;
-#pragma unroll 8
-              for (int c = 0; c < 32; ++c) {
-                const int n = c0 + c;
-                if (n < nb_ && (!diag || n >= row)) {
-                  const float f = diag ? Ds[row * kDsLd + n] + Ds[n * kDsLd + row] : Ds[row * kDsLd + n];
-                  atomicAdd(Vs + (long)__ldg(fnb + c) * nbf, (double)f);
-                }
+            for (int c = 0; c < 8; ++c) {
+              const int n = cb + c;
+              if (rok && n < nb && (a < bb || n >= row)) {
+                const float f1 = __fmul_rn(__fadd_rn(p0[c], pr[c]), __fmul_rn(sPm, sGn[n]));
+                const float f2 = __fmul_rn(__fadd_rn(q0[c], qr[c]), __fmul_rn(sGm, sPn[n]));
+                atomicAdd(Vrow + (long)__ldg(fn + 128 * bb + n) * nbf, (double)__fadd_rn(f1, f2));
               }
             }
-            __syncthreads();  // Ds is reused by the next product
           }
         }
-        advance(dc);
-        tc::fence_before_sync();
       }
-      __syncthreads();
+      tc::fence_before_sync();
+      __syncthreads();  // the accumulators are reused by the next pair
     }
+    J0 += nsteps;
   }
   goto done;
 abort:
   if (tid == 0) {
     s_abort = 1;
     // let every copy and MMA still in flight land before the CTA gives up its memory
-    for (int i = consumed; i < issued; ++i) {
-      const int st = i % kAdderStages;
-      if (tc::mbar_wait_bounded(&full[st], (fph >> st) & 1u, kWaitLimitNs)) fph ^= 1u << st;
-    }
-    for (int i = drained; i < committed; ++i) {
-      const int st = i % kAdderStages;
-      if (tc::mbar_wait_bounded(&mdone[st], (mph >> st) & 1u, kWaitLimitNs)) mph ^= 1u << st;
-    }
+    for (int J = last_mma + 1; J <= last_copy; ++J) tc::mbar_wait_bounded(&full[J & 1], (J >> 1) & 1u, kWaitLimitNs);
+    if (last_mma >= 0) tc::mbar_wait_bounded(&mdone[last_mma & 1], (last_mma >> 1) & 1u, kWaitLimitNs);
   }
 done:
   tc::fence_before_sync();
@@ -861,7 +826,7 @@ __global__ void mirror_upper_kernel(double* V, int nbf, int nspin) {
 }
 
 static size_t density_smem() { return 2 * kDStageBytes + 1024; }
-static size_t adder_smem() { return kAdderStages * kStageBytes + 128 * kDsLd * sizeof(float) + 1024; }
+static size_t adder_smem() { return 2 * kDStageBytes + 1024; }
 
 xcgpu_status mixed_init(Ctx* c) {
   const struct {
@@ -896,8 +861,9 @@ static void fill_item(MxItem& it, const MixedWork& w) {
   it.V = w.V;
 }
 
-// Scratch floats per CTA for the items [i0, i1): the density's [4][n_b][128] values
-// and the adder's (1 + nspin) operands of ft_max x 4 tiles (hi + lo).
+// Scratch floats per CTA for the items [i0, i1): the density's [4][n_b][128] values,
+// and per adder operand (Phi, G per spin) the FP32 rows, the slice tiles and the row
+// scales of ft_max 128-function tiles.
 static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t i1, int* ft_max) {
   int amax = 0, smax = 1;
   for (size_t i = i0; i < i1; ++i) {
@@ -907,7 +873,7 @@ static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t
   const int ft = std::max(1, (amax + 127) / 128);
   *ft_max = ft;
   const long dens = 4L * amax * 128;
-  const long add = (long)(1 + smax) * ft * 4 * 2 * kTileFloats;
+  const long add = (long)(1 + smax) * ft * (128L * 128 + kOpTileFloats + 128);
   return (std::max(dens, add) + 63) & ~63L;
 }
 
