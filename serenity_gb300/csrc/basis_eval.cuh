@@ -191,9 +191,11 @@ __device__ __forceinline__ void shell_functions(R x, R y, R z, R Rv, R dR, R ddR
 }
 
 // Same as shell_functions, with the transform coefficients as compile-time constants.
+// Emit(f, value, value_lo, dx, dy, dz): value_lo carries the rounding of the coefficients
+// to R (c - R(c) times the term), which is the same relative error of a function at
+// every point (sqrt(3) of the d functions, for one) and would otherwise bias it.
 template <class R, int L, int DERIV, class Emit>
 __device__ __forceinline__ void shell_functions_cx(R x, R y, R z, R Rv, R dR, bool pure, Emit&& emit) {
-  constexpr int NC = (L + 1) * (L + 2) / 2;
   constexpr int NS = 2 * L + 1;
   constexpr cx::Table TS = cx::solid(L);
   constexpr cx::Table TC = cx::cartesian(L);
@@ -205,10 +207,10 @@ __device__ __forceinline__ void shell_functions_cx(R x, R y, R z, R Rv, R dR, bo
     py[k] = py[k - 1] * y;
     pz[k] = pz[k - 1] * z;
   }
-  R sv[NS], sg[3 * NS];
+  R sv[NS], svl[NS], sg[3 * NS];
 #pragma unroll
   for (int m = 0; m < NS; ++m) {
-    sv[m] = R(0);
+    sv[m] = svl[m] = R(0);
     sg[3 * m] = sg[3 * m + 1] = sg[3 * m + 2] = R(0);
   }
   int k = 0;
@@ -233,8 +235,10 @@ __device__ __forceinline__ void shell_functions_cx(R x, R y, R z, R Rv, R dR, bo
 #pragma unroll
         for (int m = 0; m < NS; ++m) {
           const R t = R(TS.c[m][k]);
+          const R tl = R(TS.c[m][k] - (double)R(TS.c[m][k]));
           if (TS.c[m][k] != 0.0) {
             sv[m] += t * v;
+            if (tl != R(0)) svl[m] = fmaf(tl, v, svl[m]);
             if (DERIV >= 1) {
               sg[3 * m] += t * g0;
               sg[3 * m + 1] += t * g1;
@@ -244,13 +248,14 @@ __device__ __forceinline__ void shell_functions_cx(R x, R y, R z, R Rv, R dR, bo
         }
       } else {
         const R t = R(TC.c[0][k]);
-        emit(k, t * v, t * g0, t * g1, t * g2);
+        const R tl = R(TC.c[0][k] - (double)R(TC.c[0][k]));
+        emit(k, t * v, tl * v, t * g0, t * g1, t * g2);
       }
     }
   }
   if (pure) {
 #pragma unroll
-    for (int m = 0; m < NS; ++m) emit(m, sv[m], sg[3 * m], sg[3 * m + 1], sg[3 * m + 2]);
+    for (int m = 0; m < NS; ++m) emit(m, sv[m], svl[m], sg[3 * m], sg[3 * m + 1], sg[3 * m + 2]);
   }
 }
 

@@ -46,4 +46,26 @@ __device__ __forceinline__ float exp_tang(float x) {
   return m < -125 ? 0.f : __fmul_rn(v, __int_as_float((m + 127) << 23));
 }
 
+// the same value as an FP32 pair, exp(x) = hi + lo to ~2^-30: hi is exp_tang(x) (the
+// rounded value), lo the remainder (|lo| <= ulp(hi) / 2); for sums that must not inherit
+// the rounding of each exp
+__device__ __forceinline__ void exp_tang2(float x, float& hi, float& lo) {
+  x = fmaxf(x, -104.f);
+  const float kf = rintf(__fmul_rn(x, 46.16624f));
+  const int k = (int)kf;
+  const int j = k & 31, m = k >> 5;
+  float r = fmaf(-kf, 0x1.63p-6f, x);
+  r = fmaf(-kf, -0x1.bd0106p-18f, r);
+  r = fmaf(-kf, 0x1.cf79acp-45f, r);
+  const float q = __fmul_rn(__fmul_rn(r, r), fmaf(r, fmaf(r, 1.f / 24.f, 1.f / 6.f), 0.5f));
+  const float u = __fadd_rn(r, q);
+  const float2 T = __ldg(kExp2Tab + j);
+  const float c = fmaf(T.x, u, T.y);  // |c| < T.x / 64
+  const float h = __fadd_rn(T.x, c);
+  const float l = __fsub_rn(c, __fsub_rn(h, T.x));  // exact: T.x + c = h + l
+  const float sc = m < -125 ? 0.f : __int_as_float((m + 127) << 23);
+  hi = __fmul_rn(h, sc);
+  lo = __fmul_rn(l, sc);
+}
+
 }  // namespace xcgpu

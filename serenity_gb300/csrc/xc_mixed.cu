@@ -56,34 +56,61 @@ __device__ __forceinline__ int rec_nprim(int info) { return (info >> 4) & 31; }
 __device__ __forceinline__ int rec_nf(int info) { return (info >> 9) & 31; }
 __device__ __forceinline__ int rec_f0(int info) { return info >> 14; }
 
-// Evaluate one shell record at a point in FP32; Emit(f, value, dx, dy, dz).
-// Negligible shells (|R| below the radial threshold) emit zeros.
+// Evaluate one shell record at a point in FP32; Emit(f, value, value_lo, dx, dy, dz)
+// (value_lo: the coefficients' rounding, shell_functions_cx).
+// Negligible shells (|R| below the radial threshold) emit zeros.  The radial factor is
+// summed as an FP32 pair (exp_tang2, products and sums with their rounding errors) and
+// *rlo receives R_lo / R_hi: all grid points of one radial shell of an atom share the
+// atom's functions' R, so its FP32 rounding would be the same error at all of them (and
+// at every atom of the element) instead of averaging out; value * (1 + *rlo) carries R
+// to ~2^-30 (the angular factors vary from point to point and stay FP32).
 template <int DERIV, class Emit>
 __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __restrict__ prim4, const Pt& q,
-                                             float expthr, float thr, Emit&& emit) {
+                                             float expthr, float thr, float* rlo, Emit&& emit) {
   const float x = (q.h[0] - r.ah[0]) + (q.l[0] - r.al[0]);
   const float y = (q.h[1] - r.ah[1]) + (q.l[1] - r.al[1]);
   const float z = (q.h[2] - r.ah[2]) + (q.l[2] - r.al[2]);
-  const float r2 = x * x + y * y + z * z;
+  // r^2 = r2 + r2l (products by FMA, sums by two-sum): on a radial shell of the
+  // function's own atom r^2 is one number, so a rounding of it (or of alpha r^2) would be
+  // one relative error t 2^-25 of exp(-t) at every point of the shell
+  float r2 = __fmul_rn(x, x), r2l = fmaf(x, x, -r2);
+  {
+    const float yy = __fmul_rn(y, y), zz = __fmul_rn(z, z);
+    const float s1 = __fadd_rn(r2, yy), b1 = __fsub_rn(s1, r2);
+    const float e1 = __fadd_rn(__fsub_rn(r2, __fsub_rn(s1, b1)), __fsub_rn(yy, b1));
+    const float s2 = __fadd_rn(s1, zz), b2 = __fsub_rn(s2, s1);
+    const float e2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(zz, b2));
+    r2l = __fadd_rn(__fadd_rn(r2l, __fadd_rn(e1, e2)), __fadd_rn(fmaf(y, y, -yy), fmaf(z, z, -zz)));
+    r2 = s2;
+  }
   const int np = rec_nprim(r.info);
-  float Rv = 0.f, dR = 0.f;
+  float Rv = 0.f, Rl = 0.f, dR = 0.f;
   for (int i = 0; i < np; ++i) {
     const float4 ac = __ldg(prim4 + r.prim0 + i);  // alpha = x + z, coef = y + w
-    const float t = fmaf(ac.z, r2, __fmul_rn(ac.x, r2));
+    const float t = __fmul_rn(ac.x, r2);           // alpha r^2 = t + tl
+    const float tl = fmaf(ac.x, r2l, fmaf(ac.z, r2, fmaf(ac.x, r2, -t)));
     if (t < expthr) {
       // explicit roundings: R comes out bit-identical whether or not dR is formed
-      const float E = exp_tang(-t);
-      const float e = fmaf(ac.w, E, __fmul_rn(ac.y, E));
-      Rv = __fadd_rn(Rv, e);
-      if (DERIV >= 1) dR = fmaf(-2.f * ac.z, e, fmaf(-2.f * ac.x, e, dR));
+      float Eh, El;
+      exp_tang2(-t, Eh, El);
+      El = fmaf(-Eh, tl, El);  // exp(-t - tl) = (Eh + El)(1 - tl)
+      const float eh = __fmul_rn(ac.y, Eh);
+      const float el = fmaf(ac.y, El, fmaf(ac.w, Eh, fmaf(ac.y, Eh, -eh)));  // c E - eh
+      const float s = __fadd_rn(Rv, eh);                                       // two-sum
+      const float bp = __fsub_rn(s, Rv);
+      const float err = __fadd_rn(__fsub_rn(Rv, __fsub_rn(s, bp)), __fsub_rn(eh, bp));
+      Rl = __fadd_rn(Rl, __fadd_rn(err, el));
+      Rv = s;
+      if (DERIV >= 1) dR = fmaf(-2.f * ac.z, eh, fmaf(-2.f * ac.x, eh, dR));
     }
   }
   const int l = rec_l(r.info);
   if (!(fabsf(Rv) >= thr)) {
     const int nf = rec_nf(r.info);
-    for (int f = 0; f < nf; ++f) emit(f, 0.f, 0.f, 0.f, 0.f);
+    for (int f = 0; f < nf; ++f) emit(f, 0.f, 0.f, 0.f, 0.f, 0.f);
     return;
   }
+  *rlo = Rv != 0.f ? __fdiv_rn(Rl, Rv) : 0.f;
   shell_functions_cx_l<float, DERIV>(l, x, y, z, Rv, dR, rec_pure(r.info), emit);
 }
 
@@ -162,53 +189,102 @@ __device__ __forceinline__ const MxItem& locate(const MxBatch& bt, int gb, int& 
 //   up to an ulp per accumulation step, always towards zero, which shows as a systematic
 //   density deficit (about -6e-8 relative with 3xTF32 operands).  Here both operands are
 //   fixed point: each row of A = Phi (one point) and each column of B = P (one function
-//   nu) is scaled by a power of two that brings its largest element below 128 and cut
-//   into three 8-bit slices (fixed_slices).  Products of leading slices are integers
-//   below 2^14, so their sums over up to 1024 functions are exact in FP32 whatever the
-//   rounding of the adder tree; the remaining five slice products (at most 2^-7 of the
-//   leading ones, with signs uncorrelated with X) go to a second accumulator.  The
-//   slices are stored pre-scaled as FP16 (exact) and multiplied with kind::f16 MMAs.
-//   1. every active shell of the block is evaluated once (value and, for GGA, gradient)
-//      into the CTA's scratch, FP32, [component][function][128 points], with the
-//      largest |phi| of each point;
+//   nu) is scaled by a power of two that brings its largest element below 32 and cut
+//   into a 6-bit and two 12-bit slices (density_slices, 30 bits).  Per window of two
+//   64-wide K chunks, the leading products (integers below 2^10) and the first-order
+//   products s0 t1 + s1 t0 (below 2^17 units of 2^-12, sum below 2^24) each have an
+//   accumulator whose sums are exact in FP32 whatever the rounding of the adder tree:
+//   the first-order terms carry the elements below 2^-6 of their row or column maximum
+//   (those have s0 = 0), whose signs follow X's.  The second-order products s1 t1 and
+//   s0 t2 + s2 t0 (at most 2^-12 of the leading ones; the last with s2 stored as a
+//   multiple of 2^-12, so every FP16 operand is a normal number) have one accumulator
+//   each.  The slices are stored pre-scaled as FP16 (exact) and multiplied with
+//   kind::f16 MMAs.
+//   1. every active shell of the block is evaluated once (value with its low part and,
+//      for GGA, gradient) into the CTA's scratch, FP32, [plane][function][128 points],
+//      with the largest |phi| of each point;
 //   2. per pass of <= 128 functions nu: X = Phi P_b over K chunks of 64 functions mu,
-//      A sliced from the scratch, B gathered from the pre-sliced density matrix; the two
-//      accumulators are read after every window of up to kWinChunks chunks;
+//      A sliced from the scratch, B gathered from the pre-sliced density matrix; the
+//      accumulators are read after every window of kWinChunks chunks;
 //   3. rho_p += sum_nu X_p,nu phi_nu(p), grad rho_p += 2 sum_nu X_p,nu grad phi_nu(p).
 // =====================================================================================
 constexpr uint32_t kDStageBytes = 6 * kTileA;  // A slices 0-2, B slices 0-2 (64 FP16 wide)
-constexpr int kWinChunks = 8;                  // 512 functions: |sum of leading products| < 2^23
-constexpr uint32_t kColsAcc0 = 0, kColsAccR = 128;
+constexpr int kWinChunks = 2;                  // density: chunks per exact window (128 functions)
 
-// v in (-128, 128) -> s0 + s1 / 2^8 + s2 / 2^16, s_i integers in [-128, 128], as FP16
-// (s0, s1 / 2^8, s2 / 2^16); every step is exact (each remainder is a multiple of the
-// unit of v) except the rounding of s2, so |v - sum| <= 2^-17
+// Fixed-point slices of a value v scaled into (-2^R, 2^R): v = s0 + s1 / 2^B + s2 / 2^(2B)
+// + r with integers s0 in [-2^R, 2^R], s1, s2 in [-2^(B-1), 2^(B-1)], |r| <= 2^-(2B+1);
+// every step is exact (each remainder is a multiple of the unit of v) except the
+// rounding of s2.  Stored pre-scaled, (s0, s1 / 2^B, s2 / 2^(2B)), in FP16, which holds
+// each exactly (the smallest in its subnormal range).
+//   adder   R = 7, B = 8: 24 bits; leading products below 2^14, exact sums over 1024
+//   (the density uses density_slices below)
+template <int R, int B>
 __device__ __forceinline__ void fixed_slices(float v, uint16_t& h0, uint16_t& h1, uint16_t& h2) {
+  constexpr float up = (float)(1 << B), down = 1.f / (float)(1 << B), down2 = down * down;
   const float s0 = rintf(v);
-  const float r1 = __fmul_rn(__fsub_rn(v, s0), 256.f);
+  const float r1 = __fmul_rn(__fsub_rn(v, s0), up);
   const float s1 = rintf(r1);
-  const float s2 = rintf(__fmul_rn(__fsub_rn(r1, s1), 256.f));
+  const float s2 = rintf(__fmul_rn(__fsub_rn(r1, s1), up));
   h0 = __half_as_ushort(__float2half_rn(s0));
-  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, 1.f / 256.f)));
-  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, 1.f / 65536.f)));
+  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, down)));
+  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, down2)));
 }
 
-// power-of-two scale of a row or column with largest magnitude m: m * inv < 128;
-// rows below 2^-100 count as zero
+// Density slices of v = vh + vl (|vl| at most about an ulp of vh) scaled into (-32, 32):
+// v = s0 + s1 / 2^12 + s2 / 2^24 + r, s0 in [-32, 32], s1, s2 in [-2048, 2048], |r| <=
+// 2^-25; stored as FP16 (s0, s1 / 2^12, s2 / 2^12), all exact and (but zero) normal
+// numbers: the s2 products are accumulated apart and scaled by 2^-12 when read.
+__device__ __forceinline__ void density_slices(float vh, float vl, uint16_t& h0, uint16_t& h1, uint16_t& h2) {
+  const float s0 = rintf(vh);
+  const float r1 = __fmul_rn(__fadd_rn(__fsub_rn(vh, s0), vl), 4096.f);
+  const float s1 = rintf(r1);
+  const float s2 = rintf(__fmul_rn(__fsub_rn(r1, s1), 4096.f));
+  h0 = __half_as_ushort(__float2half_rn(s0));
+  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, 1.f / 4096.f)));
+  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, 1.f / 4096.f)));
+}
+
+// power-of-two scale of a row or column with largest magnitude m >= 0: with m = f 2^e,
+// 0.5 <= f < 1 (e = biased exponent - 126), scale = 2^(e - R) and inv = 2^(R - e), so
+// m * inv < 2^R; rows below 2^-100 (and subnormal ones) count as zero
+template <int R>
 __device__ __forceinline__ void fixed_scale(float m, float& scale, float& inv) {
-  int e = 0;
-  frexpf(m, &e);  // m = f 2^e, 0.5 <= f < 1
-  if (!(m > 0.f) || e < -100) {
+  const int be = (__float_as_int(m) >> 23) & 0xff;
+  if (!(m > 0.f) || be < 26) {
     scale = inv = 0.f;
     return;
   }
-  scale = ldexpf(1.f, e - 7);
-  inv = ldexpf(1.f, 7 - e);
+  scale = __int_as_float((be - 126 - R + 127) << 23);
+  inv = __int_as_float((R - (be - 126) + 127) << 23);
 }
 
-// the six slice products of one 64-wide K chunk: leading x leading into acc0, the
-// rest into accR
-__device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t stage, int N, bool first) {
+// the six slice products of one 64-wide K chunk: leading x leading into the accumulator
+// at column acc0, the five others into the one at accR (first0 / firstR: start them)
+__device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t acc0, uint32_t accR, uint32_t stage, int N,
+                                                  bool first0, bool firstR) {
+  const uint32_t idesc = tc::idesc_f16(128, N);
+  uint64_t a[3], b[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    a[i] = tc::smem_desc_sw128(stage + i * kTileA);
+    b[i] = tc::smem_desc_sw128(stage + (3 + i) * kTileA);
+  }
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {  // 16 FP16 (32 bytes) per MMA
+    const uint64_t o = 2u * ks;
+    tc::mma_f16(tmem + acc0, a[0] + o, b[0] + o, idesc, (first0 && ks == 0) ? 0u : 1u);
+    tc::mma_f16(tmem + accR, a[0] + o, b[1] + o, idesc, (firstR && ks == 0) ? 0u : 1u);
+    tc::mma_f16(tmem + accR, a[1] + o, b[0] + o, idesc, 1u);
+    tc::mma_f16(tmem + accR, a[0] + o, b[2] + o, idesc, 1u);
+    tc::mma_f16(tmem + accR, a[1] + o, b[1] + o, idesc, 1u);
+    tc::mma_f16(tmem + accR, a[2] + o, b[0] + o, idesc, 1u);
+  }
+}
+
+// density: the six slice products of one 64-wide K chunk into four accumulators: s0 t0
+// (column 0), s0 t1 + s1 t0 (128), s1 t1 (256), s0 t2 + s2 t0 (384, in units of 2^12);
+// first starts them
+__device__ __forceinline__ void issue_density_chunk(uint32_t tmem, uint32_t stage, int N, bool first) {
   const uint32_t idesc = tc::idesc_f16(128, N);
   uint64_t a[3], b[3];
 #pragma unroll
@@ -220,12 +296,12 @@ __device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t stage,
   for (int ks = 0; ks < 4; ++ks) {  // 16 FP16 (32 bytes) per MMA
     const uint64_t o = 2u * ks;
     const uint32_t acc = (first && ks == 0) ? 0u : 1u;
-    tc::mma_f16(tmem + kColsAcc0, a[0] + o, b[0] + o, idesc, acc);
-    tc::mma_f16(tmem + kColsAccR, a[0] + o, b[1] + o, idesc, acc);
-    tc::mma_f16(tmem + kColsAccR, a[1] + o, b[0] + o, idesc, 1u);
-    tc::mma_f16(tmem + kColsAccR, a[0] + o, b[2] + o, idesc, 1u);
-    tc::mma_f16(tmem + kColsAccR, a[1] + o, b[1] + o, idesc, 1u);
-    tc::mma_f16(tmem + kColsAccR, a[2] + o, b[0] + o, idesc, 1u);
+    tc::mma_f16(tmem + 0, a[0] + o, b[0] + o, idesc, acc);
+    tc::mma_f16(tmem + 128, a[0] + o, b[1] + o, idesc, acc);
+    tc::mma_f16(tmem + 128, a[1] + o, b[0] + o, idesc, 1u);
+    tc::mma_f16(tmem + 256, a[1] + o, b[1] + o, idesc, acc);
+    tc::mma_f16(tmem + 384, a[0] + o, b[2] + o, idesc, acc);
+    tc::mma_f16(tmem + 384, a[2] + o, b[0] + o, idesc, 1u);
   }
 }
 
@@ -239,12 +315,13 @@ __global__ void __launch_bounds__(kT, 1)
   __shared__ double s_part[4][kQ - 1][128];
   __shared__ unsigned s_amax[128];  // per point: largest |phi| (FP32 bits)
   __shared__ float s_bscale[kNT];   // per function nu of the pass: scale of its column of P
+  __shared__ long s_rowoff[kNT];    // and the offset of that column
   const uint32_t base_s = tc::smem_u32(smem_raw);
   uint8_t* sm = smem_raw + ((1024 - (base_s & 1023)) & 1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int p = tid & 127, quarter = tid >> 7;  // point (TMEM lane), and which of its kQ threads
   const int c0 = 32 * quarter;                  // this thread's 32 accumulator columns
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
   if (tid == 0) {
     tc::mbar_init(&mbar[0], 1);
     tc::mbar_init(&mbar[1], 1);
@@ -279,12 +356,12 @@ __global__ void __launch_bounds__(kT, 1)
     const int nact = P.fn_off[b + 1] - P.fn_off[b];
     const int* __restrict__ fn = P.fn_list + P.fn_off[b];
     const int s0 = P.sh_off[b], s1 = P.sh_off[b + 1];
-    if (4L * nact * 128 > bt.cta_floats) {  // scratch sized for a smaller block: report, skip
+    if (5L * nact * 128 > bt.cta_floats) {  // scratch sized for a smaller block: report, skip
       if (tid == 0) atomicExch(err, kErrScratch);
       continue;
     }
     const bool live = p < npts;
-    const long cs = (long)nact * 128;  // component stride of the scratch
+    const long cs = (long)nact * 128;  // plane stride of the scratch: value, its low part, gradient
     // ---- 1. basis values (and gradients) of the block, largest |phi| per point ----
     {
       const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
@@ -297,28 +374,30 @@ __global__ void __launch_bounds__(kT, 1)
         const ShellRec r = next;
         if (si + kQ < s1) next = load_rec(P.rec + si + kQ);  // in flight while r is evaluated
         float* const t0 = col + (long)rec_f0(r.info) * 128;
-        auto put = [&](int f, float v, float dx, float dy, float dz) {
+        float rlo = 0.f;
+        auto put = [&](int f, float v, float vl, float dx, float dy, float dz) {
           float* t = t0 + f * 128;
           t[0] = v;
+          t[cs] = fmaf(v, rlo, vl);  // the value's low part: radial factor's and coefficients'
           vmax = fmaxf(vmax, fabsf(v));
           if (DERIV) {
-            t[cs] = dx;
-            t[2 * cs] = dy;
-            t[3 * cs] = dz;
+            t[2 * cs] = dx;
+            t[3 * cs] = dy;
+            t[4 * cs] = dz;
           }
         };
         if (live) {
-          shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, put);
+          shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, &rlo, put);
         } else {
           const int nf = rec_nf(r.info);
-          for (int f = 0; f < nf; ++f) put(f, 0.f, 0.f, 0.f, 0.f);
+          for (int f = 0; f < nf; ++f) put(f, 0.f, 0.f, 0.f, 0.f, 0.f);
         }
       }
       atomicMax(&s_amax[p], __float_as_uint(vmax));  // non-negative floats order as integers
     }
     __syncthreads();
     float sa, inva;  // this point's row scale
-    fixed_scale(__uint_as_float(s_amax[p]), sa, inva);
+    fixed_scale<5>(__uint_as_float(s_amax[p]), sa, inva);
     const int nkc = (nact + 63) / 64;
     for (int s = 0; s < nspin; ++s) {
       const uint2* __restrict__ Psl = I.Psl + (long)s * nbf * nbf;
@@ -327,7 +406,12 @@ __global__ void __launch_bounds__(kT, 1)
       for (int nu0 = 0; nu0 < nact; nu0 += kNT) {
         const int nnu = min(kNT, nact - nu0);
         const int N = (nnu + 15) & ~15;
-        if (tid < nnu) s_bscale[tid] = __ldg(Pcs + __ldg(fn + nu0 + tid));
+        if (tid < nnu) {
+          const int f = __ldg(fn + nu0 + tid);
+          s_bscale[tid] = __ldg(Pcs + f);
+          s_rowoff[tid] = (long)f * nbf;
+        }
+        __syncthreads();  // the B fill of the pass's first chunk reads s_rowoff
         for (int kc = 0; kc < nkc; ++kc) {
           const int st = gc & 1;
           if ((pend >> st) & 1u) {  // the MMAs of two chunks ago still read this stage
@@ -342,51 +426,69 @@ __global__ void __launch_bounds__(kT, 1)
           uint8_t* const stage = sm + st * kDStageBytes;
           const int mu0 = kc * 64;
           // ---- A: row p, 16-byte chunks j = 2 quarter, 2 quarter + 1 (8 functions each) ----
-#pragma unroll 1
-          for (int jj = 0; jj < 2; ++jj) {
-            const int j = 2 * quarter + jj;
-            uint32_t w0[4], w1[4], w2[4];
+          {
+            float av[16], al[16];  // all loads in flight before any is used
 #pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-              uint16_t a0, a1, a2, b0, b1, b2;
-              const int mu = mu0 + 8 * j + e;
-              fixed_slices(mu < nact ? __fmul_rn(my[(long)mu * 128 + p], inva) : 0.f, a0, a1, a2);
-              fixed_slices(mu + 1 < nact ? __fmul_rn(my[(long)(mu + 1) * 128 + p], inva) : 0.f, b0, b1, b2);
-              w0[e >> 1] = (uint32_t)a0 | ((uint32_t)b0 << 16);
-              w1[e >> 1] = (uint32_t)a1 | ((uint32_t)b1 << 16);
-              w2[e >> 1] = (uint32_t)a2 | ((uint32_t)b2 << 16);
+            for (int e = 0; e < 16; ++e) {
+              const int mu = mu0 + 16 * quarter + e;
+              av[e] = mu < nact ? my[(long)mu * 128 + p] : 0.f;
+              al[e] = mu < nact ? my[cs + (long)mu * 128 + p] : 0.f;
             }
-            const uint32_t off = (uint32_t)(p * 128 + ((j ^ (p & 7)) << 4));
-            *reinterpret_cast<uint4*>(stage + off) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
-            *reinterpret_cast<uint4*>(stage + kTileA + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
-            *reinterpret_cast<uint4*>(stage + 2 * kTileA + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+#pragma unroll
+            for (int jj = 0; jj < 2; ++jj) {
+              const int j = 2 * quarter + jj;
+              uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+              for (int e = 0; e < 8; e += 2) {
+                uint16_t a0, a1, a2, b0, b1, b2;
+                const int k = 8 * jj + e;
+                density_slices(__fmul_rn(av[k], inva), __fmul_rn(al[k], inva), a0, a1, a2);
+                density_slices(__fmul_rn(av[k + 1], inva), __fmul_rn(al[k + 1], inva), b0, b1, b2);
+                w0[e >> 1] = (uint32_t)a0 | ((uint32_t)b0 << 16);
+                w1[e >> 1] = (uint32_t)a1 | ((uint32_t)b1 << 16);
+                w2[e >> 1] = (uint32_t)a2 | ((uint32_t)b2 << 16);
+              }
+              const uint32_t off = (uint32_t)(p * 128 + ((j ^ (p & 7)) << 4));
+              *reinterpret_cast<uint4*>(stage + off) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+              *reinterpret_cast<uint4*>(stage + kTileA + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+              *reinterpret_cast<uint4*>(stage + 2 * kTileA + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+            }
           }
-          // ---- B: row nu, elements mu0 + 2 lane, + 1: P[fn[mu]][fn[nu]] (symmetric P) ----
+          // ---- B: row nu, elements mu0 + 2 lane, + 1: P[fn[mu]][fn[nu]] (symmetric P); a
+          //      warp's rows (at most 8) loaded together, row offsets from shared memory ----
           {
             const int k0 = 2 * lane;
             const int muA = mu0 + k0, muB = muA + 1;
             const long cA = muA < nact ? (long)__ldg(fn + muA) : -1;
             const long cB = muB < nact ? (long)__ldg(fn + muB) : -1;
-#pragma unroll 4
-            for (int row = warp; row < N; row += kWarps) {
-              uint2 ea = make_uint2(0u, 0u), eb = make_uint2(0u, 0u);
+            uint2 ea[kNT / kWarps], eb[kNT / kWarps];
+#pragma unroll
+            for (int k = 0; k < kNT / kWarps; ++k) {
+              const int row = warp + k * kWarps;
+              ea[k] = eb[k] = make_uint2(0u, 0u);
               if (row < nnu) {
-                const uint2* prow = Psl + (long)__ldg(fn + nu0 + row) * nbf;
-                if (cA >= 0) ea = __ldg(prow + cA);
-                if (cB >= 0) eb = __ldg(prow + cB);
+                const uint2* prow = Psl + s_rowoff[row];
+                if (cA >= 0) ea[k] = __ldg(prow + cA);
+                if (cB >= 0) eb[k] = __ldg(prow + cB);
               }
-              const uint32_t off = tc::swz_offset_h(row, k0);
-              *reinterpret_cast<uint32_t*>(stage + 3 * kTileA + off) = (ea.x & 0xFFFFu) | (eb.x << 16);
-              *reinterpret_cast<uint32_t*>(stage + 4 * kTileA + off) = (ea.x >> 16) | (eb.x & 0xFFFF0000u);
-              *reinterpret_cast<uint32_t*>(stage + 5 * kTileA + off) = (ea.y & 0xFFFFu) | (eb.y << 16);
+            }
+#pragma unroll
+            for (int k = 0; k < kNT / kWarps; ++k) {
+              const int row = warp + k * kWarps;
+              if (row < N) {
+                const uint32_t off = tc::swz_offset_h(row, k0);
+                *reinterpret_cast<uint32_t*>(stage + 3 * kTileA + off) = (ea[k].x & 0xFFFFu) | (eb[k].x << 16);
+                *reinterpret_cast<uint32_t*>(stage + 4 * kTileA + off) = (ea[k].x >> 16) | (eb[k].x & 0xFFFF0000u);
+                *reinterpret_cast<uint32_t*>(stage + 5 * kTileA + off) = (ea[k].y & 0xFFFFu) | (eb[k].y << 16);
+              }
             }
           }
           tc::fence_async_smem();
           __syncthreads();
-          const bool wfirst = (kc % kWinChunks) == 0;
+          const int kw = kc % kWinChunks;  // chunk within the window
           if (tid == 0) {
             tc::fence_after_sync();
-            issue_fixed_chunk(tmem, tc::smem_u32(stage), N, wfirst);
+            issue_density_chunk(tmem, tc::smem_u32(stage), N, kw == 0);
             tc::mma_commit(&mbar[st]);
           }
           pend |= 1u << st;
@@ -412,22 +514,27 @@ __global__ void __launch_bounds__(kT, 1)
             const float* t = my + (long)nu0 * 128 + p;
 #pragma unroll 1
             for (int cb = c0; cb < c0 + 32; cb += 8) {
-              float a0[8], ar[8];
-              tc::tmem_ld8(tmem + trow + kColsAcc0 + cb, a0);
-              tc::tmem_ld8(tmem + trow + kColsAccR + cb, ar);
+              float a0[8], a1[8], ar[8], a3[8];
+              tc::tmem_ld8(tmem + trow + cb, a0);
+              tc::tmem_ld8(tmem + trow + 128 + cb, a1);
+              tc::tmem_ld8(tmem + trow + 256 + cb, ar);
+              tc::tmem_ld8(tmem + trow + 384 + cb, a3);
+#pragma unroll
+              for (int c = 0; c < 8; ++c)
+                ar[c] = __fadd_rn(__fadd_rn(a0[c], a1[c]), fmaf(a3[c], 1.f / 4096.f, ar[c]));
               if (live) {
                 float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
                   const int col = cb + c;
                   if (col < nnu) {
-                    const float xv = __fmul_rn(__fadd_rn(a0[c], ar[c]), __fmul_rn(sa, s_bscale[col]));
+                    const float xv = __fmul_rn(ar[c], __fmul_rn(sa, s_bscale[col]));
                     const float* tc_ = t + (long)col * 128;
-                    rr = fmaf(xv, tc_[0], rr);
+                    rr = fmaf(xv, tc_[cs], fmaf(xv, tc_[0], rr));
                     if (DERIV) {
-                      gx = fmaf(xv, tc_[cs], gx);
-                      gy = fmaf(xv, tc_[2 * cs], gy);
-                      gz = fmaf(xv, tc_[3 * cs], gz);
+                      gx = fmaf(xv, tc_[2 * cs], gx);
+                      gy = fmaf(xv, tc_[3 * cs], gy);
+                      gz = fmaf(xv, tc_[4 * cs], gz);
                     }
                   }
                 }
@@ -476,7 +583,7 @@ done:
     if ((pend >> q) & 1u) wait_or_abort(&mbar[q], (phase >> q) & 1u, err);
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // =====================================================================================
@@ -597,7 +704,7 @@ __global__ void __launch_bounds__(kT, 1)
           const ShellRec r = next;
           if (si + kQ < s1) next = load_rec(P.rec + si + kQ);  // in flight while r is evaluated
           float* const t0 = col + (long)rec_f0(r.info) * 128;
-          auto put = [&](int f, float val, float dx, float dy, float dz) {
+          auto put = [&](int f, float val, float, float dx, float dy, float dz) {
             float* t = t0 + f * 128;
             t[0] = val;
             if (sp0) {
@@ -611,7 +718,8 @@ __global__ void __launch_bounds__(kT, 1)
               t[2 * rows_pad * 128] = gv;
             }
           };
-          shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, put);
+          float rlo;  // the adder's operands are sliced from FP32 values
+          shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, &rlo, put);
         }
       }
     }
@@ -620,32 +728,63 @@ __global__ void __launch_bounds__(kT, 1)
     {
       const int nop = 1 + __popc(smask);
       const int k4 = 4 * lane;  // this lane's 4 points
-      for (int r = warp; r < nop * nact; r += kWarps) {
-        const int oi = r / nact, m = r - oi * nact;
-        const int o = oi == 0 ? 0 : (smask == 2 ? 2 : oi);
-        float4 v = *reinterpret_cast<const float4*>(stg + ((long)o * rows_pad + m) * 128 + k4);
-        if (k4 + 0 >= npts) v.x = 0.f;
-        if (k4 + 1 >= npts) v.y = 0.f;
-        if (k4 + 2 >= npts) v.z = 0.f;
-        if (k4 + 3 >= npts) v.w = 0.f;
-        float mx = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+      const int nrows = nop * nact;
+      // four rows per pass, their loads issued together (the rows were just written:
+      // L2 latency, not bandwidth, bounds this loop)
+      int oi0 = 0, m0 = warp;  // row r0 = oi0 * nact + m0
+      while (m0 >= nact) {
+        m0 -= nact;
+        ++oi0;
+      }
+      for (int r0 = warp; r0 < nrows; r0 += 4 * kWarps) {
+        float4 v[4];
+        int ou[4], mu[4];
+        {
+          int oi = oi0, m = m0;
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
-        float scale, inv;
-        fixed_scale(mx, scale, inv);
-        if (lane == 0) scl[o * rows_pad + m] = scale;
-        uint16_t h[3][4];
-        fixed_slices(__fmul_rn(v.x, inv), h[0][0], h[1][0], h[2][0]);
-        fixed_slices(__fmul_rn(v.y, inv), h[0][1], h[1][1], h[2][1]);
-        fixed_slices(__fmul_rn(v.z, inv), h[0][2], h[1][2], h[2][2]);
-        fixed_slices(__fmul_rn(v.w, inv), h[0][3], h[1][3], h[2][3]);
-        uint8_t* tb = reinterpret_cast<uint8_t*>(tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 *
-                                                            kTileFloats);
-        const uint32_t off = tc::swz_offset_h(m & 127, k4 & 63);
+          for (int u = 0; u < 4; ++u) {
+            ou[u] = oi == 0 ? 0 : (smask == 2 ? 2 : oi);
+            mu[u] = m;
+            v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r0 + u * kWarps < nrows)
+              v[u] = *reinterpret_cast<const float4*>(stg + ((long)ou[u] * rows_pad + m) * 128 + k4);
+            m += kWarps;
+            while (m >= nact) {
+              m -= nact;
+              ++oi;
+            }
+          }
+          oi0 = oi;
+          m0 = m;
+        }
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
-          *reinterpret_cast<uint2*>(tb + i * kTileA + off) =
-              make_uint2((uint32_t)h[i][0] | ((uint32_t)h[i][1] << 16), (uint32_t)h[i][2] | ((uint32_t)h[i][3] << 16));
+        for (int u = 0; u < 4; ++u) {
+          if (r0 + u * kWarps >= nrows) break;  // warp-uniform
+          const int o = ou[u], m = mu[u];
+          float4 x = v[u];
+          if (k4 + 0 >= npts) x.x = 0.f;
+          if (k4 + 1 >= npts) x.y = 0.f;
+          if (k4 + 2 >= npts) x.z = 0.f;
+          if (k4 + 3 >= npts) x.w = 0.f;
+          float mx = fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fmaxf(fabsf(x.z), fabsf(x.w)));
+#pragma unroll
+          for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+          float scale, inv;
+          fixed_scale<7>(mx, scale, inv);
+          if (lane == 0) scl[o * rows_pad + m] = scale;
+          uint16_t h[3][4];
+          fixed_slices<7, 8>(__fmul_rn(x.x, inv), h[0][0], h[1][0], h[2][0]);
+          fixed_slices<7, 8>(__fmul_rn(x.y, inv), h[0][1], h[1][1], h[2][1]);
+          fixed_slices<7, 8>(__fmul_rn(x.z, inv), h[0][2], h[1][2], h[2][2]);
+          fixed_slices<7, 8>(__fmul_rn(x.w, inv), h[0][3], h[1][3], h[2][3]);
+          uint8_t* tb = reinterpret_cast<uint8_t*>(tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 *
+                                                              kTileFloats);
+          const uint32_t off = tc::swz_offset_h(m & 127, k4 & 63);
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+            *reinterpret_cast<uint2*>(tb + i * kTileA + off) = make_uint2(
+                (uint32_t)h[i][0] | ((uint32_t)h[i][1] << 16), (uint32_t)h[i][2] | ((uint32_t)h[i][3] << 16));
+        }
       }
       tc::fence_async_global();  // these generic writes are read by the bulk copies below
     }
@@ -704,7 +843,8 @@ __global__ void __launch_bounds__(kT, 1)
           int spin, a, bb, ph, kc;
           decode(i, spin, a, bb, ph, kc);
           const int N = (min(128, nact - 128 * bb) + 15) & ~15;
-          issue_fixed_chunk(tmem + (ph ? 256u : 0u), tc::smem_u32(sm + st * kDStageBytes), N, kc == 0);
+          issue_fixed_chunk(tmem, ph ? 256u : 0u, ph ? 384u : 128u, tc::smem_u32(sm + st * kDStageBytes), N, kc == 0,
+                            kc == 0);
           tc::mma_commit(&mdone[st]);
           last_mma = J;
           // the stage of step i - 1 (same pair) is free once its MMAs are done: refill it
@@ -779,8 +919,8 @@ done:
 
 // Fixed-point slices of the density matrices, once per build: one CTA per (spin,
 // column j) finds the column's largest |P_ij|, its power-of-two scale (the largest
-// scaled element below 128) and the three FP16 slices of every scaled element (taken
-// from the FP64 value, so P enters to 2^-24 of its column maximum).
+// scaled element below 32) and the three FP16 slices of density_slices of every scaled
+// element, taken from the FP64 value, so P enters to 2^-30 of its column maximum.
 __global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__ P, uint2* __restrict__ out,
                                                       float* __restrict__ colscale, int nbf) {
   __shared__ double red[8];
@@ -797,17 +937,17 @@ __global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__
   int e = 0;
   frexp(m, &e);
   const bool zero = !(m > 0.0) || e < -100;
-  const double inv = zero ? 0.0 : ldexp(1.0, 7 - e);
-  if (threadIdx.x == 0) colscale[c] = zero ? 0.f : ldexpf(1.f, e - 7);
+  const double inv = zero ? 0.0 : ldexp(1.0, 5 - e);
+  if (threadIdx.x == 0) colscale[c] = zero ? 0.f : ldexpf(1.f, e - 5);
   for (int i = threadIdx.x; i < nbf; i += blockDim.x) {
-    const double v = col[i] * inv;  // |v| < 128, exact
+    const double v = col[i] * inv;  // |v| < 32, exact
     const double s0 = rint(v);
-    const double r1 = (v - s0) * 256.0;
+    const double r1 = (v - s0) * 4096.0;
     const double s1 = rint(r1);
-    const double s2 = rint((r1 - s1) * 256.0);
+    const double s2 = rint((r1 - s1) * 4096.0);
     const uint32_t h0 = __half_as_ushort(__float2half_rn((float)s0));
-    const uint32_t h1 = __half_as_ushort(__float2half_rn((float)(s1 * (1.0 / 256.0))));
-    const uint32_t h2 = __half_as_ushort(__float2half_rn((float)(s2 * (1.0 / 65536.0))));
+    const uint32_t h1 = __half_as_ushort(__float2half_rn((float)(s1 * (1.0 / 4096.0))));
+    const uint32_t h2 = __half_as_ushort(__float2half_rn((float)(s2 * (1.0 / 4096.0))));
     o[i] = make_uint2(h0 | (h1 << 16), h2);
   }
 }
@@ -861,7 +1001,7 @@ static void fill_item(MxItem& it, const MixedWork& w) {
   it.V = w.V;
 }
 
-// Scratch floats per CTA for the items [i0, i1): the density's [4][n_b][128] values,
+// Scratch floats per CTA for the items [i0, i1): the density's [5][n_b][128] values,
 // and per adder operand (Phi, G per spin) the FP32 rows, the slice tiles and the row
 // scales of ft_max 128-function tiles.
 static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t i1, int* ft_max) {
@@ -872,7 +1012,7 @@ static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t
   }
   const int ft = std::max(1, (amax + 127) / 128);
   *ft_max = ft;
-  const long dens = 4L * amax * 128;
+  const long dens = 5L * amax * 128;
   const long add = (long)(1 + smax) * ft * (128L * 128 + kOpTileFloats + 128);
   return (std::max(dens, add) + 63) & ~63L;
 }
