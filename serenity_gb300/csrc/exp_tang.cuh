@@ -46,26 +46,33 @@ __device__ __forceinline__ float exp_tang(float x) {
   return m < -125 ? 0.f : __fmul_rn(v, __int_as_float((m + 127) << 23));
 }
 
-// the same value as an FP32 pair, exp(x) = hi + lo to ~2^-30: hi is exp_tang(x) (the
-// rounded value), lo the remainder (|lo| <= ulp(hi) / 2); for sums that must not inherit
-// the rounding of each exp
+// the same value as an FP32 pair, exp(x) = hi + lo to ~2^-36: hi is the rounded value,
+// lo the remainder (|lo| <= ulp(hi) / 2); for sums that must not inherit the rounding of
+// each exp.  The reduced argument is kept as a pair (kf ln2/32 by an exact product and
+// a two-sum), T_hi r as an exact product, and the pieces are added largest first.
 __device__ __forceinline__ void exp_tang2(float x, float& hi, float& lo) {
   x = fmaxf(x, -104.f);
   const float kf = rintf(__fmul_rn(x, 46.16624f));
   const int k = (int)kf;
   const int j = k & 31, m = k >> 5;
-  float r = fmaf(-kf, 0x1.63p-6f, x);
-  r = fmaf(-kf, -0x1.bd0106p-18f, r);
-  r = fmaf(-kf, 0x1.cf79acp-45f, r);
-  const float q = __fmul_rn(__fmul_rn(r, r), fmaf(r, fmaf(r, 1.f / 24.f, 1.f / 6.f), 0.5f));
-  const float u = __fadd_rn(r, q);
+  const float r1 = fmaf(-kf, 0x1.63p-6f, x);  // exact
+  const float p = __fmul_rn(kf, -0x1.bd0106p-18f), pe = fmaf(kf, -0x1.bd0106p-18f, -p);
+  const float rh = __fsub_rn(r1, p);  // two-sum r1 - p
+  const float bp = __fsub_rn(rh, r1);
+  const float re = __fadd_rn(__fsub_rn(r1, __fsub_rn(rh, bp)), __fsub_rn(-p, bp));
+  const float rl = fmaf(-kf, 0x1.cf79acp-45f, __fsub_rn(re, pe));  // r = rh + rl
+  const float q = __fmul_rn(__fmul_rn(rh, rh), fmaf(rh, fmaf(rh, 1.f / 24.f, 1.f / 6.f), 0.5f));
   const float2 T = __ldg(kExp2Tab + j);
-  const float c = fmaf(T.x, u, T.y);  // |c| < T.x / 64
-  const float h = __fadd_rn(T.x, c);
-  const float l = __fsub_rn(c, __fsub_rn(h, T.x));  // exact: T.x + c = h + l
+  // T (1 + r + q) = T.x + T.x rh + [T.x (rl + q) + T.y (1 + rh + q)]
+  const float ph = __fmul_rn(T.x, rh), phe = fmaf(T.x, rh, -ph);
+  const float small = fmaf(T.x, __fadd_rn(rl, q), fmaf(T.y, __fadd_rn(rh, q), T.y));
+  const float h = __fadd_rn(T.x, ph);
+  const float l = __fadd_rn(__fsub_rn(ph, __fsub_rn(h, T.x)), __fadd_rn(phe, small));
+  const float h2 = __fadd_rn(h, l);
+  const float l2 = __fsub_rn(l, __fsub_rn(h2, h));
   const float sc = m < -125 ? 0.f : __int_as_float((m + 127) << 23);
-  hi = __fmul_rn(h, sc);
-  lo = __fmul_rn(l, sc);
+  hi = __fmul_rn(h2, sc);
+  lo = __fmul_rn(l2, sc);
 }
 
 }  // namespace xcgpu

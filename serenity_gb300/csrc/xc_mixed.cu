@@ -189,17 +189,15 @@ __device__ __forceinline__ const MxItem& locate(const MxBatch& bt, int gb, int& 
 //   up to an ulp per accumulation step, always towards zero, which shows as a systematic
 //   density deficit (about -6e-8 relative with 3xTF32 operands).  Here both operands are
 //   fixed point: each row of A = Phi (one point) and each column of B = P (one function
-//   nu) is scaled by a power of two that brings its largest element below 32 and cut
-//   into a 6-bit and two 12-bit slices (density_slices, 30 bits).  Per window of two
-//   64-wide K chunks, the leading products (integers below 2^10) and the first-order
-//   products s0 t1 + s1 t0 (below 2^17 units of 2^-12, sum below 2^24) each have an
-//   accumulator whose sums are exact in FP32 whatever the rounding of the adder tree:
-//   the first-order terms carry the elements below 2^-6 of their row or column maximum
-//   (those have s0 = 0), whose signs follow X's.  The second-order products s1 t1 and
-//   s0 t2 + s2 t0 (at most 2^-12 of the leading ones; the last with s2 stored as a
-//   multiple of 2^-12, so every FP16 operand is a normal number) have one accumulator
-//   each.  The slices are stored pre-scaled as FP16 (exact) and multiplied with
-//   kind::f16 MMAs.
+//   nu) is scaled by a power of two that brings its largest element below 256 and cut
+//   into three 9-bit slices (density_slices, 27 bits).  Per window of two 64-wide K
+//   chunks the products go to four accumulators by order, s0 t0 (integers, sum below
+//   2^23), s0 t1 + s1 t0 (sum below 2^24 units of 2^-9), s1 t1 (below 2^23 units of
+//   2^-18) and s0 t2 + s2 t0 (below 2^24 units of 2^-18, with s2 stored as a multiple of
+//   2^-9 so that every FP16 operand is a normal number): all four sums are exact in FP32
+//   whatever the rounding of the tensor core's adder tree, and only the third-order
+//   products (below 2^-27 of the leading ones) are left out.  The slices are stored
+//   pre-scaled as FP16 (exact) and multiplied with kind::f16 MMAs.
 //   1. every active shell of the block is evaluated once (value with its low part and,
 //      for GGA, gradient) into the CTA's scratch, FP32, [plane][function][128 points],
 //      with the largest |phi| of each point;
@@ -230,18 +228,52 @@ __device__ __forceinline__ void fixed_slices(float v, uint16_t& h0, uint16_t& h1
   h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, down2)));
 }
 
-// Density slices of v = vh + vl (|vl| at most about an ulp of vh) scaled into (-32, 32):
-// v = s0 + s1 / 2^12 + s2 / 2^24 + r, s0 in [-32, 32], s1, s2 in [-2048, 2048], |r| <=
-// 2^-25; stored as FP16 (s0, s1 / 2^12, s2 / 2^12), all exact and (but zero) normal
-// numbers: the s2 products are accumulated apart and scaled by 2^-12 when read.
-__device__ __forceinline__ void density_slices(float vh, float vl, uint16_t& h0, uint16_t& h1, uint16_t& h2) {
+// fixed_slices of v = vh + vl (|vl| at most about an ulp of vh): the remainder after s0
+// takes vl in
+template <int R, int B>
+__device__ __forceinline__ void fixed_slices2(float vh, float vl, uint16_t& h0, uint16_t& h1, uint16_t& h2) {
+  constexpr float up = (float)(1 << B), down = 1.f / (float)(1 << B), down2 = down * down;
   const float s0 = rintf(vh);
-  const float r1 = __fmul_rn(__fadd_rn(__fsub_rn(vh, s0), vl), 4096.f);
+  const float r1 = __fmul_rn(__fadd_rn(__fsub_rn(vh, s0), vl), up);
   const float s1 = rintf(r1);
-  const float s2 = rintf(__fmul_rn(__fsub_rn(r1, s1), 4096.f));
+  const float s2 = rintf(__fmul_rn(__fsub_rn(r1, s1), up));
   h0 = __half_as_ushort(__float2half_rn(s0));
-  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, 1.f / 4096.f)));
-  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, 1.f / 4096.f)));
+  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, down)));
+  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, down2)));
+}
+
+// Density slices of v = vh + vl (|vl| at most about an ulp of vh) scaled into (-256, 256):
+// v = s0 + s1 / 2^9 + s2 / 2^18 + r, s0 in [-256, 256], s1, s2 in [-256, 256], |r| <
+// 2^-18; stored as FP16 (s0, s1 / 2^9, s2 / 2^9), all exact and (but zero) normal
+// numbers: the s2 products are accumulated apart and scaled by 2^-9 when read.  The last
+// digit is rounded stochastically, s2 = floor(r2 + u) with a dither u in [0, 1)
+// (Connolly, Higham & Mary, SIAM J. Sci. Comput. 43 (2021) A1508): an s function has the
+// same value at every point of a radial shell of its atom (and at every atom of the
+// element), where round-to-nearest would repeat one error; the dither makes it zero-mean.
+__device__ __forceinline__ void density_slices(float vh, float vl, float u, uint16_t& h0, uint16_t& h1,
+                                               uint16_t& h2) {
+  const float s0 = rintf(vh);
+  const float r1 = __fmul_rn(__fadd_rn(__fsub_rn(vh, s0), vl), 512.f);
+  const float s1 = rintf(r1);
+  const float s2 = floorf(__fadd_rn(__fmul_rn(__fsub_rn(r1, s1), 512.f), u));
+  h0 = __half_as_ushort(__float2half_rn(s0));
+  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, 1.f / 512.f)));
+  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, 1.f / 512.f)));
+}
+
+// dither of point g (global index): a hash to [0, 1); a function mu adds mu times the
+// golden ratio (mod 1), so the dithers of one point are spread evenly
+__device__ __forceinline__ float point_dither(uint32_t g) {
+  g ^= g >> 16;
+  g *= 0x7feb352dU;
+  g ^= g >> 15;
+  g *= 0x846ca68bU;
+  g ^= g >> 16;
+  return (float)(g >> 8) * (1.f / 16777216.f);
+}
+__device__ __forceinline__ float function_dither(float up, int mu) {
+  const float x = fmaf((float)mu, 0.6180339887f, up);
+  return __fsub_rn(x, floorf(x));
 }
 
 // power-of-two scale of a row or column with largest magnitude m >= 0: with m = f 2^e,
@@ -282,7 +314,7 @@ __device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t acc0, 
 }
 
 // density: the six slice products of one 64-wide K chunk into four accumulators: s0 t0
-// (column 0), s0 t1 + s1 t0 (128), s1 t1 (256), s0 t2 + s2 t0 (384, in units of 2^12);
+// (column 0), s0 t1 + s1 t0 (128), s1 t1 (256), s0 t2 + s2 t0 (384, in units of 2^9);
 // first starts them
 __device__ __forceinline__ void issue_density_chunk(uint32_t tmem, uint32_t stage, int N, bool first) {
   const uint32_t idesc = tc::idesc_f16(128, N);
@@ -397,7 +429,8 @@ __global__ void __launch_bounds__(kT, 1)
     }
     __syncthreads();
     float sa, inva;  // this point's row scale
-    fixed_scale<5>(__uint_as_float(s_amax[p]), sa, inva);
+    fixed_scale<8>(__uint_as_float(s_amax[p]), sa, inva);
+    const float up = point_dither((uint32_t)(first + p));
     const int nkc = (nact + 63) / 64;
     for (int s = 0; s < nspin; ++s) {
       const uint2* __restrict__ Psl = I.Psl + (long)s * nbf * nbf;
@@ -441,9 +474,10 @@ __global__ void __launch_bounds__(kT, 1)
 #pragma unroll
               for (int e = 0; e < 8; e += 2) {
                 uint16_t a0, a1, a2, b0, b1, b2;
-                const int k = 8 * jj + e;
-                density_slices(__fmul_rn(av[k], inva), __fmul_rn(al[k], inva), a0, a1, a2);
-                density_slices(__fmul_rn(av[k + 1], inva), __fmul_rn(al[k + 1], inva), b0, b1, b2);
+                const int k = 8 * jj + e, mu = mu0 + 16 * quarter + k;
+                density_slices(__fmul_rn(av[k], inva), __fmul_rn(al[k], inva), function_dither(up, mu), a0, a1, a2);
+                density_slices(__fmul_rn(av[k + 1], inva), __fmul_rn(al[k + 1], inva), function_dither(up, mu + 1), b0,
+                               b1, b2);
                 w0[e >> 1] = (uint32_t)a0 | ((uint32_t)b0 << 16);
                 w1[e >> 1] = (uint32_t)a1 | ((uint32_t)b1 << 16);
                 w2[e >> 1] = (uint32_t)a2 | ((uint32_t)b2 << 16);
@@ -521,7 +555,7 @@ __global__ void __launch_bounds__(kT, 1)
               tc::tmem_ld8(tmem + trow + 384 + cb, a3);
 #pragma unroll
               for (int c = 0; c < 8; ++c)
-                ar[c] = __fadd_rn(__fadd_rn(a0[c], a1[c]), fmaf(a3[c], 1.f / 4096.f, ar[c]));
+                ar[c] = __fadd_rn(__fadd_rn(a0[c], a1[c]), fmaf(a3[c], 1.f / 512.f, ar[c]));
               if (live) {
                 float rr = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
@@ -591,7 +625,8 @@ done:
 // FP64 red.add on and above the diagonal (ScalarOperatorToMatrixAdder.cpp:224-303).  The
 // leading slice products are accumulated exactly, as in the density:
 //   1a. every active shell of the block is evaluated once; Phi and G (per spin) go to
-//       the CTA's scratch in FP32, [operand][function][128 points];
+//       the CTA's scratch in FP32 with their low parts, [part][operand][function][128
+//       points];
 //   1b. one warp per (operand, function) row: the row's largest |value| over the block's
 //       points sets its power-of-two scale (kept in the scratch), and the three FP16
 //       slices of the scaled row go to the scratch as operand tiles (128 functions x 64
@@ -638,8 +673,8 @@ __global__ void __launch_bounds__(kT, 1)
   int last_copy = -1, last_mma = -1;     // thread 0: highest step copied / issued
   float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
   const long rows_pad = (long)bt.ft_max * 128;
-  float* const stg = my;                               // [NOPS][rows_pad][128]
-  float* const tiles = stg + NOPS * rows_pad * 128;    // [NOPS][ft_max][2 chunks][3 slices][4096]
+  float* const stg = my;                               // [2][NOPS][rows_pad][128]: values, low parts
+  float* const tiles = stg + 2 * NOPS * rows_pad * 128;  // [NOPS][ft_max][2 chunks][3 slices][4096]
   float* const scl = tiles + NOPS * bt.ft_max * kOpTileFloats;  // [NOPS][rows_pad]
 
   for (;;) {
@@ -664,7 +699,7 @@ __global__ void __launch_bounds__(kT, 1)
     if (smask == 0 || nact == 0) continue;
     const int nft = (nact + 127) >> 7, nkc = (npts + 63) >> 6;
     if (nft > bt.ft_max || nspin > NOPS - 1 ||
-        (long)NOPS * (rows_pad * 128 + bt.ft_max * kOpTileFloats + rows_pad) > bt.cta_floats) {
+        (long)NOPS * (2 * rows_pad * 128 + bt.ft_max * kOpTileFloats + rows_pad) > bt.cta_floats) {
       if (tid == 0) atomicExch(err, kErrScratch);  // scratch sized for a smaller block: report, skip
       continue;
     }
@@ -704,21 +739,28 @@ __global__ void __launch_bounds__(kT, 1)
           const ShellRec r = next;
           if (si + kQ < s1) next = load_rec(P.rec + si + kQ);  // in flight while r is evaluated
           float* const t0 = col + (long)rec_f0(r.info) * 128;
-          auto put = [&](int f, float val, float, float dx, float dy, float dz) {
+          float rlo = 0.f;
+          const long lo = (long)NOPS * rows_pad * 128;  // plane offset of the low parts
+          // Phi and G with the low part of the value (radial factor's and coefficients',
+          // the same at every point of a radial shell); the gradient terms stay FP32
+          auto put = [&](int f, float val, float vl, float dx, float dy, float dz) {
             float* t = t0 + f * 128;
+            const float vlo = fmaf(val, rlo, vl);
             t[0] = val;
+            t[lo] = vlo;
             if (sp0) {
               float gv = wsp[0][0] * val;
               if (DERIV) gv += wsp[0][1] * dx + wsp[0][2] * dy + wsp[0][3] * dz;
               t[rows_pad * 128] = gv;
+              t[lo + rows_pad * 128] = __fmul_rn(wsp[0][0], vlo);
             }
             if (TWO_SPINS && sp1) {
               float gv = wsp[NS - 1][0] * val;
               if (DERIV) gv += wsp[NS - 1][1] * dx + wsp[NS - 1][2] * dy + wsp[NS - 1][3] * dz;
               t[2 * rows_pad * 128] = gv;
+              t[lo + 2 * rows_pad * 128] = __fmul_rn(wsp[NS - 1][0], vlo);
             }
           };
-          float rlo;  // the adder's operands are sliced from FP32 values
           shell_rec_at<DERIV>(r, B.prim4, pt, expthr, thr, &rlo, put);
         }
       }
@@ -729,25 +771,28 @@ __global__ void __launch_bounds__(kT, 1)
       const int nop = 1 + __popc(smask);
       const int k4 = 4 * lane;  // this lane's 4 points
       const int nrows = nop * nact;
-      // four rows per pass, their loads issued together (the rows were just written:
-      // L2 latency, not bandwidth, bounds this loop)
+      // U rows per pass, their loads issued together (the rows were just written: L2
+      // latency, not bandwidth, bounds this loop)
+      constexpr int U = TWO_SPINS ? 2 : 4;  // rows per pass (registers of the two-spin form)
       int oi0 = 0, m0 = warp;  // row r0 = oi0 * nact + m0
       while (m0 >= nact) {
         m0 -= nact;
         ++oi0;
       }
-      for (int r0 = warp; r0 < nrows; r0 += 4 * kWarps) {
-        float4 v[4];
-        int ou[4], mu[4];
+      for (int r0 = warp; r0 < nrows; r0 += U * kWarps) {
+        float4 v[U], vl[U];
+        int ou[U], mu[U];
         {
           int oi = oi0, m = m0;
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < U; ++u) {
             ou[u] = oi == 0 ? 0 : (smask == 2 ? 2 : oi);
             mu[u] = m;
-            v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r0 + u * kWarps < nrows)
+            v[u] = vl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r0 + u * kWarps < nrows) {
               v[u] = *reinterpret_cast<const float4*>(stg + ((long)ou[u] * rows_pad + m) * 128 + k4);
+              vl[u] = *reinterpret_cast<const float4*>(stg + ((long)(NOPS + ou[u]) * rows_pad + m) * 128 + k4);
+            }
             m += kWarps;
             while (m >= nact) {
               m -= nact;
@@ -758,14 +803,14 @@ __global__ void __launch_bounds__(kT, 1)
           m0 = m;
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
           if (r0 + u * kWarps >= nrows) break;  // warp-uniform
           const int o = ou[u], m = mu[u];
-          float4 x = v[u];
-          if (k4 + 0 >= npts) x.x = 0.f;
-          if (k4 + 1 >= npts) x.y = 0.f;
-          if (k4 + 2 >= npts) x.z = 0.f;
-          if (k4 + 3 >= npts) x.w = 0.f;
+          float4 x = v[u], xl = vl[u];
+          if (k4 + 0 >= npts) x.x = xl.x = 0.f;
+          if (k4 + 1 >= npts) x.y = xl.y = 0.f;
+          if (k4 + 2 >= npts) x.z = xl.z = 0.f;
+          if (k4 + 3 >= npts) x.w = xl.w = 0.f;
           float mx = fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fmaxf(fabsf(x.z), fabsf(x.w)));
 #pragma unroll
           for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
@@ -773,10 +818,10 @@ __global__ void __launch_bounds__(kT, 1)
           fixed_scale<7>(mx, scale, inv);
           if (lane == 0) scl[o * rows_pad + m] = scale;
           uint16_t h[3][4];
-          fixed_slices<7, 8>(__fmul_rn(x.x, inv), h[0][0], h[1][0], h[2][0]);
-          fixed_slices<7, 8>(__fmul_rn(x.y, inv), h[0][1], h[1][1], h[2][1]);
-          fixed_slices<7, 8>(__fmul_rn(x.z, inv), h[0][2], h[1][2], h[2][2]);
-          fixed_slices<7, 8>(__fmul_rn(x.w, inv), h[0][3], h[1][3], h[2][3]);
+          fixed_slices2<7, 8>(__fmul_rn(x.x, inv), __fmul_rn(xl.x, inv), h[0][0], h[1][0], h[2][0]);
+          fixed_slices2<7, 8>(__fmul_rn(x.y, inv), __fmul_rn(xl.y, inv), h[0][1], h[1][1], h[2][1]);
+          fixed_slices2<7, 8>(__fmul_rn(x.z, inv), __fmul_rn(xl.z, inv), h[0][2], h[1][2], h[2][2]);
+          fixed_slices2<7, 8>(__fmul_rn(x.w, inv), __fmul_rn(xl.w, inv), h[0][3], h[1][3], h[2][3]);
           uint8_t* tb = reinterpret_cast<uint8_t*>(tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 *
                                                               kTileFloats);
           const uint32_t off = tc::swz_offset_h(m & 127, k4 & 63);
@@ -919,8 +964,8 @@ done:
 
 // Fixed-point slices of the density matrices, once per build: one CTA per (spin,
 // column j) finds the column's largest |P_ij|, its power-of-two scale (the largest
-// scaled element below 32) and the three FP16 slices of density_slices of every scaled
-// element, taken from the FP64 value, so P enters to 2^-30 of its column maximum.
+// scaled element below 256) and the three FP16 slices of density_slices of every scaled
+// element, taken from the FP64 value, so P enters to 2^-27 of its column maximum.
 __global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__ P, uint2* __restrict__ out,
                                                       float* __restrict__ colscale, int nbf) {
   __shared__ double red[8];
@@ -937,17 +982,17 @@ __global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__
   int e = 0;
   frexp(m, &e);
   const bool zero = !(m > 0.0) || e < -100;
-  const double inv = zero ? 0.0 : ldexp(1.0, 5 - e);
-  if (threadIdx.x == 0) colscale[c] = zero ? 0.f : ldexpf(1.f, e - 5);
+  const double inv = zero ? 0.0 : ldexp(1.0, 8 - e);
+  if (threadIdx.x == 0) colscale[c] = zero ? 0.f : ldexpf(1.f, e - 8);
   for (int i = threadIdx.x; i < nbf; i += blockDim.x) {
-    const double v = col[i] * inv;  // |v| < 32, exact
+    const double v = col[i] * inv;  // |v| < 256, exact
     const double s0 = rint(v);
-    const double r1 = (v - s0) * 4096.0;
+    const double r1 = (v - s0) * 512.0;
     const double s1 = rint(r1);
-    const double s2 = rint((r1 - s1) * 4096.0);
+    const double s2 = rint((r1 - s1) * 512.0);
     const uint32_t h0 = __half_as_ushort(__float2half_rn((float)s0));
-    const uint32_t h1 = __half_as_ushort(__float2half_rn((float)(s1 * (1.0 / 4096.0))));
-    const uint32_t h2 = __half_as_ushort(__float2half_rn((float)(s2 * (1.0 / 4096.0))));
+    const uint32_t h1 = __half_as_ushort(__float2half_rn((float)(s1 * (1.0 / 512.0))));
+    const uint32_t h2 = __half_as_ushort(__float2half_rn((float)(s2 * (1.0 / 512.0))));
     o[i] = make_uint2(h0 | (h1 << 16), h2);
   }
 }
@@ -1002,8 +1047,8 @@ static void fill_item(MxItem& it, const MixedWork& w) {
 }
 
 // Scratch floats per CTA for the items [i0, i1): the density's [5][n_b][128] values,
-// and per adder operand (Phi, G per spin) the FP32 rows, the slice tiles and the row
-// scales of ft_max 128-function tiles.
+// and per adder operand (Phi, G per spin) the FP32 rows with their low parts, the slice
+// tiles and the row scales of ft_max 128-function tiles.
 static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t i1, int* ft_max) {
   int amax = 0, smax = 1;
   for (size_t i = i0; i < i1; ++i) {
@@ -1013,7 +1058,7 @@ static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t
   const int ft = std::max(1, (amax + 127) / 128);
   *ft_max = ft;
   const long dens = 5L * amax * 128;
-  const long add = (long)(1 + smax) * ft * (128L * 128 + kOpTileFloats + 128);
+  const long add = (long)(1 + smax) * ft * (2 * 128L * 128 + kOpTileFloats + 128);
   return (std::max(dens, add) + 63) & ~63L;
 }
 
