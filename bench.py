@@ -172,8 +172,8 @@ def time_builds(ctx, plan, w, P_dev, V_dev, prec, steps, warmup, flush, stream, 
             results.append(plan.vxc(w.func, P_dev, precision=prec, out=V_dev))
             ev[i][1].record(stream)
         torch.cuda.synchronize()
-    kms = (ctypes.c_double * 5)()
-    kcnt = (ctypes.c_uint64 * 5)()
+    kms = (ctypes.c_double * 6)()
+    kcnt = (ctypes.c_uint64 * 6)()
     ctx.L.xcgpu_get_timing(ctx.h, kms, kcnt)
     ctx.L.xcgpu_set_timing(ctx.h, 0)
     return [a.elapsed_time(b) for a, b in ev], list(kms), ctx.kernel_launches - launches0, results, clk.summary()
@@ -412,7 +412,7 @@ def main():
         import torch
         n = res["plan"]["npoints"]
         flops = res["plan"]["flops_per_spin"] * res["nspin"]
-        names = ["eval", "density", "functional", "adder", "other"]
+        names = ["eval", "density", "functional", "adder", "other", "build"]
         peaks = measured_peaks()
 
         def summarize(name):
@@ -420,20 +420,23 @@ def main():
             steps = r["steps"]
             value = dist.world * steps / (r["total_ms"] / 1e3)
             kms = r["kernel_ms"]
-            dom = 3 if kms[3] >= kms[1] else 1
+            if kms[5] > 0:  # one kernel per build (density, functional and Vxc per block)
+                dom, share = 5, 1.0
+            else:
+                dom, share = (3 if kms[3] >= kms[1] else 1), 0.5
             dom_ms = kms[dom] / steps
-            achieved = (flops / 2) / (dom_ms / 1e3) / 1e12
+            achieved = (flops * share) / (dom_ms / 1e3) / 1e12
             if name == "mixed":
                 peak = peaks.get("bf16_tflops_sustained")
                 roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                         "frac": (achieved / peak) if peak else None,
-                        "traffic": MIXED_DRAM_BYTES[names[dom]] if args.config == 1 else None,
+                        "traffic": MIXED_DRAM_BYTES.get(names[dom]) if args.config == 1 else None,
                         "traffic_note": "DRAM read + write bytes per launch of this kernel on this workload, "
-                                        "one ncu capture (profiles/mx_kernels_h2o32_pbe.md)",
-                        "note": "useful FP32-equivalent flops (2 npts n_b^2 per block) of the dominant kernel "
-                                "over its CUDA-event time; peak = measured cuBLAS bf16 sustained (of measured). "
-                                "3xTF32 issues 3 TF32 MMAs per product at half the bf16 rate, so its useful "
-                                "ceiling is 1/6 of that peak"}
+                                        "one ncu capture (profiles/mx_build_h2o32_pbe.md)",
+                        "note": "useful FP32-equivalent flops (2 npts n_b^2 per block and product) of the "
+                                "dominant kernel over its CUDA-event time; peak = measured cuBLAS bf16 sustained "
+                                "(of measured). The fixed-point operands issue six FP16 MMAs per product (three "
+                                "9-bit slices a side), so the useful ceiling is 1/6 of that peak"}
             else:
                 peak = fp64_peak_tflops(torch)
                 roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

@@ -94,7 +94,9 @@ enum {
   XCGPU_KERNEL_FUNCTIONAL = 2, /* functional + grid sums */
   XCGPU_KERNEL_ADDER = 3,      /* Vxc accumulation */
   XCGPU_KERNEL_OTHER = 4,      /* screening, skip flags, reductions, symmetrisation */
-  XCGPU_KERNEL_CLASSES = 5
+  XCGPU_KERNEL_BUILD = 5,      /* whole mixed-precision builds in one kernel (density,
+                                  functional and Vxc per grid block) */
+  XCGPU_KERNEL_CLASSES = 6
 };
 xcgpu_status xcgpu_set_timing(xcgpu_ctx* ctx, int enable);
 xcgpu_status xcgpu_get_timing(xcgpu_ctx* ctx, double* ms, uint64_t* launches);

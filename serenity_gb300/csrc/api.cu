@@ -730,6 +730,32 @@ static xcgpu_status run_builds(Ctx* c, std::vector<BuildReq>& reqs, int precisio
   int* err = counter + 2;
   XC_TRY(c->cuda(cudaMemsetAsync(counter, 0, 4 * sizeof(int), c->stream), "memset aux"));
   std::vector<MixedWork> work;
+  // mixed precision with 128-point blocks (the functional's block skip then coincides
+  // with the plan's blocks): one kernel per launch does density, functional and Vxc of
+  // each block, the basis values evaluated once
+  bool fused = mixed;
+  for (const auto& r : reqs) fused = fused && r.plan->max_block == kSkipBlock;
+  if (fused) {
+    for (size_t i = 0; i < reqs.size(); ++i) {
+      const BuildReq& r = reqs[i];
+      xcgpu_plan* P = r.plan;
+      const int nbf = P->basis->nbf;
+      XC_TRY(mixed_split(c, r.P, r.nspin, nbf, bw[i].psplit));
+      XC_TRY(c->cuda(cudaMemsetAsync(r.V, 0, (size_t)r.nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
+      MixedWork mw{&P->basis->dev, &P->dev, r.nspin, bw[i].psplit, nullptr, nullptr, nullptr, nullptr, nullptr, r.V};
+      mw.func = r.func;
+      mw.thr = r.thr;
+      mw.partials = bw[i].partials;
+      work.push_back(mw);
+    }
+    XC_TRY(mixed_build_batch(c, work, counter, err));
+    for (size_t i = 0; i < reqs.size(); ++i) {
+      const int nb = reqs[i].plan->nblocks;
+      if (nb) XC_TRY(launch_sum_partials(c, bw[i].partials, nb, 2, reqs[i].exc_nel));
+      else XC_TRY(c->cuda(cudaMemsetAsync(reqs[i].exc_nel, 0, 2 * sizeof(double), c->stream), "memset sums"));
+    }
+    return XCGPU_OK;
+  }
   // 1. rho, grad rho
   for (size_t i = 0; i < reqs.size(); ++i) {
     const BuildReq& r = reqs[i];

@@ -82,7 +82,7 @@ struct DevBuf {
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
-enum KernelClass { kEval = 0, kDensity = 1, kFunctional = 2, kAdder = 3, kOther = 4, kClasses = 5 };
+enum KernelClass { kEval = 0, kDensity = 1, kFunctional = 2, kAdder = 3, kOther = 4, kBuild = 5, kClasses = 6 };
 
 struct Ctx {
   int device = 0;
@@ -90,8 +90,8 @@ struct Ctx {
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
-  double t_ms[kClasses] = {0, 0, 0, 0, 0};
-  uint64_t t_count[kClasses] = {0, 0, 0, 0, 0};
+  double t_ms[kClasses] = {0, 0, 0, 0, 0, 0};
+  uint64_t t_count[kClasses] = {0, 0, 0, 0, 0, 0};
   cudaEvent_t take_event() {
     if (ev_pool.empty()) {
       cudaEvent_t e;
@@ -257,12 +257,19 @@ struct MixedWork {
   const double* g;
   const unsigned char* skip;
   double* V;
+  int func = 0;               // whole builds: functional,
+  double thr = 0.0;           // adder block-skip threshold,
+  double* partials = nullptr;  // per-block E_xc, N_el sums [2][nblocks]
 };
 xcgpu_status mixed_init(Ctx* c);
 // bytes of the density kernel's form of nspin density matrices: 8 bytes of FP16
 // slices per element, then one FP32 scale per column
 inline size_t psplit_bytes(int nspin, int nbf) { return (size_t)nspin * nbf * nbf * 8 + (size_t)nspin * nbf * 4; }
 xcgpu_status mixed_split(Ctx* c, const double* Pm, int nspin, int nbf, float* Psplit);
+// whole builds (density, functional, Vxc per block) of the MixedWork items with func,
+// thr and partials set (plans of 128-point blocks); V is mirrored, partials hold the
+// per-block E_xc and N_el sums
+xcgpu_status mixed_build_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
 xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
 xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
 

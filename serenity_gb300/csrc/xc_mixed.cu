@@ -26,6 +26,7 @@
 
 #include "basis_eval.cuh"
 #include "exp_tang.cuh"
+#include "functionals.cuh"
 #include "internal.h"
 #include "tcgen05.cuh"
 
@@ -154,6 +155,9 @@ struct MxItem {
   const double* g;
   const unsigned char* skip;
   double* V;
+  int func;           // build: functional,
+  double thr;         // adder block-skip threshold,
+  double* partials;   // and the per-block E_xc, N_el partial sums [2][nblocks]
 };
 // Up to kMaxItems builds per launch, passed by value as the kernel parameter (no
 // host staging buffer, so launches can be issued back to back and captured in a
@@ -337,17 +341,55 @@ __device__ __forceinline__ void issue_density_chunk(uint32_t tmem, uint32_t stag
   }
 }
 
-template <int DERIV>
+// =====================================================================================
+// adder: F_b = Phi^T G + G^T Phi per block, G = w (v/2 Phi + g . grad Phi); V += F_b with
+// FP64 red.add on and above the diagonal (ScalarOperatorToMatrixAdder.cpp:224-303).  The
+// leading slice products are accumulated exactly, as in the density:
+//   1a. every active shell of the block is evaluated once; Phi and G (per spin) go to
+//       the CTA's scratch in FP32 with their low parts, [part][operand][function][128
+//       points];
+//   1b. one warp per (operand, function) row: the row's largest |value| over the block's
+//       points sets its power-of-two scale (kept in the scratch), and the three FP16
+//       slices of the scaled row go to the scratch as operand tiles (128 functions x 64
+//       points, 128-byte swizzled K-major: the shared-memory image of the tile);
+//   2. per spin and function tile pair a <= b: P1 = Phi_a^T G_b and P2 = G_a^T Phi_b
+//      (= (Phi_b^T G_a)^T, so F(a, b) = P1 + P2 needs no transposition), each over
+//      64-point chunks.  Thread 0 streams the six slice tiles of a step into one of two
+//      shared-memory stages with bulk copies (TMA) and issues the MMAs: leading x leading
+//      into one accumulator, the five other slice products into a second, per product
+//      (all 512 TMEM columns).  After a pair every thread reads its row's 32 columns of
+//      the four accumulators, applies the row and column scales and adds F to V.
+//   Steps are numbered per CTA (J); step J uses stage J & 1 and completes phase
+//   (J >> 1) & 1 of that stage's barriers, so every waiter knows its parity.
+// =====================================================================================
+constexpr int kOpTileFloats = 2 * 3 * kTileFloats;  // one 128-function tile: 2 chunks x 3 slices
+
+// =====================================================================================
+// The mixed kernels, one template in three modes:
+//   kModeDensity  rho, grad rho of every block (1. + 2. below)
+//   kModeAdder    V from given v, g (3. below, with its own shell evaluation)
+//   kModeBuild    per block 1., 2., the functional at the block's points, and 3. with G
+//                 formed from the stored basis values: a whole build
+//                 (FuncPotential::getMatrix) whose basis values are evaluated once and
+//                 whose rho, v and g never leave the SM
+// =====================================================================================
+enum MxMode { kModeDensity = 0, kModeAdder = 1, kModeBuild = 2 };
+
+template <int MODE, int DERIV, bool TWO_SPINS>
 __global__ void __launch_bounds__(kT, 1)
-    mx_density_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
+    mx_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
+  constexpr bool HAS_D = MODE != kModeAdder, HAS_A = MODE != kModeDensity;
+  constexpr int NOPS = TWO_SPINS ? 3 : 2;  // adder operands: Phi, G per spin
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t mbar[2];
+  __shared__ uint64_t mbar[2], full[2], mdone[2];
   __shared__ uint32_t tmem_slot;
-  __shared__ int s_block, s_abort;
-  __shared__ double s_part[4][kQ - 1][128];
-  __shared__ unsigned s_amax[128];  // per point: largest |phi| (FP32 bits)
-  __shared__ float s_bscale[kNT];   // per function nu of the pass: scale of its column of P
-  __shared__ long s_rowoff[kNT];    // and the offset of that column
+  __shared__ int s_block, s_abort, s_smask;
+  __shared__ double s_part[4][kQ - 1][128];  // density: partial sums of a point's threads
+  __shared__ unsigned s_amax[128];           // per point: largest |phi| (FP32 bits)
+  __shared__ float s_bscale[kNT];            // per function nu of the pass: scale of its column of P
+  __shared__ long s_rowoff[kNT];             // and the offset of that column
+  __shared__ __align__(16) float s_w[2][4][128];  // adder: per spin and point w v / 2, w g_x, w g_y, w g_z
+  __shared__ double s_rg[MODE == kModeBuild ? 2 * 4 * 128 : 1];  // build: rho, grad rho per spin
   const uint32_t base_s = tc::smem_u32(smem_raw);
   uint8_t* sm = smem_raw + ((1024 - (base_s & 1023)) & 1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -355,8 +397,11 @@ __global__ void __launch_bounds__(kT, 1)
   const int c0 = 32 * quarter;                  // this thread's 32 accumulator columns
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
   if (tid == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&mbar[i], 1);
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&mdone[i], 1);
+    }
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -365,12 +410,21 @@ __global__ void __launch_bounds__(kT, 1)
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
-  uint32_t phase = 0, pend = 0;  // per stage (bit): barrier parity; a commit not yet waited for
-  int gc = 0;                    // chunks issued by this CTA (stage = gc & 1)
+  uint32_t phase = 0, pend = 0;       // density: per stage (bit) barrier parity; a commit not yet waited for
+  int gc = 0;                         // density: chunks issued by this CTA (stage = gc & 1)
+  int J0 = 0;                         // adder: steps of earlier blocks (uniform)
+  int last_copy = -1, last_mma = -1;  // adder, thread 0: highest step copied / issued
   float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
+  const long rows_pad = (long)bt.ft_max * 128;
+  // adder scratch: (adder mode) FP32 operand rows [2][NOPS][rows_pad][128]: values, low
+  // parts; (build) the density phase's planes come first; then the slice tiles
+  // [NOPS][ft_max][2 chunks][3 slices][4096] and the row scales [NOPS][rows_pad]
+  float* const stg = my;
+  float* const tiles = my + (MODE == kModeBuild ? 5 : 2 * NOPS) * rows_pad * 128;
+  float* const scl = tiles + NOPS * bt.ft_max * kOpTileFloats;
 
   for (;;) {
-    if (tid < 128) s_amax[tid] = 0u;
+    if (HAS_D && tid < 128) s_amax[tid] = 0u;
     __syncthreads();
     if (tid == 0) s_block = atomicAdd(counter, 1);
     __syncthreads();
@@ -381,19 +435,30 @@ __global__ void __launch_bounds__(kT, 1)
     const DevBasis& B = I.B;
     const DevPlan& P = I.P;
     const int nspin = I.nspin, nbf = P.nbf;
-    double* __restrict__ rho = I.rho;
-    double* __restrict__ grad = I.grad;
     const long first = (long)b * P.max_block;
     const int npts = (int)min((long)P.max_block, P.npoints - first);
     const int nact = P.fn_off[b + 1] - P.fn_off[b];
     const int* __restrict__ fn = P.fn_list + P.fn_off[b];
     const int s0 = P.sh_off[b], s1 = P.sh_off[b + 1];
-    if (5L * nact * 128 > bt.cta_floats) {  // scratch sized for a smaller block: report, skip
-      if (tid == 0) atomicExch(err, kErrScratch);
+    const long cs = (long)nact * 128;  // plane stride of the density scratch: value, its low part, gradient
+    const int nft = (nact + 127) >> 7;
+    int smask = 0;
+    if constexpr (MODE == kModeAdder) {
+      for (int s = 0; s < nspin; ++s)
+        if (!I.skip[(long)s * P.nblocks + b]) smask |= 1 << s;
+      if (smask == 0 || nact == 0) continue;
+    }
+    if (HAS_A && (nft > bt.ft_max || nspin > NOPS - 1 ||
+                  (tiles - my) + (long)NOPS * (bt.ft_max * kOpTileFloats + rows_pad) > bt.cta_floats)) {
+      if (tid == 0) atomicExch(err, kErrScratch);  // scratch sized for a smaller block: report, skip
       continue;
     }
-    const bool live = p < npts;
-    const long cs = (long)nact * 128;  // plane stride of the scratch: value, its low part, gradient
+    if constexpr (HAS_D) {
+      if (5L * nact * 128 > bt.cta_floats) {  // scratch sized for a smaller block: report, skip
+        if (tid == 0) atomicExch(err, kErrScratch);
+        continue;
+      }
+      const bool live = p < npts;
     // ---- 1. basis values (and gradients) of the block, largest |phi| per point ----
     {
       const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
@@ -428,6 +493,7 @@ __global__ void __launch_bounds__(kT, 1)
       atomicMax(&s_amax[p], __float_as_uint(vmax));  // non-negative floats order as integers
     }
     __syncthreads();
+      {
     float sa, inva;  // this point's row scale
     fixed_scale<8>(__uint_as_float(s_amax[p]), sa, inva);
     const float up = point_dither((uint32_t)(first + p));
@@ -593,116 +659,248 @@ __global__ void __launch_bounds__(kT, 1)
         s_part[3][quarter - 1][p] = g_acc[2];
       }
       __syncthreads();
-      if (quarter == 0 && live) {
+      if (quarter == 0) {
+        if (live) {
 #pragma unroll
-        for (int k = 0; k < kQ - 1; ++k) {
-          r_acc += s_part[0][k][p];
-          g_acc[0] += s_part[1][k][p];
-          g_acc[1] += s_part[2][k][p];
-          g_acc[2] += s_part[3][k][p];
+          for (int k = 0; k < kQ - 1; ++k) {
+            r_acc += s_part[0][k][p];
+            g_acc[0] += s_part[1][k][p];
+            g_acc[1] += s_part[2][k][p];
+            g_acc[2] += s_part[3][k][p];
+          }
         }
-        rho[(long)s * P.npoints + first + p] = r_acc;
-        if (DERIV && grad) {
-          grad[((long)s * 3 + 0) * P.npoints + first + p] = 2.0 * g_acc[0];
-          grad[((long)s * 3 + 1) * P.npoints + first + p] = 2.0 * g_acc[1];
-          grad[((long)s * 3 + 2) * P.npoints + first + p] = 2.0 * g_acc[2];
+        if constexpr (MODE == kModeDensity) {
+          if (live) {
+            I.rho[(long)s * P.npoints + first + p] = r_acc;
+            if (DERIV && I.grad) {
+              I.grad[((long)s * 3 + 0) * P.npoints + first + p] = 2.0 * g_acc[0];
+              I.grad[((long)s * 3 + 1) * P.npoints + first + p] = 2.0 * g_acc[1];
+              I.grad[((long)s * 3 + 2) * P.npoints + first + p] = 2.0 * g_acc[2];
+            }
+          }
+        } else {  // kept on the SM for the functional
+          s_rg[(s * 4 + 0) * 128 + p] = live ? r_acc : 0.0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) s_rg[(s * 4 + 1 + k) * 128 + p] = live ? 2.0 * g_acc[k] : 0.0;
         }
       }
       __syncthreads();
     }
-  }
-done:
+      }
+    }
+    // ---- 1b. row scales and FP16 slice tiles, one warp per (operand, function) row;
+    //      rows r = oi * nact + m of operand oi (0: Phi, then G of the active spins),
+    //      [rbeg, rend) by warp wi of a group of nw ----
+    auto slice_rows = [&](int rbeg, int rend, int wi, int nw) {
+      if (rbeg + wi >= rend) return;
+      const int k4 = 4 * lane;  // this lane's 4 points
+      // U rows per pass, their loads issued together (the rows were just written: L2
+      // latency, not bandwidth, bounds this loop)
+      constexpr int U = (TWO_SPINS || MODE == kModeBuild) ? 2 : 4;  // rows per pass (registers)
+      int oi0 = (rbeg + wi) / nact, m0 = rbeg + wi - oi0 * nact;  // row r0 = oi0 * nact + m0
+      for (int r0 = rbeg + wi; r0 < rend; r0 += U * nw) {
+        float4 v[U], vl[U];
+        int ou[U], mu[U];
+        {
+          int oi = oi0, m = m0;
 #pragma unroll
-  for (int q = 0; q < 2; ++q)
-    if ((pend >> q) & 1u) wait_or_abort(&mbar[q], (phase >> q) & 1u, err);
-  tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 512);
-}
-
-// =====================================================================================
-// adder: F_b = Phi^T G + G^T Phi per block, G = w (v/2 Phi + g . grad Phi); V += F_b with
-// FP64 red.add on and above the diagonal (ScalarOperatorToMatrixAdder.cpp:224-303).  The
-// leading slice products are accumulated exactly, as in the density:
-//   1a. every active shell of the block is evaluated once; Phi and G (per spin) go to
-//       the CTA's scratch in FP32 with their low parts, [part][operand][function][128
-//       points];
-//   1b. one warp per (operand, function) row: the row's largest |value| over the block's
-//       points sets its power-of-two scale (kept in the scratch), and the three FP16
-//       slices of the scaled row go to the scratch as operand tiles (128 functions x 64
-//       points, 128-byte swizzled K-major: the shared-memory image of the tile);
-//   2. per spin and function tile pair a <= b: P1 = Phi_a^T G_b and P2 = G_a^T Phi_b
-//      (= (Phi_b^T G_a)^T, so F(a, b) = P1 + P2 needs no transposition), each over
-//      64-point chunks.  Thread 0 streams the six slice tiles of a step into one of two
-//      shared-memory stages with bulk copies (TMA) and issues the MMAs: leading x leading
-//      into one accumulator, the five other slice products into a second, per product
-//      (all 512 TMEM columns).  After a pair every thread reads its row's 32 columns of
-//      the four accumulators, applies the row and column scales and adds F to V.
-//   Steps are numbered per CTA (J); step J uses stage J & 1 and completes phase
-//   (J >> 1) & 1 of that stage's barriers, so every waiter knows its parity.
-// =====================================================================================
-constexpr int kOpTileFloats = 2 * 3 * kTileFloats;  // one 128-function tile: 2 chunks x 3 slices
-
-template <int DERIV, bool TWO_SPINS>
-__global__ void __launch_bounds__(kT, 1)
-    mx_adder_kernel(const __grid_constant__ MxBatch bt, int* __restrict__ counter, int* __restrict__ err) {
-  constexpr int NOPS = TWO_SPINS ? 3 : 2;  // Phi, G per spin
-  extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full[2], mdone[2];
-  __shared__ uint32_t tmem_slot;
-  __shared__ int s_block, s_abort;
-  __shared__ float s_w[2][4][128];  // per spin and point: w v / 2, w g_x, w g_y, w g_z
-  const uint32_t base_s = tc::smem_u32(smem_raw);
-  uint8_t* sm = smem_raw + ((1024 - (base_s & 1023)) & 1023);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
-  if (tid == 0) {
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&full[i], 1);
-      tc::mbar_init(&mdone[i], 1);
+          for (int u = 0; u < U; ++u) {
+            ou[u] = oi == 0 ? 0 : (smask == 2 ? 2 : oi);
+            mu[u] = m;
+            v[u] = vl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r0 + u * nw < rend) {
+              if constexpr (MODE == kModeAdder) {
+                v[u] = *reinterpret_cast<const float4*>(stg + ((long)ou[u] * rows_pad + m) * 128 + k4);
+                vl[u] = *reinterpret_cast<const float4*>(stg + ((long)(NOPS + ou[u]) * rows_pad + m) * 128 + k4);
+              } else {
+                // the density phase's planes (value, low part, gradient) of function m: Phi
+                // itself, or G = w v/2 phi + w g . grad phi formed here as the adder's
+                // shell evaluation forms it
+                const float* ph = my + (long)m * 128 + k4;
+                const float4 f = *reinterpret_cast<const float4*>(ph);
+                const float4 fl = *reinterpret_cast<const float4*>(ph + cs);
+                if (ou[u] == 0) {
+                  v[u] = f;
+                  vl[u] = fl;
+                } else {
+                  const int sp = ou[u] - 1;
+                  const float4 w0 = *reinterpret_cast<const float4*>(&s_w[sp][0][k4]);
+                  float4 g = make_float4(__fmul_rn(w0.x, f.x), __fmul_rn(w0.y, f.y), __fmul_rn(w0.z, f.z),
+                                         __fmul_rn(w0.w, f.w));
+                  if (DERIV) {
+                    const float4 dx = *reinterpret_cast<const float4*>(ph + 2 * cs);
+                    const float4 dy = *reinterpret_cast<const float4*>(ph + 3 * cs);
+                    const float4 dz = *reinterpret_cast<const float4*>(ph + 4 * cs);
+                    const float4 w1 = *reinterpret_cast<const float4*>(&s_w[sp][1][k4]);
+                    const float4 w2 = *reinterpret_cast<const float4*>(&s_w[sp][2][k4]);
+                    const float4 w3 = *reinterpret_cast<const float4*>(&s_w[sp][3][k4]);
+                    g.x = fmaf(w3.x, dz.x, fmaf(w2.x, dy.x, fmaf(w1.x, dx.x, g.x)));
+                    g.y = fmaf(w3.y, dz.y, fmaf(w2.y, dy.y, fmaf(w1.y, dx.y, g.y)));
+                    g.z = fmaf(w3.z, dz.z, fmaf(w2.z, dy.z, fmaf(w1.z, dx.z, g.z)));
+                    g.w = fmaf(w3.w, dz.w, fmaf(w2.w, dy.w, fmaf(w1.w, dx.w, g.w)));
+                  }
+                  v[u] = g;
+                  vl[u] = make_float4(__fmul_rn(w0.x, fl.x), __fmul_rn(w0.y, fl.y), __fmul_rn(w0.z, fl.z),
+                                      __fmul_rn(w0.w, fl.w));
+                }
+              }
+            }
+            m += nw;
+            while (m >= nact) {
+              m -= nact;
+              ++oi;
+            }
+          }
+          oi0 = oi;
+          m0 = m;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (r0 + u * nw >= rend) break;  // warp-uniform
+          const int o = ou[u], m = mu[u];
+          float4 x = v[u], xl = vl[u];
+          if (k4 + 0 >= npts) x.x = xl.x = 0.f;
+          if (k4 + 1 >= npts) x.y = xl.y = 0.f;
+          if (k4 + 2 >= npts) x.z = xl.z = 0.f;
+          if (k4 + 3 >= npts) x.w = xl.w = 0.f;
+          float mx = fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fmaxf(fabsf(x.z), fabsf(x.w)));
+#pragma unroll
+          for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+          float scale, inv;
+          fixed_scale<7>(mx, scale, inv);
+          if (lane == 0) scl[o * rows_pad + m] = scale;
+          uint16_t h[3][4];
+          fixed_slices2<7, 8>(__fmul_rn(x.x, inv), __fmul_rn(xl.x, inv), h[0][0], h[1][0], h[2][0]);
+          fixed_slices2<7, 8>(__fmul_rn(x.y, inv), __fmul_rn(xl.y, inv), h[0][1], h[1][1], h[2][1]);
+          fixed_slices2<7, 8>(__fmul_rn(x.z, inv), __fmul_rn(xl.z, inv), h[0][2], h[1][2], h[2][2]);
+          fixed_slices2<7, 8>(__fmul_rn(x.w, inv), __fmul_rn(xl.w, inv), h[0][3], h[1][3], h[2][3]);
+          uint8_t* tb = reinterpret_cast<uint8_t*>(tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 *
+                                                              kTileFloats);
+          const uint32_t off = tc::swz_offset_h(m & 127, k4 & 63);
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+            *reinterpret_cast<uint2*>(tb + i * kTileA + off) = make_uint2(
+                (uint32_t)h[i][0] | ((uint32_t)h[i][1] << 16), (uint32_t)h[i][2] | ((uint32_t)h[i][3] << 16));
+        }
+      }
+      tc::fence_async_global();  // these generic writes are read by the bulk copies below
+    };
+    if constexpr (MODE == kModeBuild) {
+    // ---- the functional at the block's points (build): the reference's steps, with the
+    //      reductions in the same order as the separate kernels (functional skip of the
+    //      block, E_xc and N_el partials, the adder's block skip per spin, the weights) ----
+    // warps 0-3 evaluate the functional (group barrier 1) while warps 4-15 slice the
+    // adder's Phi rows, which do not depend on it
+    if (warp < 4) {
+      auto group_sync = [] { asm volatile("bar.sync 1, 128;" ::: "memory"); };
+      double* red = &s_part[0][0][0];  // 2 x 128 doubles (the density's partial sums are done)
+      const bool pt = tid < 128;
+      const int q = tid;
+      const bool gga = xc::is_gga(I.func);
+      bool fsk = true;  // XCFun's block skip (functional data): sum |rho| < n 1e-12 for every spin
+      for (int s = 0; s < nspin; ++s) {
+        if (pt) red[q] = q < npts ? fabs(s_rg[(s * 4) * 128 + q]) : 0.0;
+        group_sync();
+        for (int w2 = 64; w2 > 0; w2 >>= 1) {
+          if (tid < w2) red[tid] += red[tid + w2];
+          group_sync();
+        }
+        fsk = fsk && (red[0] < npts * 1e-12);
+        group_sync();
+      }
+      double e = 0.0, rtot = 0.0, vv[2] = {0.0, 0.0}, gg[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+      if (pt && q < npts) {
+        if (nspin == 1) {
+          const double r = s_rg[0 * 128 + q];
+          const double gx = s_rg[1 * 128 + q], gy = s_rg[2 * 128 + q], gz = s_rg[3 * 128 + q];
+          double vn = 0.0, vs = 0.0;
+          if (!fsk) xc::eval_restricted<double>(I.func, r, gga ? gx * gx + gy * gy + gz * gz : 0.0, e, vn, vs);
+          vv[0] = vn;
+          if (gga) {
+            gg[0][0] = 2.0 * vs * gx;
+            gg[0][1] = 2.0 * vs * gy;
+            gg[0][2] = 2.0 * vs * gz;
+          }
+          rtot = r;
+        } else {
+          const double ra = s_rg[0 * 128 + q], rb = s_rg[4 * 128 + q];
+          double ga[3], gb[3];
+          for (int k = 0; k < 3; ++k) {
+            ga[k] = gga ? s_rg[(1 + k) * 128 + q] : 0.0;
+            gb[k] = gga ? s_rg[(5 + k) * 128 + q] : 0.0;
+          }
+          double va = 0, vb = 0, vaa = 0, vab = 0, vbb = 0;
+          if (!fsk) {
+            const double saa = ga[0] * ga[0] + ga[1] * ga[1] + ga[2] * ga[2];
+            const double sab = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
+            const double sbb = gb[0] * gb[0] + gb[1] * gb[1] + gb[2] * gb[2];
+            xc::eval_unrestricted<double>(I.func, ra, rb, saa, sab, sbb, e, va, vb, vaa, vab, vbb);
+          }
+          vv[0] = va;
+          vv[1] = vb;
+          if (gga)
+            for (int k = 0; k < 3; ++k) {
+              gg[0][k] = 2.0 * vaa * ga[k] + vab * gb[k];
+              gg[1][k] = 2.0 * vbb * gb[k] + vab * ga[k];
+            }
+          rtot = ra + rb;
+        }
+      }
+      const double wp = (pt && q < npts) ? P.w[first + q] : 0.0;
+      if (pt) {
+        red[q] = wp * e;
+        red[128 + q] = wp * rtot;
+      }
+      group_sync();
+      for (int w2 = 64; w2 > 0; w2 >>= 1) {
+        if (tid < w2) {
+          red[tid] += red[tid + w2];
+          red[128 + tid] += red[128 + tid + w2];
+        }
+        group_sync();
+      }
+      if (tid == 0) {
+        I.partials[b] = red[0];
+        I.partials[P.nblocks + b] = red[128];
+      }
+      group_sync();
+      for (int s = 0; s < nspin; ++s) {  // ScalarOperatorToMatrixAdder's block skip
+        double a = 0.0;
+        if (pt && q < npts) {
+          a += fabs(wp * vv[s]);
+          if (gga)
+            for (int k = 0; k < 3; ++k) a += fabs(wp * gg[s][k]);
+        }
+        if (pt) red[q] = a;
+        group_sync();
+        for (int w2 = 64; w2 > 0; w2 >>= 1) {
+          if (tid < w2) red[tid] += red[tid + w2];
+          group_sync();
+        }
+        if (!(red[0] / npts < I.thr)) smask |= 1 << s;
+        group_sync();
+      }
+      if (pt)
+        for (int s = 0; s < 2; ++s) {
+          float w4[4] = {0.f, 0.f, 0.f, 0.f};
+          if (((smask >> s) & 1) && q < npts) {
+            w4[0] = (float)(0.5 * wp * vv[s]);
+            if (DERIV && gga)
+              for (int c = 0; c < 3; ++c) w4[1 + c] = (float)(wp * gg[s][c]);
+          }
+          for (int c = 0; c < 4; ++c) s_w[s][c][q] = w4[c];
+        }
+      if (tid == 0) s_smask = smask;
+    } else if (nact > 0) {
+      slice_rows(0, nact, warp - 4, kWarps - 4);
     }
-    tc::fence_mbar_init();
-    s_abort = 0;
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = tmem_slot;
-  const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
-  int J0 = 0;                            // steps of earlier blocks (uniform)
-  int last_copy = -1, last_mma = -1;     // thread 0: highest step copied / issued
-  float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
-  const long rows_pad = (long)bt.ft_max * 128;
-  float* const stg = my;                               // [2][NOPS][rows_pad][128]: values, low parts
-  float* const tiles = stg + 2 * NOPS * rows_pad * 128;  // [NOPS][ft_max][2 chunks][3 slices][4096]
-  float* const scl = tiles + NOPS * bt.ft_max * kOpTileFloats;  // [NOPS][rows_pad]
-
-  for (;;) {
     __syncthreads();
-    if (tid == 0) s_block = atomicAdd(counter, 1);
-    __syncthreads();
-    const int gb = s_block;
-    if (gb >= bt.nblocks || s_abort) break;
-    int b;
-    const MxItem& I = locate(bt, gb, b);
-    const DevBasis& B = I.B;
-    const DevPlan& P = I.P;
-    const int nspin = I.nspin, nbf = P.nbf;
-    const long first = (long)b * P.max_block;
-    const int npts = (int)min((long)P.max_block, P.npoints - first);
-    const int nact = P.fn_off[b + 1] - P.fn_off[b];
-    const int* __restrict__ fn = P.fn_list + P.fn_off[b];
-    const int s0 = P.sh_off[b], s1 = P.sh_off[b + 1];
-    int smask = 0;
-    for (int s = 0; s < nspin; ++s)
-      if (!I.skip[(long)s * P.nblocks + b]) smask |= 1 << s;
-    if (smask == 0 || nact == 0) continue;
-    const int nft = (nact + 127) >> 7, nkc = (npts + 63) >> 6;
-    if (nft > bt.ft_max || nspin > NOPS - 1 ||
-        (long)NOPS * (2 * rows_pad * 128 + bt.ft_max * kOpTileFloats + rows_pad) > bt.cta_floats) {
-      if (tid == 0) atomicExch(err, kErrScratch);  // scratch sized for a smaller block: report, skip
-      continue;
+    smask = s_smask;
+      if (smask == 0 || nact == 0) continue;
     }
+    if constexpr (HAS_A) {
+      const int nkc = (npts + 63) >> 6;
+      if constexpr (MODE == kModeAdder) {
     // ---- weights ----
     if (tid < 256) {
       const int s = tid >> 7, q = tid & 127;
@@ -749,14 +947,14 @@ __global__ void __launch_bounds__(kT, 1)
             t[0] = val;
             t[lo] = vlo;
             if (sp0) {
-              float gv = wsp[0][0] * val;
-              if (DERIV) gv += wsp[0][1] * dx + wsp[0][2] * dy + wsp[0][3] * dz;
+              float gv = __fmul_rn(wsp[0][0], val);
+              if (DERIV) gv = fmaf(wsp[0][3], dz, fmaf(wsp[0][2], dy, fmaf(wsp[0][1], dx, gv)));
               t[rows_pad * 128] = gv;
               t[lo + rows_pad * 128] = __fmul_rn(wsp[0][0], vlo);
             }
             if (TWO_SPINS && sp1) {
-              float gv = wsp[NS - 1][0] * val;
-              if (DERIV) gv += wsp[NS - 1][1] * dx + wsp[NS - 1][2] * dy + wsp[NS - 1][3] * dz;
+              float gv = __fmul_rn(wsp[NS - 1][0], val);
+              if (DERIV) gv = fmaf(wsp[NS - 1][3], dz, fmaf(wsp[NS - 1][2], dy, fmaf(wsp[NS - 1][1], dx, gv)));
               t[2 * rows_pad * 128] = gv;
               t[lo + 2 * rows_pad * 128] = __fmul_rn(wsp[NS - 1][0], vlo);
             }
@@ -766,72 +964,11 @@ __global__ void __launch_bounds__(kT, 1)
       }
     }
     __syncthreads();
-    // ---- 1b. row scales and FP16 slice tiles, one warp per (operand, function) row ----
-    {
-      const int nop = 1 + __popc(smask);
-      const int k4 = 4 * lane;  // this lane's 4 points
-      const int nrows = nop * nact;
-      // U rows per pass, their loads issued together (the rows were just written: L2
-      // latency, not bandwidth, bounds this loop)
-      constexpr int U = TWO_SPINS ? 2 : 4;  // rows per pass (registers of the two-spin form)
-      int oi0 = 0, m0 = warp;  // row r0 = oi0 * nact + m0
-      while (m0 >= nact) {
-        m0 -= nact;
-        ++oi0;
       }
-      for (int r0 = warp; r0 < nrows; r0 += U * kWarps) {
-        float4 v[U], vl[U];
-        int ou[U], mu[U];
-        {
-          int oi = oi0, m = m0;
-#pragma unroll
-          for (int u = 0; u < U; ++u) {
-            ou[u] = oi == 0 ? 0 : (smask == 2 ? 2 : oi);
-            mu[u] = m;
-            v[u] = vl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r0 + u * kWarps < nrows) {
-              v[u] = *reinterpret_cast<const float4*>(stg + ((long)ou[u] * rows_pad + m) * 128 + k4);
-              vl[u] = *reinterpret_cast<const float4*>(stg + ((long)(NOPS + ou[u]) * rows_pad + m) * 128 + k4);
-            }
-            m += kWarps;
-            while (m >= nact) {
-              m -= nact;
-              ++oi;
-            }
-          }
-          oi0 = oi;
-          m0 = m;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (r0 + u * kWarps >= nrows) break;  // warp-uniform
-          const int o = ou[u], m = mu[u];
-          float4 x = v[u], xl = vl[u];
-          if (k4 + 0 >= npts) x.x = xl.x = 0.f;
-          if (k4 + 1 >= npts) x.y = xl.y = 0.f;
-          if (k4 + 2 >= npts) x.z = xl.z = 0.f;
-          if (k4 + 3 >= npts) x.w = xl.w = 0.f;
-          float mx = fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fmaxf(fabsf(x.z), fabsf(x.w)));
-#pragma unroll
-          for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
-          float scale, inv;
-          fixed_scale<7>(mx, scale, inv);
-          if (lane == 0) scl[o * rows_pad + m] = scale;
-          uint16_t h[3][4];
-          fixed_slices2<7, 8>(__fmul_rn(x.x, inv), __fmul_rn(xl.x, inv), h[0][0], h[1][0], h[2][0]);
-          fixed_slices2<7, 8>(__fmul_rn(x.y, inv), __fmul_rn(xl.y, inv), h[0][1], h[1][1], h[2][1]);
-          fixed_slices2<7, 8>(__fmul_rn(x.z, inv), __fmul_rn(xl.z, inv), h[0][2], h[1][2], h[2][2]);
-          fixed_slices2<7, 8>(__fmul_rn(x.w, inv), __fmul_rn(xl.w, inv), h[0][3], h[1][3], h[2][3]);
-          uint8_t* tb = reinterpret_cast<uint8_t*>(tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 *
-                                                              kTileFloats);
-          const uint32_t off = tc::swz_offset_h(m & 127, k4 & 63);
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-            *reinterpret_cast<uint2*>(tb + i * kTileA + off) = make_uint2(
-                (uint32_t)h[i][0] | ((uint32_t)h[i][1] << 16), (uint32_t)h[i][2] | ((uint32_t)h[i][3] << 16));
-        }
-      }
-      tc::fence_async_global();  // these generic writes are read by the bulk copies below
+    if constexpr (MODE == kModeAdder) {
+      slice_rows(0, (1 + __popc(smask)) * nact, warp, kWarps);
+    } else {  // the Phi rows were sliced beside the functional
+      slice_rows(nact, (1 + __popc(smask)) * nact, warp, kWarps);
     }
     __syncthreads();
     // ---- 2. tile pairs ----
@@ -946,7 +1083,8 @@ __global__ void __launch_bounds__(kT, 1)
       tc::fence_before_sync();
       __syncthreads();  // the accumulators are reused by the next pair
     }
-    J0 += nsteps;
+      J0 += nsteps;
+    }
   }
   goto done;
 abort:
@@ -957,6 +1095,9 @@ abort:
     if (last_mma >= 0) tc::mbar_wait_bounded(&mdone[last_mma & 1], (last_mma >> 1) & 1u, kWaitLimitNs);
   }
 done:
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    if ((pend >> q) & 1u) wait_or_abort(&mbar[q], (phase >> q) & 1u, err);
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
@@ -1010,23 +1151,17 @@ __global__ void mirror_upper_kernel(double* V, int nbf, int nspin) {
   M[e] = M[(long)i * nbf + j];
 }
 
-static size_t density_smem() { return 2 * kDStageBytes + 1024; }
-static size_t adder_smem() { return 2 * kDStageBytes + 1024; }
+static size_t mx_smem() { return 2 * kDStageBytes + 1024; }  // two stages, 1024-byte aligned
 
 xcgpu_status mixed_init(Ctx* c) {
-  const struct {
-    const void* fn;
-    size_t bytes;
-    const char* what;
-  } k[] = {{(const void*)mx_density_kernel<0>, density_smem(), "density smem attribute"},
-           {(const void*)mx_density_kernel<1>, density_smem(), "density smem attribute"},
-           {(const void*)mx_adder_kernel<0, false>, adder_smem(), "adder smem attribute"},
-           {(const void*)mx_adder_kernel<1, false>, adder_smem(), "adder smem attribute"},
-           {(const void*)mx_adder_kernel<0, true>, adder_smem(), "adder smem attribute"},
-           {(const void*)mx_adder_kernel<1, true>, adder_smem(), "adder smem attribute"}};
-  for (const auto& e : k) {
-    xcgpu_status st =
-        c->cuda(cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.bytes), e.what);
+  const void* k[] = {(const void*)mx_kernel<kModeDensity, 0, false>, (const void*)mx_kernel<kModeDensity, 1, false>,
+                     (const void*)mx_kernel<kModeAdder, 0, false>,   (const void*)mx_kernel<kModeAdder, 1, false>,
+                     (const void*)mx_kernel<kModeAdder, 0, true>,    (const void*)mx_kernel<kModeAdder, 1, true>,
+                     (const void*)mx_kernel<kModeBuild, 0, false>,   (const void*)mx_kernel<kModeBuild, 1, false>,
+                     (const void*)mx_kernel<kModeBuild, 0, true>,    (const void*)mx_kernel<kModeBuild, 1, true>};
+  for (const void* fn : k) {
+    xcgpu_status st = c->cuda(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx_smem()),
+                              "mixed kernel smem attribute");
     if (st) return st;
   }
   return XCGPU_OK;
@@ -1044,11 +1179,15 @@ static void fill_item(MxItem& it, const MixedWork& w) {
   it.g = w.g;
   it.skip = w.skip;
   it.V = w.V;
+  it.func = w.func;
+  it.thr = w.thr;
+  it.partials = w.partials;
 }
 
 // Scratch floats per CTA for the items [i0, i1): the density's [5][n_b][128] values,
-// and per adder operand (Phi, G per spin) the FP32 rows with their low parts, the slice
-// tiles and the row scales of ft_max 128-function tiles.
+// per adder operand (Phi, G per spin) the FP32 rows with their low parts, the slice
+// tiles and the row scales of ft_max 128-function tiles, and for a whole build the
+// density's planes followed by the tiles and scales.
 static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t i1, int* ft_max) {
   int amax = 0, smax = 1;
   for (size_t i = i0; i < i1; ++i) {
@@ -1059,7 +1198,8 @@ static long cta_floats_for(const std::vector<MixedWork>& work, size_t i0, size_t
   *ft_max = ft;
   const long dens = 5L * amax * 128;
   const long add = (long)(1 + smax) * ft * (2 * 128L * 128 + kOpTileFloats + 128);
-  return (std::max(dens, add) + 63) & ~63L;
+  const long build = 5L * ft * 128 * 128 + (long)(1 + smax) * ft * (kOpTileFloats + 128);
+  return (std::max(std::max(dens, add), build) + 63) & ~63L;
 }
 
 // parameter blocks for the items [i0, i1) of a batch
@@ -1103,7 +1243,10 @@ xcgpu_status mixed_split(Ctx* c, const double* Pm, int nspin, int nbf, float* Ps
   return c->check_launch("split_p_kernel");
 }
 
-xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
+// one persistent launch per kMaxItems items of the mode's kernel
+template <int MODE>
+static xcgpu_status mixed_launch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err, int cls,
+                                 const char* what) {
   static thread_local MxBatch bt;  // host-side parameter block (the launch copies it)
   for (size_t i0 = 0; i0 < work.size(); i0 += kMaxItems) {
     const size_t i1 = std::min(work.size(), i0 + kMaxItems);
@@ -1112,41 +1255,46 @@ xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int
     xcgpu_status st = batch_scratch(c, work, i0, i1, bt);
     if (st) return st;
     if ((st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter"))) return st;
-    KernelTimer kt(c, kDensity);
-    if (any_gga(work, i0, i1, true))
-      mx_density_kernel<1><<<c->sm_count, kT, density_smem(), c->stream>>>(bt, counter, err);
-    else
-      mx_density_kernel<0><<<c->sm_count, kT, density_smem(), c->stream>>>(bt, counter, err);
-    if ((st = c->check_launch("mx_density_kernel"))) return st;
+    bool two = false, gga = false;
+    for (size_t i = i0; i < i1; ++i) {
+      two = two || work[i].nspin == 2;
+      gga = gga || (MODE == kModeDensity ? work[i].grad != nullptr
+                    : MODE == kModeAdder ? work[i].g != nullptr
+                                         : xc::is_gga(work[i].func));
+    }
+    KernelTimer kt(c, cls);
+    auto* kern = MODE == kModeDensity ? (gga ? mx_kernel<MODE, 1, false> : mx_kernel<MODE, 0, false>)
+                 : gga ? (two ? mx_kernel<MODE, 1, true> : mx_kernel<MODE, 1, false>)
+                       : (two ? mx_kernel<MODE, 0, true> : mx_kernel<MODE, 0, false>);
+    kern<<<c->sm_count, kT, mx_smem(), c->stream>>>(bt, counter, err);
+    if ((st = c->check_launch(what))) return st;
   }
   return XCGPU_OK;
 }
 
-xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
-  static thread_local MxBatch bt;
-  xcgpu_status st = XCGPU_OK;
-  for (size_t i0 = 0; i0 < work.size(); i0 += kMaxItems) {
-    const size_t i1 = std::min(work.size(), i0 + kMaxItems);
-    make_batch(work, i0, i1, bt);
-    if (bt.nblocks == 0) continue;
-    if ((st = batch_scratch(c, work, i0, i1, bt))) return st;
-    if ((st = c->cuda(cudaMemsetAsync(counter, 0, sizeof(int), c->stream), "counter"))) return st;
-    KernelTimer kt(c, kAdder);
-    bool two = false;
-    for (size_t i = i0; i < i1; ++i) two = two || work[i].nspin == 2;
-    const bool gga = any_gga(work, i0, i1, false);
-    auto* kern = gga ? (two ? mx_adder_kernel<1, true> : mx_adder_kernel<1, false>)
-                     : (two ? mx_adder_kernel<0, true> : mx_adder_kernel<0, false>);
-    kern<<<c->sm_count, kT, adder_smem(), c->stream>>>(bt, counter, err);
-    if ((st = c->check_launch("mx_adder_kernel"))) return st;
-  }
-  KernelTimer kt2(c, kOther);
+static xcgpu_status mirror_all(Ctx* c, const std::vector<MixedWork>& work) {
+  KernelTimer kt(c, kOther);
   for (const auto& w : work) {
     const long n = (long)w.P->nbf * w.P->nbf * w.nspin;
     mirror_upper_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(w.V, w.P->nbf, w.nspin);
-    if ((st = c->check_launch("mirror_upper_kernel"))) return st;
+    xcgpu_status st = c->check_launch("mirror_upper_kernel");
+    if (st) return st;
   }
   return XCGPU_OK;
+}
+
+xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
+  return mixed_launch<kModeDensity>(c, work, counter, err, kDensity, "mx_kernel (density)");
+}
+
+xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
+  xcgpu_status st = mixed_launch<kModeAdder>(c, work, counter, err, kAdder, "mx_kernel (adder)");
+  return st ? st : mirror_all(c, work);
+}
+
+xcgpu_status mixed_build_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
+  xcgpu_status st = mixed_launch<kModeBuild>(c, work, counter, err, kBuild, "mx_kernel (build)");
+  return st ? st : mirror_all(c, work);
 }
 
 }  // namespace xcgpu
