@@ -31,9 +31,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "XC builds/s & Mpts/s, (H2O)32 PBE, mixed vs FP64 GPU at 1e-7 Eh; p50/p99 latency"
-# dram__bytes_read.sum + dram__bytes_write.sum per launch of the mixed kernels on the
-# (H2O)32 workload, from one ncu --set full capture (profiles/mx_kernels_h2o32_pbe.md)
-MIXED_DRAM_BYTES = {"density": 120.1e6 + 546.5e6, "adder": 209.1e6 + 756.1e6}
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the whole-build mixed kernel
+# on the (H2O)32 workload, from one ncu --set full capture (profiles/mx_build_h2o32_pbe.md)
+MIXED_DRAM_BYTES = {"build": 941.1e6 + 5.2e6}
 WORKLOAD = "(H2O)32 def2-SVP PBE restricted, 75x302 Becke grid, 128-point blocks"
 
 

@@ -569,6 +569,9 @@ static xcgpu_status prep_chunks(xcgpu_plan* P) {
   P->chunk_max_doubles = std::max(mx, cur);
   P->chunk_bounds.push_back(P->nblocks);
   XC_TRY(upload(c, P->w_slab, slab_off.data(), slab_off.size()));
+  // plans are shared by builds on several streams: the offsets must be on the device
+  // before any stream's kernels can read them (once per plan)
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "plan chunks"));
   P->chunks_ready = true;
   return XCGPU_OK;
 }
