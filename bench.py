@@ -475,7 +475,7 @@ def main():
             "metric": METRIC, "value": H["value"], "unit": "builds/s", "n_gpus": args.gpus, "steps": H["steps"],
             "warmup": args.warmup, "ms_per_step": H["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if head == "fp64" else "fp32+tf32x3 (f64 functional, sums, Vxc)",
+            "dtype": "f64" if head == "fp64" else "fp32 basis, fp16 fixed-point slices on the tensor cores (f64 functional, sums, Vxc)",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "npoints": n, "nbf": res["nbf"], "nblocks": res["plan"]["nblocks"],
                        "mean_active": res["plan"]["sum_active"] / res["plan"]["nblocks"], "precision": head,

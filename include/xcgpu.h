@@ -43,8 +43,9 @@ enum { XCGPU_MEM_HOST = 0, XCGPU_MEM_DEVICE = 1 };
 /* precision of a whole build */
 enum {
   XCGPU_PREC_FP64 = 0, /* every stage in FP64: the drop-in */
-  XCGPU_PREC_MIXED = 1 /* FP32 basis values, 3xTF32 tensor-core contractions with FP32
-                          accumulation; FP64 functional, grid sums and cross-block Vxc */
+  XCGPU_PREC_MIXED = 1 /* FP32 basis values with FP32-pair corrections, tensor-core
+                          contractions over fixed-point FP16 slices whose leading products
+                          sum exactly; FP64 functional, grid sums and cross-block Vxc */
 };
 
 /* functionals (CompositeFunctionals.cpp:233-246; basic_functionals.dat) */
@@ -167,7 +168,7 @@ void xcgpu_plan_destroy(xcgpu_plan* plan);
  * DensityOnGridCalculator::calcDensityAndGradientOnGrid (DensityOnGridCalculator.h:53-128,
  * MatrixOperatorToGridTransformer.cpp:37-198): rho = rowsum((phi P_b) o phi),
  * grad rho = 2 rowsum((phi P_b) o grad phi).  grad may be NULL (density only).
- * precision: XCGPU_PREC_FP64 (the drop-in) or XCGPU_PREC_MIXED (3xTF32 tensor cores). */
+ * precision: XCGPU_PREC_FP64 (the drop-in) or XCGPU_PREC_MIXED (tensor cores). */
 xcgpu_status xcgpu_density(xcgpu_plan* plan, int nspin, const double* P, double* rho, double* grad, int precision,
                            int mem);
 /* FP64 rho and grad rho without any device allocation.  No counterpart in the reference:

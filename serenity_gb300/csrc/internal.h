@@ -243,9 +243,10 @@ xcgpu_status launch_lr_kernel(Ctx* c, int func, long n, const double* rho0, cons
 xcgpu_status launch_symmetrise_half(Ctx* c, const double* D, double* S, int n);
 xcgpu_status launch_scale_add(Ctx* c, long n, double a, const double* x, double* y);  // y += a x
 xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out /*device*/);
-// mixed precision (tcgen05, 3xTF32): one persistent launch per stage over the blocks of
-// every build in `work`; density writes rho / grad rho (FP64), the adder accumulates
-// V += D and then symmetrises V <- V + V^T.
+// mixed precision (tcgen05 over fixed-point FP16 slices): one persistent launch over the
+// blocks of every build in `work`; the density writes rho / grad rho (FP64), the adder
+// accumulates F_b on and above the diagonal of V and mirrors it, a whole build does both
+// with the functional in between.
 struct MixedWork {
   const DevBasis* B;
   const DevPlan* P;

@@ -1,13 +1,10 @@
 // Thin inline-PTX layer for the sm_100-family tensor cores (tcgen05 / TMEM),
-// shared-memory matrix descriptors, mbarriers and the TF32 split used by the
-// 3xTF32 products (error-compensated FP32 GEMM emulation: a = a_hi + a_lo with both
-// parts representable in TF32, a*b ~ a_hi*b_hi + a_hi*b_lo + a_lo*b_hi; the method
-// CUTLASS documents for its "3xTF32" FP32 GEMMs).
+// shared-memory matrix descriptors, mbarriers and bulk copies.
 //
 // Operand layout used everywhere: K-major, 128-byte swizzle.  A tile of R rows
-// (R % 8 == 0) and 32 FP32/TF32 elements (128 bytes) per row starts on a 1024-byte
-// boundary; element (r, k) lives at byte
-//     r * 128 + (((k >> 2) ^ (r & 7)) << 4) + (k & 3) * 4
+// (R % 8 == 0) and 128 bytes per row (64 FP16, or 32 FP32/TF32 elements) starts on a
+// 1024-byte boundary; byte b of row r lives at
+//     r * 128 + (((b >> 4) ^ (r & 7)) << 4) + (b & 15)
 // (16-byte chunks XOR-permuted by the row index within each 8-row, 1024-byte atom).
 #pragma once
 #include <cstdint>
@@ -19,10 +16,6 @@ namespace tc {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint32_t swz_offset(int r, int k) {
-  return (uint32_t)(r * 128 + ((((k >> 2) ^ (r & 7)) & 7) << 4) + (k & 3) * 4);
 }
 
 // Shared-memory matrix descriptor (tcgen05): start >> 4 in bits [0,14), leading byte
@@ -38,14 +31,8 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9,
-// 10-12 = 2), both K-major, N >> 3 in bits 17-22, M >> 4 in bits 24-28.
-__host__ __device__ __forceinline__ uint32_t idesc_tf32(int M, int N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-// Instruction descriptor, kind::f16 with FP16 A and B (bits 7-9, 10-12 = 0) and an F32
-// accumulator; otherwise as above.
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = FP16 (bits 7-9,
+// 10-12 = 0), both K-major, N >> 3 in bits 17-22, M >> 4 in bits 24-28.
 __host__ __device__ __forceinline__ uint32_t idesc_f16(int M, int N) {
   return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
@@ -55,14 +42,6 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
       "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
 }
 
@@ -180,30 +159,6 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
 // (64 FP16 per 128-byte row; the same 16-byte chunk permutation as above)
 __device__ __forceinline__ uint32_t swz_offset_h(int r, int k) {
   return (uint32_t)(r * 128 + ((((k >> 3) ^ (r & 7)) & 7) << 4) + (k & 7) * 2);
-}
-
-// Round an FP32 bit pattern to TF32 (10 stored mantissa bits), to nearest with ties
-// away from zero: adding half a TF32 unit (bit 12) to the sign-magnitude pattern carries
-// into bit 13 exactly when the dropped magnitude is at least half a unit (a carry out of
-// the mantissa steps the exponent, which is the correctly rounded result); then clear the
-// 13 dropped bits.  Two integer operations instead of a conversion instruction.
-__device__ __forceinline__ uint32_t round_tf32(float x) { return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u; }
-
-// TF32 split of an FP32 value: hi = round-to-nearest TF32(x), lo = TF32(x - hi) (x - hi
-// is exact in FP32).
-__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
-  const uint32_t h = round_tf32(x);
-  hi = h;
-  lo = round_tf32(x - __uint_as_float(h));
-}
-// same for an FP64 value (the remainder is taken in FP64 before rounding)
-__device__ __forceinline__ void split_tf32(double x, uint32_t& hi, uint32_t& lo) {
-  uint32_t h, l;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"((float)x));
-  const float r = (float)(x - (double)__uint_as_float(h));
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
-  hi = h;
-  lo = l;
 }
 
 }  // namespace tc

@@ -1,9 +1,12 @@
-"""GPU parity of the mixed-precision form (FP32 basis values, 3xTF32 tcgen05
-contractions with FP32 accumulation; FP64 functional, grid sums and cross-block
-Vxc) against the FP64 path and the oracle on the same inputs.
+"""GPU parity of the mixed-precision form (FP32 basis values with FP32-pair
+corrections, tcgen05 contractions over fixed-point FP16 slices whose leading products
+sum exactly; FP64 functional, grid sums and cross-block Vxc) against the FP64 path and
+the oracle on the same inputs.
 
-Stated tolerances (water tetramer, def2-SVP / def2-TZVP, 30 x 110 grid): density
-relative to max rho 2e-6, adder 2e-6 absolute, E_xc 5e-6 Eh, max|dVxc| 1e-6."""
+Stated tolerances (water tetramer, 30 x 110 grid): density relative to max rho 1e-6,
+adder 1.5e-6 (random v and g), N_el 1e-8 relative; whole builds against the oracle
+E_xc 1e-7 Eh and max|dVxc| 1.5e-7 with def2-SVP (measured 2-6e-8 and 0.8-1.0e-7),
+3e-7 Eh and 4e-7 with def2-TZVP (measured 1.3-1.9e-7 and 2.6-2.8e-7)."""
 import numpy as np
 import pytest
 
@@ -40,8 +43,8 @@ def test_mixed_density_vs_fp64(ctx, max_block):
     r64, g64 = plan.density(P)
     rmx, gmx = plan.density(P, precision=xcgpu.PREC_MIXED)
     scale = np.abs(r64).max()
-    assert np.abs(rmx - r64).max() <= 2e-6 * scale, np.abs(rmx - r64).max() / scale
-    assert np.abs(gmx - g64).max() <= 2e-6 * np.abs(g64).max()
+    assert np.abs(rmx - r64).max() <= 1e-6 * scale, np.abs(rmx - r64).max() / scale
+    assert np.abs(gmx - g64).max() <= 1e-6 * np.abs(g64).max()
 
 
 def test_mixed_adder_vs_fp64(ctx):
@@ -53,23 +56,24 @@ def test_mixed_adder_vs_fp64(ctx):
     g = rng.standard_normal((1, 3, len(wts)))
     F64 = plan.add_scalar(v, g)
     Fmx = plan.add_scalar(v, g, precision=xcgpu.PREC_MIXED)
-    assert np.abs(Fmx - F64).max() <= 2e-6 * max(1.0, np.abs(F64).max())
+    assert np.abs(Fmx - F64).max() <= 1.5e-6 * max(1.0, np.abs(F64).max())
     F64 = plan.add_scalar(v)
     Fmx = plan.add_scalar(v, precision=xcgpu.PREC_MIXED)
-    assert np.abs(Fmx - F64).max() <= 2e-6 * max(1.0, np.abs(F64).max())
+    assert np.abs(Fmx - F64).max() <= 1.5e-6 * max(1.0, np.abs(F64).max())
 
 
-@pytest.mark.parametrize("func,unrestricted,basis,spherical", [
-    ("LDA", False, "DEF2-SVP", True), ("PBE", False, "DEF2-SVP", True), ("BLYP", False, "DEF2-SVP", True),
-    ("PBE", True, "DEF2-SVP", True), ("PBE", False, "DEF2-TZVP", True), ("PBE", False, "DEF2-TZVP", False)])
-def test_mixed_vxc_vs_oracle(ctx, func, unrestricted, basis, spherical):
+@pytest.mark.parametrize("func,unrestricted,basis,spherical,etol,vtol", [
+    ("LDA", False, "DEF2-SVP", True, 1e-7, 1.5e-7), ("PBE", False, "DEF2-SVP", True, 1e-7, 1.5e-7),
+    ("BLYP", False, "DEF2-SVP", True, 1e-7, 1.5e-7), ("PBE", True, "DEF2-SVP", True, 1e-7, 1.5e-7),
+    ("PBE", False, "DEF2-TZVP", True, 3e-7, 4e-7), ("PBE", False, "DEF2-TZVP", False, 3e-7, 4e-7)])
+def test_mixed_vxc_vs_oracle(ctx, func, unrestricted, basis, spherical, etol, vtol):
     from serenity_gb300 import xcgpu
     w, pts, wts = _case(func, unrestricted, basis=basis, spherical=spherical)
     plan = _plan(ctx, w, pts, wts)
     P = w.density()
     V, exc, nel = plan.vxc(func, P, precision=xcgpu.PREC_MIXED)
     rV, rexc, rnel = po.Basis(w.shells).vxc(pts, wts, func, P)
-    assert abs(exc - rexc) <= 5e-6, abs(exc - rexc)
-    assert abs(nel - rnel) <= 1e-6 * rnel
-    assert np.abs(V - rV).max() <= 1e-6, np.abs(V - rV).max()
+    assert abs(exc - rexc) <= etol, abs(exc - rexc)
+    assert abs(nel - rnel) <= 1e-8 * rnel
+    assert np.abs(V - rV).max() <= vtol, np.abs(V - rV).max()
     np.testing.assert_allclose(V, np.swapaxes(V, 1, 2), rtol=0, atol=1e-14)
