@@ -502,6 +502,9 @@ __global__ void __launch_bounds__(kT, 1)
       const uint2* __restrict__ Psl = I.Psl + (long)s * nbf * nbf;
       const float* __restrict__ Pcs = I.Pcs + (long)s * nbf;
       double r_acc = 0.0, g_acc[3] = {0.0, 0.0, 0.0};
+      // the basis values' low parts enter through their own FP32 sum: added into rr, each
+      // (about an ulp of rr) would mostly round away, a systematic loss of the corrections
+      float r_lo = 0.f;
       for (int nu0 = 0; nu0 < nact; nu0 += kNT) {
         const int nnu = min(kNT, nact - nu0);
         const int N = (nnu + 15) & ~15;
@@ -630,7 +633,8 @@ __global__ void __launch_bounds__(kT, 1)
                   if (col < nnu) {
                     const float xv = __fmul_rn(ar[c], __fmul_rn(sa, s_bscale[col]));
                     const float* tc_ = t + (long)col * 128;
-                    rr = fmaf(xv, tc_[cs], fmaf(xv, tc_[0], rr));
+                    rr = fmaf(xv, tc_[0], rr);
+                    r_lo = fmaf(xv, tc_[cs], r_lo);
                     if (DERIV) {
                       gx = fmaf(xv, tc_[2 * cs], gx);
                       gy = fmaf(xv, tc_[3 * cs], gy);
@@ -651,6 +655,7 @@ __global__ void __launch_bounds__(kT, 1)
           __syncthreads();  // the accumulators and s_bscale are reused
         }
       }
+      r_acc += (double)r_lo;
       // combine the kQ partial sums of each point
       if (quarter > 0) {
         s_part[0][quarter - 1][p] = r_acc;
