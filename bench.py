@@ -41,6 +41,12 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def replica_throughput(world, steps, total_ms):
+    """Whole-job builds/s of `world` independent replicas that each ran `steps` builds, the
+    job's time being the slowest replica's `total_ms` (max over ranks)."""
+    return world * steps / (total_ms / 1e3)
+
+
 class Dist:
     """Host-side barrier and max-reduction across replicas (gloo, 127.0.0.1)."""
 
@@ -418,7 +424,7 @@ def main():
         def summarize(name):
             r = res[name]
             steps = r["steps"]
-            value = dist.world * steps / (r["total_ms"] / 1e3)
+            value = replica_throughput(dist.world, steps, r["total_ms"])
             kms = r["kernel_ms"]
             if kms[5] > 0:  # one kernel per build (density, functional and Vxc per block)
                 dom, share = 5, 1.0
@@ -483,7 +489,7 @@ def main():
                        "l2": "flushed between steps (512 MB write, outside the timed events)"},
             "mpts_per_s": H["mpts_per_s"], "latency_ms": H["latency_ms"], "roofline": H["roofline"],
             "kernel_ms_per_step": H["kernel_ms_per_step"],
-            "e2e": {"value": dist.world * len(res["e2e_ms"]) / (res["e2e_total_ms"] / 1e3), "unit": "builds/s",
+            "e2e": {"value": replica_throughput(dist.world, len(res["e2e_ms"]), res["e2e_total_ms"]), "unit": "builds/s",
                     "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
                     "latency_ms": {"p50": float(np.percentile(res["e2e_ms"], 50)),
                                    "p99": float(np.percentile(res["e2e_ms"], 99))}},
