@@ -1234,12 +1234,6 @@ static xcgpu_status batch_scratch(Ctx* c, const std::vector<MixedWork>& work, si
   return XCGPU_OK;
 }
 
-static bool any_gga(const std::vector<MixedWork>& work, size_t i0, size_t i1, bool density) {
-  for (size_t i = i0; i < i1; ++i)
-    if (density ? work[i].grad != nullptr : work[i].g != nullptr) return true;
-  return false;
-}
-
 xcgpu_status mixed_split(Ctx* c, const double* Pm, int nspin, int nbf, float* Psplit) {
   KernelTimer kt(c, kOther);
   uint2* sl = reinterpret_cast<uint2*>(Psplit);
