@@ -198,10 +198,11 @@ __device__ __forceinline__ const MxItem& locate(const MxBatch& bt, int gb, int& 
 //   chunks the products go to four accumulators by order, s0 t0 (integers, sum below
 //   2^23), s0 t1 + s1 t0 (sum below 2^24 units of 2^-9), s1 t1 (below 2^23 units of
 //   2^-18) and s0 t2 + s2 t0 (below 2^24 units of 2^-18, with s2 stored as a multiple of
-//   2^-9 so that every FP16 operand is a normal number): all four sums are exact in FP32
-//   whatever the rounding of the tensor core's adder tree, and only the third-order
-//   products (below 2^-27 of the leading ones) are left out.  The slices are stored
-//   pre-scaled as FP16 (exact) and multiplied with kind::f16 MMAs.
+//   2^-9 so that every FP16 operand is a normal number): the first three sums are exact
+//   in FP32 whatever the rounding of the tensor core's adder tree.  The fourth also takes
+//   s1 t2 + s2 t1, which round there at 2^-35 of the leading products; left out, these
+//   (2^-27) were the largest noise term of the density.  Only s2 t2 (2^-36) is dropped.
+//   The slices are stored pre-scaled as FP16 (exact) and multiplied with kind::f16 MMAs.
 //   1. every active shell of the block is evaluated once (value with its low part and,
 //      for GGA, gradient) into the CTA's scratch, FP32, [plane][function][128 points],
 //      with the largest |phi| of each point;
@@ -338,6 +339,11 @@ __device__ __forceinline__ void issue_density_chunk(uint32_t tmem, uint32_t stag
     tc::mma_f16(tmem + 256, a[1] + o, b[1] + o, idesc, acc);
     tc::mma_f16(tmem + 384, a[0] + o, b[2] + o, idesc, acc);
     tc::mma_f16(tmem + 384, a[2] + o, b[0] + o, idesc, 1u);
+    // the third-order products s1 t2 + s2 t1 carry the same 2^-9 weight as the stored
+    // third slices: added here they round in this accumulator (2^-35 of the leading
+    // products) instead of being left out (2^-27)
+    tc::mma_f16(tmem + 384, a[1] + o, b[2] + o, idesc, 1u);
+    tc::mma_f16(tmem + 384, a[2] + o, b[1] + o, idesc, 1u);
   }
 }
 
