@@ -441,8 +441,9 @@ def main():
                                         "one ncu capture (profiles/mx_build_h2o32_pbe.md)",
                         "note": "useful FP32-equivalent flops (2 npts n_b^2 per block and product) of the "
                                 "dominant kernel over its CUDA-event time; peak = measured cuBLAS bf16 sustained "
-                                "(of measured). The fixed-point operands issue six FP16 MMAs per product (three "
-                                "9-bit slices a side), so the useful ceiling is 1/6 of that peak"}
+                                "(of measured). The fixed-point operands (three slices a side) issue eight FP16 MMAs "
+                                "per density product and six per adder product, so the useful ceiling is about 1/7 "
+                                "of that peak"}
             else:
                 peak = fp64_peak_tflops(torch)
                 roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
