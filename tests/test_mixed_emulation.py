@@ -1,0 +1,68 @@
+"""The CPU emulation of the mixed density arithmetic (tests/mixed_emulation.py): its exact
+part equals the oracle's basis values and gradients, its FP32 basis values carry the
+errors the kernel's arithmetic has (and none in the exact mode), and on one water the
+emulated mixed density integrates to the FP64 electron count within the slices' noise."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from serenity_gb300 import workload as wl
+
+import mixed_emulation as me
+
+
+@pytest.fixture(scope="module")
+def water():
+    sym, xyz = wl.water_cluster(1, seed=0, jitter=0.0)
+    w = wl.Workload(sym, xyz, "DEF2-SVP", "PBE", 5, 30, 110, seed=0)
+    pts, wts = po.becke_grid(w.Z, w.coords, n_rad=30, n_ang=110)
+    return w, pts, wts
+
+
+def _shells(w):
+    sh = w.shells
+    b = po.Basis(sh)
+    off = np.concatenate([[0], np.cumsum(sh.nprim)])
+    cen = np.asarray(sh.centers).reshape(-1, 3)
+    return sh, b, off, cen
+
+
+def test_exact_part_matches_oracle(water):
+    w, pts, _ = water
+    sh, b, off, cen = _shells(w)
+    xyz = pts[::7]
+    ref = b.block(xyz, 1e-9, deriv=1)
+    j = 0
+    for s in range(sh.nshell):
+        n = 2 * int(sh.l[s]) + 1
+        phi, grad, _, _, _ = me.shell_values(xyz, cen[s], int(sh.l[s]), sh.alpha[off[s]:off[s + 1]], b.shell_coefs(s))
+        np.testing.assert_allclose(phi, ref["values"][:, j:j + n], rtol=0, atol=1e-14)
+        for ax in range(3):
+            np.testing.assert_allclose(grad[ax], ref["grad"][ax][:, j:j + n], rtol=0, atol=1e-13)
+        j += n
+
+
+def test_fp32_values_carry_kernel_errors_and_exact_mode_none(water):
+    w, pts, _ = water
+    sh, b, off, cen = _shells(w)
+    xyz = pts[::3]
+    worst = {"kernel": 0.0, "exact": 0.0}
+    for s in range(sh.nshell):
+        for mode in worst:
+            phi, _, V, VL, _ = me.shell_values(xyz, cen[s], int(sh.l[s]), sh.alpha[off[s]:off[s + 1]], b.shell_coefs(s),
+                                               mode)
+            scale = max(np.abs(phi).max(), 1e-300)
+            worst[mode] = max(worst[mode], np.abs(V.astype(np.float64) + VL - phi).max() / scale)
+    assert worst["exact"] < 1e-14
+    assert 1e-10 < worst["kernel"] < 1e-6  # FP32 rounding of the offsets and angular parts
+
+
+def test_emulated_mixed_density_of_one_water(water):
+    w, pts, wts = water
+    P = np.asarray(w.density()).reshape(w.nbf, w.nbf)
+    dN, dE, N = me.density_errors(w.shells, pts, wts, P, "PBE", "kernel")
+    assert N == pytest.approx(10.0, abs=1e-3)
+    assert abs(dN) < 2e-7 and abs(dE) < 2e-7
+    # the exact basis values leave only the slices' and the epilogue's noise
+    dNx, dEx, _ = me.density_errors(w.shells, pts, wts, P, "PBE", "exact")
+    assert abs(dNx) < 2e-7 and abs(dEx) < 2e-7
