@@ -89,6 +89,8 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
 
     mode "kernel": the kernel's arithmetic; "offset_pair_p": the point-centre offset as an
     FP32 pair entering r^2, and p functions compensated (value = x R to second order);
+    "pairs": the offset pair, and the whole angular part (powers, monomials, x R, the
+    solid-harmonic sums) carried as FP32 pairs (error-free products by FMA, two-sum);
     "exact": the exact value split into FP32 high and low parts (gradients as in "kernel")."""
     ethr = -math.log(thr)
     d = xyz - A[None, :]
@@ -121,7 +123,7 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
     al = fl(A - ah.astype(f64))
     X = [(qh[:, i] - ah[i]) + (ql[:, i] - al[i]) for i in range(3)]
     XL = None
-    if mode == "offset_pair_p":
+    if mode in ("offset_pair_p", "pairs"):
         XL = []
         for i in range(3):
             s, e = two_sum(qh[:, i], -np.full_like(qh[:, i], ah[i]))
@@ -192,7 +194,33 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
                 svl[m] = fma(tl * np.ones_like(v), v, svl[m])
             for ax in range(3):
                 sg[ax][m] = fma(t * np.ones_like(v), g[ax], sg[ax][m])
-    if XL is not None and l == 1:
+    if mode == "pairs":
+        def pmul(ah_, al_, bh_, bl_):
+            h = ah_ * bh_
+            return h, fma(ah_, bh_, -h) + fma(ah_, bl_, al_ * bh_)
+        qx = [[np.ones_like(x), np.zeros_like(x)]]
+        qy = [[np.ones_like(x), np.zeros_like(x)]]
+        qz = [[np.ones_like(x), np.zeros_like(x)]]
+        for _ in range(l):
+            qx.append(list(pmul(qx[-1][0], qx[-1][1], x, XL[0])))
+            qy.append(list(pmul(qy[-1][0], qy[-1][1], y, XL[1])))
+            qz.append(list(pmul(qz[-1][0], qz[-1][1], z, XL[2])))
+        sh_ = [np.zeros_like(x) for _ in range(NS)]
+        sl_ = [np.zeros_like(x) for _ in range(NS)]
+        for k, (a, b, c) in enumerate(ks):
+            mh, ml = pmul(qx[a][0], qx[a][1], qy[b][0], qy[b][1])
+            mh, ml = pmul(mh, ml, qz[c][0], qz[c][1])
+            vh, vl_ = pmul(mh, ml, Rv, np.zeros_like(Rv))
+            for m in range(NS):
+                T = TS[l][m, k]
+                if T == 0.0:
+                    continue
+                t, tl = f32(T), f32(T - float(f32(T)))
+                ph, pl = pmul(t * np.ones_like(vh), tl * np.ones_like(vh), vh, vl_)
+                sh_[m], e = two_sum(sh_[m], ph)
+                sl_[m] = sl_[m] + (e + pl)
+        sv, svl = sh_, sl_
+    if XL is not None and l == 1 and mode == "offset_pair_p":
         for m in range(NS):
             ax = [i for i in range(3) if ks[int(np.nonzero(TS[1][m])[0][0])][i] == 1][0]
             svl[m] = fma(XL[ax], Rv, fma(X[ax], Rv, -sv[m]))
@@ -370,7 +398,7 @@ def main():
     from serenity_gb300 import workload as wl
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--basis", default="kernel", choices=["kernel", "offset_pair_p", "exact"])
+    ap.add_argument("--basis", default="kernel", choices=["kernel", "offset_pair_p", "pairs", "exact"])
     args = ap.parse_args()
     w = wl.config(args.config)
     if w.nspin != 1:
