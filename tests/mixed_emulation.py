@@ -91,6 +91,7 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
     FP32 pair entering r^2, and p functions compensated (value = x R to second order);
     "pairs": the offset pair, and the whole angular part (powers, monomials, x R, the
     solid-harmonic sums) carried as FP32 pairs (error-free products by FMA, two-sum);
+    "pairs_sterbenz": as "pairs" with the high parts' difference taken as exact;
     "exact": the exact value split into FP32 high and low parts (gradients as in "kernel")."""
     ethr = -math.log(thr)
     d = xyz - A[None, :]
@@ -123,10 +124,12 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
     al = fl(A - ah.astype(f64))
     X = [(qh[:, i] - ah[i]) + (ql[:, i] - al[i]) for i in range(3)]
     XL = None
-    if mode in ("offset_pair_p", "pairs"):
+    if mode in ("offset_pair_p", "pairs", "pairs_sterbenz"):
         XL = []
         for i in range(3):
             s, e = two_sum(qh[:, i], -np.full_like(qh[:, i], ah[i]))
+            if mode == "pairs_sterbenz":  # qh - ah taken as exact (it is when qh / ah is in [1/2, 2])
+                e = np.zeros_like(e)
             dl = (ql[:, i] - al[i]) + e
             X[i] = s + dl
             XL.append(dl - (X[i] - s))
@@ -194,7 +197,7 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
                 svl[m] = fma(tl * np.ones_like(v), v, svl[m])
             for ax in range(3):
                 sg[ax][m] = fma(t * np.ones_like(v), g[ax], sg[ax][m])
-    if mode == "pairs":
+    if mode in ("pairs", "pairs_sterbenz"):
         def pmul(ah_, al_, bh_, bl_):
             h = ah_ * bh_
             return h, fma(ah_, bh_, -h) + fma(ah_, bl_, al_ * bh_)
@@ -398,7 +401,7 @@ def main():
     from serenity_gb300 import workload as wl
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--basis", default="kernel", choices=["kernel", "offset_pair_p", "pairs", "exact"])
+    ap.add_argument("--basis", default="kernel", choices=["kernel", "offset_pair_p", "pairs", "pairs_sterbenz", "exact"])
     args = ap.parse_args()
     w = wl.config(args.config)
     if w.nspin != 1:
