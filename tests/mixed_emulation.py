@@ -272,13 +272,17 @@ def slice_digits(vh, vl, u):
     return s0.astype(f64), s1.astype(f64) / 512, s2.astype(f64) / 512
 
 
-def split_p(P):
-    """split_p_kernel: per column a power-of-two scale and three stored slices."""
+def split_p(P, exact=False):
+    """split_p_kernel: per column a power-of-two scale and three stored slices (exact: the
+    scaled column itself as the leading slice, for bounding what the slicing costs)."""
     n = P.shape[0]
     T0, T1, T2, sc = np.empty_like(P), np.empty_like(P), np.empty_like(P), np.empty(n)
     for j in range(n):
         e = np.frexp(np.abs(P[:, j]).max())[1]
         v = P[:, j] * 2.0 ** (8 - e)
+        if exact:
+            T0[:, j], T1[:, j], T2[:, j], sc[j] = v, 0.0, 0.0, 2.0 ** (e - 8)
+            continue
         s0 = np.rint(v)
         r1 = (v - s0) * 512
         s1 = np.rint(r1)
@@ -337,7 +341,7 @@ def block_density(V, VL, G32, Psl, g0):
 
 
 def density_errors(sh, pts, wts, P, func="PBE", basis_mode="kernel", chunk=8192, blocks=None, log=None,
-                   chunk_stride=1):
+                   chunk_stride=1, p_exact=False):
     """(dN_el, first-order dE_xc, N_el) of the emulated mixed density against FP64 for the
     density matrix P ([nbf, nbf] restricted, or [nspin, nbf, nbf] per spin) on the points
     (Hilbert-ordered, 128-point blocks).  With chunk_stride k only every k-th chunk of points
@@ -352,7 +356,7 @@ def density_errors(sh, pts, wts, P, func="PBE", basis_mode="kernel", chunk=8192,
     first = np.concatenate([[0], np.cumsum(2 * sh.l + 1)])
     alpha = [sh.alpha[off[s]:off[s + 1]] for s in range(sh.nshell)]
     cen = np.asarray(sh.centers).reshape(-1, 3)
-    Psl = [split_p(Ps[i]) for i in range(nspin)]
+    Psl = [split_p(Ps[i], p_exact) for i in range(nspin)]
     dN = dE = N = 0.0
     nblk = 0
     for ci_, c0 in enumerate(range(0, len(pts), chunk)):
@@ -414,14 +418,16 @@ def main():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--basis", default="kernel", choices=["kernel", "offset_pair_p", "pairs", "pairs_sterbenz", "exact"])
     ap.add_argument("--chunk-stride", type=int, default=1, help="emulate every k-th chunk of 8192 points (sampled)")
+    ap.add_argument("--p-exact", action="store_true", help="P unsliced (bounds the cost of its 27-bit slices)")
     args = ap.parse_args()
     w = wl.config(args.config)
     pts, wts = po.becke_grid(w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
     P = np.asarray(w.density()).reshape(w.nspin, w.nbf, w.nbf)
     dN, dE, N = density_errors(w.shells, pts, wts, P, w.func, args.basis, log=lambda m: print(m, flush=True),
-                               chunk_stride=args.chunk_stride)
-    print("basis %s%s: N_el %.10f  dN_el %+.4e  dE_xc (first order) %+.4e" % (
-        args.basis, " (every %d-th chunk, scaled)" % args.chunk_stride if args.chunk_stride > 1 else "", N, dN, dE))
+                               chunk_stride=args.chunk_stride, p_exact=args.p_exact)
+    print("basis %s%s%s: N_el %.10f  dN_el %+.4e  dE_xc (first order) %+.4e" % (
+        args.basis, ", P exact" if args.p_exact else "",
+        " (every %d-th chunk, scaled)" % args.chunk_stride if args.chunk_stride > 1 else "", N, dN, dE))
 
 
 if __name__ == "__main__":
