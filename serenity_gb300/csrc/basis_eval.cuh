@@ -190,28 +190,55 @@ __device__ __forceinline__ void shell_functions(R x, R y, R z, R Rv, R dR, R ddR
   }
 }
 
-// Same as shell_functions, with the transform coefficients as compile-time constants.
-// Emit(f, value, value_lo, dx, dy, dz): value_lo carries the rounding of the coefficients
-// to R (c - R(c) times the term), which is the same relative error of a function at
-// every point (sqrt(3) of the d functions, for one) and would otherwise bias it.
-template <class R, int L, int DERIV, class Emit>
-__device__ __forceinline__ void shell_functions_cx(R x, R y, R z, R Rv, R dR, bool pure, Emit&& emit) {
+// FP32 pairs (h + l, |l| about an ulp of h) and their error-free transformations:
+// products by FMA, sums by Knuth's two-sum (Ogita, Rump & Oishi, SIAM J. Sci. Comput.
+// 26 (2005) 1955), with explicit roundings so no contraction changes them.
+struct F2 {
+  float h, l;
+};
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  const float h = __fmul_rn(a.h, b.h);
+  return {h, fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -h)))};
+}
+__device__ __forceinline__ F2 f2_mul1(F2 a, float b) {  // pair times an FP32 number
+  const float h = __fmul_rn(a.h, b);
+  return {h, fmaf(a.l, b, fmaf(a.h, b, -h))};
+}
+__device__ __forceinline__ void f2_acc(F2& s, F2 p) {  // s += p
+  const float t = __fadd_rn(s.h, p.h), bp = __fsub_rn(t, s.h);
+  const float e = __fadd_rn(__fsub_rn(s.h, __fsub_rn(t, bp)), __fsub_rn(p.h, bp));
+  s.l = __fadd_rn(s.l, __fadd_rn(e, p.l));
+  s.h = t;
+}
+
+// Values and gradients of an l = L shell with the transform coefficients as
+// compile-time constants, the value carried as an FP32 pair.
+// Emit(f, value, value_lo, dx, dy, dz).  The point-centre offset comes as pairs (x + xl,
+// ...), and the monomials, the coefficients (with their FP32 rounding) and the
+// solid-harmonic sums are pair products and two-sums, so value + value_lo is the FP32
+// radial value Rv times the exact angular factor to about 2^-44: every FP32 rounding of
+// the angular part would otherwise be one relative error repeated wherever the same
+// offset recurs (on a radial shell of the function's own atom, at every atom of an
+// element), a bias rather than noise.  The gradients stay FP32.
+template <int L, int DERIV, class Emit>
+__device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, float dR, bool pure, Emit&& emit) {
   constexpr int NS = 2 * L + 1;
   constexpr cx::Table TS = cx::solid(L);
   constexpr cx::Table TC = cx::cartesian(L);
-  R px[L + 2], py[L + 2], pz[L + 2];
-  px[0] = py[0] = pz[0] = R(1);
+  F2 px[L + 1], py[L + 1], pz[L + 1];
+  px[0] = py[0] = pz[0] = F2{1.f, 0.f};
 #pragma unroll
-  for (int k = 1; k < L + 2; ++k) {
-    px[k] = px[k - 1] * x;
-    py[k] = py[k - 1] * y;
-    pz[k] = pz[k - 1] * z;
+  for (int k = 1; k <= L; ++k) {
+    px[k] = f2_mul(px[k - 1], x);
+    py[k] = f2_mul(py[k - 1], y);
+    pz[k] = f2_mul(pz[k - 1], z);
   }
-  R sv[NS], svl[NS], sg[3 * NS];
+  F2 sv[NS];
+  float sg[3 * NS];
 #pragma unroll
   for (int m = 0; m < NS; ++m) {
-    sv[m] = svl[m] = R(0);
-    sg[3 * m] = sg[3 * m + 1] = sg[3 * m + 2] = R(0);
+    sv[m] = F2{0.f, 0.f};
+    sg[3 * m] = sg[3 * m + 1] = sg[3 * m + 2] = 0.f;
   }
   int k = 0;
 #pragma unroll
@@ -219,26 +246,28 @@ __device__ __forceinline__ void shell_functions_cx(R x, R y, R z, R Rv, R dR, bo
 #pragma unroll
     for (int b = L - a; b >= 0; --b, ++k) {
       const int c = L - a - b;
-      const R mono = px[a] * py[b] * pz[c];
-      const R v = mono * Rv;
-      R g0 = R(0), g1 = R(0), g2 = R(0);
+      F2 mono = px[a];
+      if (b > 0) mono = a > 0 ? f2_mul(mono, py[b]) : py[b];
+      if (c > 0) mono = (a > 0 || b > 0) ? f2_mul(mono, pz[c]) : pz[c];
+      float g0 = 0.f, g1 = 0.f, g2 = 0.f;
       if (DERIV >= 1) {
-        const R dmx = a > 0 ? R(a) * px[a > 0 ? a - 1 : 0] * py[b] * pz[c] : R(0);
-        const R dmy = b > 0 ? R(b) * px[a] * py[b > 0 ? b - 1 : 0] * pz[c] : R(0);
-        const R dmz = c > 0 ? R(c) * px[a] * py[b] * pz[c > 0 ? c - 1 : 0] : R(0);
-        const R md = mono * dR;
-        g0 = dmx * Rv + md * x;
-        g1 = dmy * Rv + md * y;
-        g2 = dmz * Rv + md * z;
+        const float dmx = a > 0 ? float(a) * px[a > 0 ? a - 1 : 0].h * py[b].h * pz[c].h : 0.f;
+        const float dmy = b > 0 ? float(b) * px[a].h * py[b > 0 ? b - 1 : 0].h * pz[c].h : 0.f;
+        const float dmz = c > 0 ? float(c) * px[a].h * py[b].h * pz[c > 0 ? c - 1 : 0].h : 0.f;
+        const float md = mono.h * dR;
+        g0 = dmx * Rv + md * x.h;
+        g1 = dmy * Rv + md * y.h;
+        g2 = dmz * Rv + md * z.h;
       }
       if (pure) {
 #pragma unroll
         for (int m = 0; m < NS; ++m) {
-          const R t = R(TS.c[m][k]);
-          const R tl = R(TS.c[m][k] - (double)R(TS.c[m][k]));
           if (TS.c[m][k] != 0.0) {
-            sv[m] += t * v;
-            if (tl != R(0)) svl[m] = fmaf(tl, v, svl[m]);
+            const float t = float(TS.c[m][k]);
+            const float tl = float(TS.c[m][k] - (double)float(TS.c[m][k]));
+            F2 p = f2_mul1(mono, t);
+            if (tl != 0.f) p.l = fmaf(tl, mono.h, p.l);
+            f2_acc(sv[m], p);
             if (DERIV >= 1) {
               sg[3 * m] += t * g0;
               sg[3 * m + 1] += t * g1;
@@ -247,28 +276,35 @@ __device__ __forceinline__ void shell_functions_cx(R x, R y, R z, R Rv, R dR, bo
           }
         }
       } else {
-        const R t = R(TC.c[0][k]);
-        const R tl = R(TC.c[0][k] - (double)R(TC.c[0][k]));
-        emit(k, t * v, tl * v, t * g0, t * g1, t * g2);
+        const float t = float(TC.c[0][k]);
+        const float tl = float(TC.c[0][k] - (double)float(TC.c[0][k]));
+        F2 p = f2_mul1(mono, t);
+        if (tl != 0.f) p.l = fmaf(tl, mono.h, p.l);
+        const F2 v = f2_mul1(p, Rv);
+        emit(k, v.h, v.l, t * g0, t * g1, t * g2);
       }
     }
   }
   if (pure) {
 #pragma unroll
-    for (int m = 0; m < NS; ++m) emit(m, sv[m], svl[m], sg[3 * m], sg[3 * m + 1], sg[3 * m + 2]);
+    for (int m = 0; m < NS; ++m) {
+      const F2 v = f2_mul1(sv[m], Rv);
+      emit(m, v.h, v.l, sg[3 * m], sg[3 * m + 1], sg[3 * m + 2]);
+    }
   }
 }
 
-template <class R, int DERIV, class Emit>
-__device__ __forceinline__ void shell_functions_cx_l(int l, R x, R y, R z, R Rv, R dR, bool pure, Emit&& emit) {
+template <int DERIV, class Emit>
+__device__ __forceinline__ void shell_functions_px_l(int l, F2 x, F2 y, F2 z, float Rv, float dR, bool pure,
+                                                     Emit&& emit) {
   switch (l) {
-    case 0: shell_functions_cx<R, 0, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 1: shell_functions_cx<R, 1, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 2: shell_functions_cx<R, 2, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 3: shell_functions_cx<R, 3, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 4: shell_functions_cx<R, 4, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 5: shell_functions_cx<R, 5, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 6: shell_functions_cx<R, 6, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 0: shell_functions_px<0, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 1: shell_functions_px<1, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 2: shell_functions_px<2, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 3: shell_functions_px<3, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 4: shell_functions_px<4, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 5: shell_functions_px<5, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 6: shell_functions_px<6, DERIV>(x, y, z, Rv, dR, pure, emit); break;
     default: break;
   }
 }

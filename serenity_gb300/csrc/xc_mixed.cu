@@ -58,22 +58,32 @@ __device__ __forceinline__ int rec_nf(int info) { return (info >> 9) & 31; }
 __device__ __forceinline__ int rec_f0(int info) { return info >> 14; }
 
 // Evaluate one shell record at a point in FP32; Emit(f, value, value_lo, dx, dy, dz)
-// (value_lo: the coefficients' rounding, shell_functions_cx).
+// (value_lo: the angular part's and the coefficients' rounding, shell_functions_px).
 // Negligible shells (|R| below the radial threshold) emit zeros.  The radial factor is
 // summed as an FP32 pair (exp_tang2, products and sums with their rounding errors) and
 // *rlo receives R_lo / R_hi: all grid points of one radial shell of an atom share the
 // atom's functions' R, so its FP32 rounding would be the same error at all of them (and
 // at every atom of the element) instead of averaging out; value * (1 + *rlo) carries R
-// to ~2^-30 (the angular factors vary from point to point and stay FP32).
+// to ~2^-30.  The point-centre offset is a pair too: x = (p_hi - A_hi) + (p_lo - A_lo)
+// with the first difference's rounding kept (two-sum), so r^2 and the angular factors
+// see p - A to ~2^-48 instead of one FP32 rounding per coordinate.
 template <int DERIV, class Emit>
 __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __restrict__ prim4, const Pt& q,
                                              float expthr, float thr, float* rlo, Emit&& emit) {
-  const float x = (q.h[0] - r.ah[0]) + (q.l[0] - r.al[0]);
-  const float y = (q.h[1] - r.ah[1]) + (q.l[1] - r.al[1]);
-  const float z = (q.h[2] - r.ah[2]) + (q.l[2] - r.al[2]);
-  // r^2 = r2 + r2l (products by FMA, sums by two-sum): on a radial shell of the
-  // function's own atom r^2 is one number, so a rounding of it (or of alpha r^2) would be
-  // one relative error t 2^-25 of exp(-t) at every point of the shell
+  F2 d[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float s = __fsub_rn(q.h[i], r.ah[i]), bp = __fsub_rn(s, q.h[i]);
+    const float e = __fadd_rn(__fsub_rn(q.h[i], __fsub_rn(s, bp)), __fsub_rn(-r.ah[i], bp));
+    const float dl = __fadd_rn(__fsub_rn(q.l[i], r.al[i]), e);
+    const float h = __fadd_rn(s, dl);
+    d[i] = F2{h, __fsub_rn(dl, __fsub_rn(h, s))};
+  }
+  const float x = d[0].h, y = d[1].h, z = d[2].h;
+  // r^2 = r2 + r2l (products by FMA, sums by two-sum, the offsets' low parts to first
+  // order): on a radial shell of the function's own atom r^2 is one number, so a
+  // rounding of it (or of alpha r^2) would be one relative error t 2^-25 of exp(-t) at
+  // every point of the shell
   float r2 = __fmul_rn(x, x), r2l = fmaf(x, x, -r2);
   {
     const float yy = __fmul_rn(y, y), zz = __fmul_rn(z, z);
@@ -82,6 +92,7 @@ __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __
     const float s2 = __fadd_rn(s1, zz), b2 = __fsub_rn(s2, s1);
     const float e2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(zz, b2));
     r2l = __fadd_rn(__fadd_rn(r2l, __fadd_rn(e1, e2)), __fadd_rn(fmaf(y, y, -yy), fmaf(z, z, -zz)));
+    r2l = fmaf(2.f, fmaf(x, d[0].l, fmaf(y, d[1].l, __fmul_rn(z, d[2].l))), r2l);
     r2 = s2;
   }
   const int np = rec_nprim(r.info);
@@ -112,7 +123,7 @@ __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __
     return;
   }
   *rlo = Rv != 0.f ? __fdiv_rn(Rl, Rv) : 0.f;
-  shell_functions_cx_l<float, DERIV>(l, x, y, z, Rv, dR, rec_pure(r.info), emit);
+  shell_functions_px_l<DERIV>(l, d[0], d[1], d[2], Rv, dR, rec_pure(r.info), emit);
 }
 
 __device__ __forceinline__ ShellRec load_rec(const ShellRec* p) {

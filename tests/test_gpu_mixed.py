@@ -77,3 +77,24 @@ def test_mixed_vxc_vs_oracle(ctx, func, unrestricted, basis, spherical, etol, vt
     assert abs(nel - rnel) <= 1e-8 * rnel
     assert np.abs(V - rV).max() <= vtol, np.abs(V - rV).max()
     np.testing.assert_allclose(V, np.swapaxes(V, 1, 2), rtol=0, atol=1e-14)
+
+
+# The benchmark's own tolerance, |dE_xc| <= 1e-7 Eh and max|dVxc| <= 1e-7 against the
+# FP64 oracle, on cut-down forms of the benchmark workloads: (H2O)8 def2-SVP restricted
+# PBE on the 75 x 302 grid (543 600 points before the weight cut-off), and a def2-TZVP
+# tetramer, unrestricted PBE on the 99 x 434 grid.
+@pytest.mark.parametrize("nmol,dims,basis,nocc,n_rad,n_ang", [
+    (8, (2, 2, 2), "DEF2-SVP", 40, 75, 302),
+    (4, (2, 2, 1), "DEF2-TZVP", (20, 19), 99, 434)])
+def test_mixed_vxc_benchmark_tolerance(ctx, nmol, dims, basis, nocc, n_rad, n_ang):
+    from serenity_gb300 import xcgpu
+    sym, xyz = wl.water_cluster(nmol, 0, jitter=0.2, dims=dims)
+    w = wl.Workload(sym, xyz, basis, "PBE", nocc, n_rad, n_ang, 0)
+    pts, wts = po.becke_grid(w.Z, w.coords, n_rad=n_rad, n_ang=n_ang)
+    plan = _plan(ctx, w, pts, wts)
+    P = w.density()
+    V, exc, nel = plan.vxc("PBE", P, precision=xcgpu.PREC_MIXED)
+    rV, rexc, rnel = po.Basis(w.shells).vxc(pts, wts, "PBE", P)
+    assert abs(exc - rexc) <= 1e-7, abs(exc - rexc)
+    assert abs(nel - rnel) <= 1e-8 * rnel, abs(nel - rnel)
+    assert np.abs(V - rV).max() <= 1e-7, np.abs(V - rV).max()
