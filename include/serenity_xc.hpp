@@ -318,7 +318,7 @@ class DensityOnGridCalculator {
 
 enum class FUNCTIONAL_DATA_TYPE { GRADIENTS };
 /* composite functionals of this path (CompositeFunctionals.cpp:233-246) */
-enum class Functional { LDA = XCGPU_FUNC_LDA, PBE = XCGPU_FUNC_PBE, BLYP = XCGPU_FUNC_BLYP };
+enum class Functional { LDA = XCGPU_FUNC_LDA, PBE = XCGPU_FUNC_PBE, BLYP = XCGPU_FUNC_BLYP, BP86 = XCGPU_FUNC_BP86 };
 
 template <Options::SCF_MODES M>
 struct FunctionalData {

@@ -53,13 +53,16 @@ enum {
   XCGPU_FUNC_LDA = 1,  /* Slater + VWN5 */
   XCGPU_FUNC_PBE = 2,  /* PBE exchange + PBE correlation */
   XCGPU_FUNC_BLYP = 3, /* Becke 88 + LYP */
+  XCGPU_FUNC_BP86 = 4, /* Becke 88 + P86 (PZ81 + Perdew 86 gradient correction) */
   XCGPU_FUNC_SLATER = 16,
   XCGPU_FUNC_VWN5 = 17,
   XCGPU_FUNC_PBEX = 18,
   XCGPU_FUNC_PBEC = 19,
   XCGPU_FUNC_B88 = 20,
   XCGPU_FUNC_LYP = 21,
-  XCGPU_FUNC_PW92 = 22
+  XCGPU_FUNC_PW92 = 22,
+  XCGPU_FUNC_P86 = 23, /* PZ81 + the Perdew 86 gradient correction (C_P86) */
+  XCGPU_FUNC_PZ81 = 24 /* Perdew-Zunger 1981 local correlation */
 };
 
 typedef struct xcgpu_ctx xcgpu_ctx;

@@ -15,6 +15,11 @@
  *   B88 exchange           Becke, PRA 38, 3098 (1988)
  *   LYP correlation        Lee, Yang, Parr, PRB 37, 785 (1988), Miehlich et al. form
  *                          (CPL 157, 200 (1989))
+ *   PZ81 correlation       Perdew, Zunger, PRB 23, 5048 (1981), their parametrisation of
+ *                          the Ceperley-Alder correlation energy (Table XII / eqs. C1, C3)
+ *   P86 correlation        Perdew, PRB 33, 8822 (1986), erratum PRB 34, 7406 (1986):
+ *                          PZ81 plus the gradient correction of eqs. (6), (8), (9)
+ *                          (the reference's BP86 = X_B88 + C_P86, CompositeFunctionals.cpp:244)
  *
  * Density cut-offs: a point whose total density is below 1e-14 contributes
  * nothing (the reference sets libxc's dens_threshold to 1e-14, LibXC.cpp:86-97);
@@ -338,6 +343,43 @@ template <class T> T lyp(const T& na, const T& nb, const T& saa, const T& sab, c
   return t1 - a * b * omega * inner;
 }
 
+/* ---- PZ81: eps_c(rs) of the unpolarised (U) and fully polarised (P) gas ---- */
+template <class T> T pz81_eps(const T& rs, double g, double b1, double b2, double A, double B, double C, double D) {
+  if (rs.v >= 1.0) return g / (1.0 + b1 * sqrt(rs) + b2 * rs);
+  T l = log(rs);
+  return A * l + B + C * rs * l + D * rs;
+}
+template <class T> T pz81(const T& na, const T& nb) {
+  T n = na + nb;
+  T rs = cbrt(3.0 / (4.0 * M_PI * n));
+  T z = clamp_zeta((na - nb) / n);
+  T eU = pz81_eps(rs, -0.1423, 1.0529, 0.3334, 0.0311, -0.048, 0.0020, -0.0116);
+  T eP = pz81_eps(rs, -0.0843, 1.3981, 0.2611, 0.01555, -0.0269, 0.0007, -0.0048);
+  return n * (eU + fzeta(z) * (eP - eU));
+}
+
+/* ---- P86 gradient correction: e = exp(-Phi) C(n) |grad n|^2 / (d n^(4/3)) ----
+ *   C(n) = 0.001667 + (0.002568 + a rs + b rs^2) / (1 + g rs + h rs^2 + 1e4 b rs^3),
+ *   Phi = (9 pi)^(1/6) f (C(inf) / C(n)) |grad n| / n^(7/6), f = 0.11, C(inf) = 0.004235
+ *         (the paper's 1.745 is (9 pi)^(1/6) = 1.745415 rounded; the unrounded factor
+ *         reproduces the reference's BP86 Fock matrices, the rounded one misses by 8e-6),
+ *   d = 2^(1/3) sqrt(((1 + z)/2)^(5/3) + ((1 - z)/2)^(5/3)) */
+template <class T> T p86_corr(const T& na, const T& nb, const T& saa, const T& sab, const T& sbb) {
+  const double a = 0.023266, b = 7.389e-6, g = 8.723, h = 0.472, c1 = 0.001667, c2 = 0.002568;
+  T n = na + nb;
+  T rs = cbrt(3.0 / (4.0 * M_PI * n));
+  T Cn = c1 + (c2 + a * rs + b * rs * rs) / (1.0 + g * rs + h * rs * rs + 1e4 * b * rs * rs * rs);
+  T sigma = saa + 2.0 * sab + sbb;
+  // |grad n| = sqrt(sigma); floored so the derivative of sqrt stays finite at sigma = 0
+  // (sigma exp(-Phi) itself has a finite first derivative there)
+  T gn = sigma.v > 1e-300 ? sqrt(sigma) : T(0.0);
+  T n16 = pow(n, 1.0 / 6.0);
+  T phi = (std::pow(9.0 * M_PI, 1.0 / 6.0) * 0.11 * (c1 + c2)) / Cn * gn / (n * n16);
+  T z = clamp_zeta((na - nb) / n);
+  T d = std::cbrt(2.0) * sqrt(pow(0.5 * (1.0 + z), 5.0 / 3.0) + pow(0.5 * (1.0 - z), 5.0 / 3.0));
+  return exp(-phi) * Cn * sigma / (d * pow43(n));
+}
+
 template <class T> T energy(int func, const T& na, const T& nb, const T& saa, const T& sab, const T& sbb) {
   switch (func) {
     case ORC_FUNC_LDA: return slater(na, nb) + vwn5(na, nb);
@@ -350,6 +392,9 @@ template <class T> T energy(int func, const T& na, const T& nb, const T& saa, co
     case ORC_FUNC_B88: return b88(na, nb, saa, sbb);
     case ORC_FUNC_LYP: return lyp(na, nb, saa, sab, sbb);
     case ORC_FUNC_PW92: return pw92(na, nb);
+    case ORC_FUNC_BP86: return b88(na, nb, saa, sbb) + pz81(na, nb) + p86_corr(na, nb, saa, sab, sbb);
+    case ORC_FUNC_P86: return pz81(na, nb) + p86_corr(na, nb, saa, sab, sbb);
+    case ORC_FUNC_PZ81: return pz81(na, nb);
   }
   return T(0.0);
 }
@@ -357,6 +402,7 @@ template <class T> T energy(int func, const T& na, const T& nb, const T& saa, co
 bool functional_is_gga(int func) {
   switch (func) {
     case ORC_FUNC_PBE: case ORC_FUNC_BLYP: case ORC_FUNC_PBEX: case ORC_FUNC_PBEC: case ORC_FUNC_B88: case ORC_FUNC_LYP:
+    case ORC_FUNC_BP86: case ORC_FUNC_P86:
       return true;
   }
   return false;

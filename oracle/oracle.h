@@ -30,13 +30,16 @@ enum {
   ORC_FUNC_LDA = 1,  /* Slater + VWN5          (CompositeFunctionals.cpp:233-235) */
   ORC_FUNC_PBE = 2,  /* PBE x + PBE c          (CompositeFunctionals.cpp:242-244) */
   ORC_FUNC_BLYP = 3, /* B88 + LYP              (CompositeFunctionals.cpp:239-241) */
+  ORC_FUNC_BP86 = 4, /* B88 + P86              (CompositeFunctionals.cpp:244-246) */
   ORC_FUNC_SLATER = 16,
   ORC_FUNC_VWN5 = 17,
   ORC_FUNC_PBEX = 18,
   ORC_FUNC_PBEC = 19,
   ORC_FUNC_B88 = 20,
   ORC_FUNC_LYP = 21,
-  ORC_FUNC_PW92 = 22
+  ORC_FUNC_PW92 = 22,
+  ORC_FUNC_P86 = 23, /* PZ81 + the P86 gradient correction (xcfun "p86c") */
+  ORC_FUNC_PZ81 = 24
 };
 
 /* Basis: shells with raw (file) contraction coefficients; the oracle applies the

@@ -13,8 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-FUNC = {"LDA": 1, "PBE": 2, "BLYP": 3, "SLATER": 16, "VWN5": 17, "PBEX": 18, "PBEC": 19, "B88": 20, "LYP": 21,
-        "PW92": 22}
+FUNC = {"LDA": 1, "PBE": 2, "BLYP": 3, "BP86": 4, "SLATER": 16, "VWN5": 17, "PBEX": 18, "PBEC": 19, "B88": 20,
+        "LYP": 21, "PW92": 22, "P86": 23, "PZ81": 24}
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

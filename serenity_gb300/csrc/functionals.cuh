@@ -9,6 +9,10 @@
 //   B88           Becke, PRA 38, 3098 (1988) (includes the Slater part)
 //   LYP           Lee, Yang, Parr, PRB 37, 785 (1988), Miehlich et al. form,
 //                 CPL 157, 200 (1989)
+//   PZ81          Perdew, Zunger, PRB 23, 5048 (1981), their fit of the Ceperley-Alder
+//                 correlation energy
+//   P86           Perdew, PRB 33, 8822 (1986): PZ81 plus a gradient correction (BP86 =
+//                 B88 + P86, CompositeFunctionals.cpp:244)
 // Cut-offs: no contribution below a total density of 1e-14 (the reference sets
 // libxc's dens_threshold to 1e-14, LibXC.cpp:86-97); a spin channel below 0.5e-14
 // carries no exchange; |zeta| <= 1 - 1e-12 in the correlation functionals.
@@ -318,12 +322,99 @@ __device__ __forceinline__ void lyp(R na, R nb, R saa, R sab, R sbb, R& e, R& va
   vsbb -= ab * omega * dIsbb;
 }
 
+// ---- PZ81: eps(rs) of one spin state and d eps / d rs ----
+template <class R>
+__device__ __forceinline__ void pz81_g(R rs, double g, double b1, double b2, double A, double B, double C, double D,
+                                       R& eps, R& deps) {
+  if (rs >= R(1)) {
+    const R srs = sqrt_<R>(rs);
+    const R den = R(1) + R(b1) * srs + R(b2) * rs;
+    eps = R(g) / den;
+    deps = -R(g) * (R(0.5 * b1) / srs + R(b2)) / (den * den);
+  } else {
+    const R l = log_<R>(rs);
+    eps = R(A) * l + R(B) + R(C) * rs * l + R(D) * rs;
+    deps = R(A) / rs + R(C) * (l + R(1)) + R(D);
+  }
+}
+
+// PZ81 correlation, spin-polarised (f(zeta) interpolation); adds e and de/dna, de/dnb
+template <class R>
+__device__ __forceinline__ void pz81(R na, R nb, R& e, R& va, R& vb) {
+  const R n = na + nb;
+  const R rs = cbrt_<R>(R(3.0 / (4.0 * kPi)) / n);
+  R zs;
+  const R z = clampz((na - nb) / n, zs);
+  R eps, dr, dz = R(0);
+  pz81_g(rs, -0.1423, 1.0529, 0.3334, 0.0311, -0.048, 0.0020, -0.0116, eps, dr);
+  if (z != R(0)) {
+    R eP, dP, f, df;
+    pz81_g(rs, -0.0843, 1.3981, 0.2611, 0.01555, -0.0269, 0.0007, -0.0048, eP, dP);
+    fzeta(z, f, df);
+    dz = zs * df * (eP - eps);
+    eps += f * (eP - eps);
+    dr += f * (dP - dr);
+  }
+  e += n * eps;
+  const R base = eps - rs / R(3) * dr;
+  va += base + (R(1) - z) * dz;
+  vb += base - (R(1) + z) * dz;
+}
+
+// ---- P86 gradient correction, e = exp(-Phi) C(n) sigma / (d(zeta) n^(4/3)):
+//   C(n) = c1 + (c2 + a rs + b rs^2) / (1 + g rs + h rs^2 + 1e4 b rs^3),
+//   Phi = (9 pi)^(1/6) 0.11 (C(inf) / C(n)) sigma^(1/2) / n^(7/6), C(inf) = c1 + c2,
+//   d = 2^(1/3) sqrt(((1 + z)/2)^(5/3) + ((1 - z)/2)^(5/3)).
+// The paper prints (9 pi)^(1/6) rounded to 1.745; the unrounded factor reproduces the
+// reference's BP86 Fock matrices (FuncPotential_test.cpp:148-232).  de/dsigma =
+// e (1 - Phi/2) / sigma has no singularity at sigma = 0.
+template <class R>
+__device__ __forceinline__ void p86corr(R na, R nb, R saa, R sab, R sbb, R& e, R& va, R& vb, R& vsaa, R& vsab,
+                                        R& vsbb) {
+  constexpr double a = 0.023266, b = 7.389e-6, g = 8.723, h = 0.472, c1 = 0.001667, c2 = 0.002568;
+  constexpr double K = 0.19199566167376364 * (c1 + c2);  // (9 pi)^(1/6) 0.11 C(inf)
+  const R n = na + nb;
+  const R rs = cbrt_<R>(R(3.0 / (4.0 * kPi)) / n);
+  const R num = R(c2) + R(a) * rs + R(b) * rs * rs;
+  const R den = R(1) + R(g) * rs + R(h) * rs * rs + R(1e4 * b) * rs * rs * rs;
+  const R C = R(c1) + num / den;
+  const R dC_drs = ((R(a) + R(2 * b) * rs) * den - num * (R(g) + R(2 * h) * rs + R(3e4 * b) * rs * rs)) / (den * den);
+  const R sigma = saa + R(2) * sab + sbb;
+  const R sg = sigma > R(0) ? sqrt_<R>(sigma) : R(0);
+  const R n13 = cbrt_<R>(n);
+  const R n16 = sqrt_<R>(n13);
+  const R phi = R(K) / C * sg / (n * n16);
+  const R E = exp_<R>(-phi);
+  R zs;
+  const R z = clampz((na - nb) / n, zs);
+  R dinv = R(1), dlog = R(0);  // 1/d and d'(z)/d
+  if (z != R(0)) {
+    const R up = R(0.5) * (R(1) + z), dn = R(0.5) * (R(1) - z);
+    const R u23 = cbrt_<R>(up * up), d23 = cbrt_<R>(dn * dn);
+    const R A = up * u23 + dn * d23;
+    dinv = R(1) / (R(1.2599210498948732) * sqrt_<R>(A));  // 2^(1/3)
+    dlog = zs * R(5.0 / 6.0) * (u23 - d23) / (R(2) * A);
+  }
+  const R pre = E * C * dinv / (n * n13);  // exp(-Phi) C / (d n^(4/3))
+  const R ec = pre * sigma;
+  const R dC_dn = -rs / (R(3) * n) * dC_drs;
+  const R den_ = ec * ((R(1) + phi) * dC_dn / C + (R(7.0 / 6.0) * phi - R(4.0 / 3.0)) / n);
+  const R dez = -ec * dlog;  // de/dzeta
+  e += ec;
+  va += den_ + (R(1) - z) / n * dez;
+  vb += den_ - (R(1) + z) / n * dez;
+  const R vs = pre * (R(1) - R(0.5) * phi);
+  vsaa += vs;
+  vsab += R(2) * vs;
+  vsbb += vs;
+}
+
 __host__ __device__ inline bool is_gga(int func) {
   return func == XCGPU_FUNC_PBE || func == XCGPU_FUNC_BLYP || func == XCGPU_FUNC_PBEX || func == XCGPU_FUNC_PBEC ||
-         func == XCGPU_FUNC_B88 || func == XCGPU_FUNC_LYP;
+         func == XCGPU_FUNC_B88 || func == XCGPU_FUNC_LYP || func == XCGPU_FUNC_BP86 || func == XCGPU_FUNC_P86;
 }
 __host__ __device__ inline bool is_known(int func) {
-  return func == XCGPU_FUNC_LDA || func == XCGPU_FUNC_PBE || func == XCGPU_FUNC_BLYP || (func >= 16 && func <= 22);
+  return (func >= XCGPU_FUNC_LDA && func <= XCGPU_FUNC_BP86) || (func >= 16 && func <= 24);
 }
 
 // restricted point: e, de/dn, de/dsigma
@@ -366,7 +457,18 @@ __device__ __forceinline__ void eval_restricted(int func, R n, R sigma, R& e, R&
       }
       break;
     }
+    case XCGPU_FUNC_PZ81:
+    case XCGPU_FUNC_P86: {
+      R va = R(0), vb = R(0), vaa = R(0), vab = R(0), vbb = R(0);
+      const R q = R(0.25) * sigma;
+      pz81(h, h, e, va, vb);
+      if (func == XCGPU_FUNC_P86) p86corr(h, h, q, q, q, e, va, vb, vaa, vab, vbb);
+      vn += R(0.5) * (va + vb);
+      vs += R(0.25) * (vaa + vab + vbb);
+      break;
+    }
     case XCGPU_FUNC_BLYP:
+    case XCGPU_FUNC_BP86:
     case XCGPU_FUNC_B88:
     case XCGPU_FUNC_LYP: {
       if (func != XCGPU_FUNC_LYP) {
@@ -377,7 +479,14 @@ __device__ __forceinline__ void eval_restricted(int func, R n, R sigma, R& e, R&
         vn += vns;
         vs += R(0.5) * vss;
       }
-      if (func != XCGPU_FUNC_B88) {
+      if (func == XCGPU_FUNC_BP86) {
+        R va = R(0), vb = R(0), vaa = R(0), vab = R(0), vbb = R(0);
+        const R q = R(0.25) * sigma;
+        pz81(h, h, e, va, vb);
+        p86corr(h, h, q, q, q, e, va, vb, vaa, vab, vbb);
+        vn += R(0.5) * (va + vb);
+        vs += R(0.25) * (vaa + vab + vbb);
+      } else if (func != XCGPU_FUNC_B88) {
         R va = R(0), vb = R(0), vaa = R(0), vab = R(0), vbb = R(0);
         const R q = R(0.25) * sigma;
         lyp(h, h, q, q, q, e, va, vb, vaa, vab, vbb);
@@ -431,7 +540,13 @@ __device__ __forceinline__ void eval_unrestricted(int func, R na, R nb, R saa, R
       }
       if (func != XCGPU_FUNC_PBEX) pbec(na, nb, saa, sab, sbb, e, va, vb, vaa, vab, vbb);
       break;
+    case XCGPU_FUNC_PZ81:
+    case XCGPU_FUNC_P86:
+      pz81(na, nb, e, va, vb);
+      if (func == XCGPU_FUNC_P86) p86corr(na, nb, saa, sab, sbb, e, va, vb, vaa, vab, vbb);
+      break;
     case XCGPU_FUNC_BLYP:
+    case XCGPU_FUNC_BP86:
     case XCGPU_FUNC_B88:
     case XCGPU_FUNC_LYP:
       if (func != XCGPU_FUNC_LYP) {
@@ -440,7 +555,12 @@ __device__ __forceinline__ void eval_unrestricted(int func, R na, R nb, R saa, R
         b88_spin(na, saa, e, va, vaa);
         b88_spin(nb, sbb, e, vb, vbb);
       }
-      if (func != XCGPU_FUNC_B88) lyp(na, nb, saa, sab, sbb, e, va, vb, vaa, vab, vbb);
+      if (func == XCGPU_FUNC_BP86) {
+        pz81(na, nb, e, va, vb);
+        p86corr(na, nb, saa, sab, sbb, e, va, vb, vaa, vab, vbb);
+      } else if (func != XCGPU_FUNC_B88) {
+        lyp(na, nb, saa, sab, sbb, e, va, vb, vaa, vab, vbb);
+      }
       break;
     default:
       break;

@@ -15,8 +15,8 @@ from . import build as _build
 
 MEM_HOST, MEM_DEVICE = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-FUNC = {"LDA": 1, "PBE": 2, "BLYP": 3, "SLATER": 16, "VWN5": 17, "PBEX": 18, "PBEC": 19, "B88": 20, "LYP": 21,
-        "PW92": 22}
+FUNC = {"LDA": 1, "PBE": 2, "BLYP": 3, "BP86": 4, "SLATER": 16, "VWN5": 17, "PBEX": 18, "PBEC": 19, "B88": 20,
+        "LYP": 21, "PW92": 22, "P86": 23, "PZ81": 24}
 STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NO_MEMORY", 4: "BUDGET", 5: "UNSUPPORTED", 6: "TIMEOUT", 7: "IO"}
 
 

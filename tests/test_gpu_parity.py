@@ -91,8 +91,9 @@ def test_grid_builder_matches_oracle(ctx, golden):
     np.testing.assert_allclose(w, rw, rtol=1e-11, atol=1e-14)
 
 
+@pytest.mark.parametrize("func", ["LDA", "BP86"])
 @pytest.mark.parametrize("unrestricted", [False, True])
-def test_h2_lda_fock_matrix(ctx, golden, unrestricted):
+def test_h2_fock_matrix(ctx, golden, func, unrestricted):
     from serenity_gb300 import xcgpu
     d, sym, xyz = _h2(golden)
     gs = d["grid_settings"]
@@ -101,8 +102,8 @@ def test_h2_lda_fock_matrix(ctx, golden, unrestricted):
     b = xcgpu.Basis(ctx, Shells.for_atoms(sym, xyz, d["basis"], spherical=d["spherical"]))
     plan = xcgpu.Plan(ctx, g, b, int(gs["BLOCKSIZE"]), float(gs["BASFUNCRADIALTHRESHOLD"]))
     Pm = np.stack([d["Pa"], d["Pb"]]) if unrestricted else np.array(d["P"])
-    V, exc, nel = plan.vxc("LDA", Pm, block_ave_threshold=float(gs["BLOCKAVETHRESHOLD"]))
-    F = np.array(d["F"]["LDA_UNRES" if unrestricted else "LDA"])
+    V, exc, nel = plan.vxc(func, Pm, block_ave_threshold=float(gs["BLOCKAVETHRESHOLD"]))
+    F = np.array(d["F"][func + "_UNRES" if unrestricted else func])
     for s in range(V.shape[0]):
         np.testing.assert_allclose(V[s], F, rtol=0, atol=d["tolerance"])
     assert abs(nel - 2.0) < 1e-5
@@ -117,7 +118,8 @@ def _random_points(n, nspin, seed):
     return rho, grad
 
 
-@pytest.mark.parametrize("func", ["SLATER", "VWN5", "PW92", "PBEX", "PBEC", "B88", "LYP", "LDA", "PBE", "BLYP"])
+@pytest.mark.parametrize("func", ["SLATER", "VWN5", "PW92", "PBEX", "PBEC", "B88", "LYP", "PZ81", "P86", "LDA", "PBE",
+                                  "BLYP", "BP86"])
 @pytest.mark.parametrize("nspin", [1, 2])
 def test_functional_vs_oracle(ctx, func, nspin):
     rho, grad = _random_points(4000, nspin, 7 + nspin)
@@ -137,8 +139,8 @@ def _small_case(func, unrestricted, seed=3):
     return w, pts, wts
 
 
-@pytest.mark.parametrize("func,unrestricted", [("LDA", False), ("PBE", False), ("BLYP", False), ("PBE", True),
-                                               ("LDA", True)])
+@pytest.mark.parametrize("func,unrestricted", [("LDA", False), ("PBE", False), ("BLYP", False), ("BP86", False),
+                                               ("PBE", True), ("LDA", True), ("BP86", True)])
 def test_vxc_vs_oracle_water_tetramer(ctx, func, unrestricted):
     from serenity_gb300 import xcgpu
     w, pts, wts = _small_case(func, unrestricted)
