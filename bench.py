@@ -32,9 +32,18 @@ sys.path.insert(0, ROOT)
 
 METRIC = "XC builds/s & Mpts/s, (H2O)32 PBE, mixed vs FP64 GPU at 1e-7 Eh; p50/p99 latency"
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the whole-build mixed kernel
-# on the (H2O)32 workload, from one ncu --set full capture (profiles/mx_build_h2o32_pbe.md)
+# on the (H2O)32 workload, from one ncu capture of that kernel
 MIXED_DRAM_BYTES = {"build": 941.1e6 + 5.2e6}
-WORKLOAD = "(H2O)32 def2-SVP PBE restricted, 75x302 Becke grid, 128-point blocks"
+WORKLOADS = {0: "(H2O)4 def2-SVP LDA restricted, 50x194 Becke grid, 128-point blocks",
+             1: "(H2O)32 def2-SVP PBE restricted, 75x302 Becke grid, 128-point blocks",
+             2: "(H2O)64 def2-TZVP PBE unrestricted, 99x434 Becke grid, 128-point blocks"}
+
+
+def bench_config(config, npoints, nbf, nblocks, mean_active, world):
+    """The workload description both arms print (identical keys and values)."""
+    return {"workload": WORKLOADS[config], "npoints": int(npoints), "nbf": int(nbf), "nblocks": int(nblocks),
+            "mean_active": float(mean_active), "parallelism": "replicas" if world > 1 else "single",
+            "l2": "GPU arm: L2 flushed between steps (512 MB write, outside the timed events); CPU arm: host memory"}
 
 
 def dist_env():
@@ -290,18 +299,51 @@ def run_extra(args):
     line = {"metric": "serving loop: Poisson stream of Vxc requests (1-128 waters, SVP/TZVP 70/30, LDA/PBE 50/50, "
                       "50x110 grids), continuous batching under a 40 GB HBM budget",
             "unit": "requests/s", "rate_req_s": args.rate, "requests": args.requests, "data": "synthetic"}
-    server = serve.Server(ctx, hbm_budget=40 << 30, max_batch=64)
+    server = serve.Server(ctx, hbm_budget=40 << 30, max_batch=64, max_batch_flops=args.batch_flops)
     reqs, setup_s = serve.make_requests(server, n=args.requests, rate=args.rate, seed=args.seed)
     line["setup_s"] = setup_s
     line["resident_geometries"] = len(server.cache)
+    line["max_batch_flops"] = args.batch_flops
+
+    def at_rate(rate, k=None):
+        """The same stream, its arrival times scaled to `rate` requests/s."""
+        out = []
+        for r in reqs[:k]:
+            q = r.fresh()
+            q.arrival = r.arrival * args.rate / rate
+            out.append(q)
+        return out
+
     # the FP64 leg serves the first --fp64-requests requests of the same stream (at the
     # same arrival rate it runs far behind, so the whole stream would take many minutes)
     for name, p, k in [("mixed", xcgpu.PREC_MIXED, len(reqs)), ("fp64", xcgpu.PREC_FP64, args.fp64_requests)]:
         server.precision = p
         torch.cuda.synchronize()
-        line[name] = server.run([r.fresh() for r in reqs[:k]], keep_results=False)
+        line[name] = server.run(at_rate(args.rate, k), keep_results=False)
         torch.cuda.synchronize()
     line["value"] = line["mixed"]["throughput_req_s"]
+    # mixed: the rate sweep without admission control, and the sustainable rate (the
+    # highest at which p99 stays within 10x p50); then each rate with a latency budget
+    server.precision = xcgpu.PREC_MIXED
+    sweep = []
+    for rate in args.rates:
+        torch.cuda.synchronize()
+        st = server.run(at_rate(rate), keep_results=False)
+        st["rate_req_s"] = rate
+        sweep.append(st)
+    line["rate_sweep"] = sweep
+    ok = [st["rate_req_s"] for st in sweep if st["p99_ms"] <= 10.0 * st["p50_ms"]]
+    line["sustainable_rate_req_s"] = max(ok) if ok else None
+    if args.latency_budget_ms > 0:
+        server.latency_budget_s = args.latency_budget_ms / 1e3
+        adm = []
+        for rate in args.rates:
+            torch.cuda.synchronize()
+            st = server.run(at_rate(rate), keep_results=False)
+            st["rate_req_s"] = rate
+            adm.append(st)
+        server.latency_budget_s = None
+        line["admission"] = {"latency_budget_ms": args.latency_budget_ms, "runs": adm}
     print(json.dumps(line))
 
 
@@ -371,6 +413,12 @@ def main():
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rate", type=float, default=100.0)
     ap.add_argument("--fp64-requests", type=int, default=300, help="serving: requests of the FP64 comparison leg")
+    ap.add_argument("--rates", type=lambda x: [float(v) for v in x.split(",")], default=[25.0, 50.0, 75.0, 100.0],
+                    help="serving: arrival rates of the mixed-precision sweep")
+    ap.add_argument("--latency-budget-ms", type=float, default=1000.0,
+                    help="serving: admission's latency budget for the sweep's second pass (0: none)")
+    ap.add_argument("--batch-flops", type=float, default=2e12,
+                    help="serving: cap on a batch's estimated contraction flops")
     args = ap.parse_args()
     if args.workload != "single":
         return run_extra(args)
@@ -382,14 +430,13 @@ def main():
             dist.close()
             return
         from oracle import pyoracle as po
-        from serenity_gb300 import xcgpu
         w, P = build_workload(args)
-        # the same grid the GPU arm integrates on (built by the library's grid builder)
-        import torch  # noqa: F401
-        ctx = xcgpu.Context(device=0)
-        grid = xcgpu.Grid.build(ctx, w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
-        pts = grid.points()
-        ctx.close()
+        # the grid the GPU arm integrates on, built by the oracle's restatement of the
+        # reference's grid factory (equal to the library's builder to 1e-12); nothing of the
+        # product library is loaded in this arm
+        pts = po.becke_grid(w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
+        nblocks = (len(pts[1]) + 127) // 128
+        mean_active = po.Basis(w.shells).active_functions(pts[0]) / nblocks
         lat = []
         for i in range(args.warmup + args.steps):
             dt, V, exc, nel = cpu_baseline(w, P, pts, threads=0)
@@ -401,12 +448,13 @@ def main():
             "metric": METRIC, "impl": "reference", "value": value, "unit": "builds/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "npoints": len(pts[1]), "nbf": w.nbf, "precision": "fp64",
-                       "l2": "inputs larger than L2 (CPU run)"},
+            "config": bench_config(args.config, len(pts[1]), w.nbf, nblocks, mean_active, dist.world),
+            "precision": "fp64",
             "mpts_per_s": len(pts[1]) * value / 1e6,
             "cpu_baseline": {"value": value, "unit": "builds/s", "cores": ncores, "kind": "port",
-                             "sample": "full builds of the workload, reference-algorithm restatement (oracle/), "
-                                       "OpenMP over 128-point blocks"},
+                             "sample": "full builds of the workload, reference-algorithm restatement (oracle/): "
+                                       "OpenMP over 128-point blocks, per-block register-blocked GEMMs, basis "
+                                       "evaluated for the active functions, twice per build as in the reference"},
             "e2e": {"value": value, "unit": "builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "exc": exc, "nel": nel,
         }
@@ -433,17 +481,17 @@ def main():
             dom_ms = kms[dom] / steps
             achieved = (flops * share) / (dom_ms / 1e3) / 1e12
             if name == "mixed":
-                peak = peaks.get("bf16_tflops_sustained")
+                peak = peaks.get("bf16_tflops")
                 roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                         "frac": (achieved / peak) if peak else None,
                         "traffic": MIXED_DRAM_BYTES.get(names[dom]) if args.config == 1 else None,
                         "traffic_note": "DRAM read + write bytes per launch of this kernel on this workload, "
-                                        "one ncu capture (profiles/mx_build_h2o32_pbe.md)",
+                                        "one ncu capture",
                         "note": "useful FP32-equivalent flops (2 npts n_b^2 per block and product) of the "
-                                "dominant kernel over its CUDA-event time; peak = measured cuBLAS bf16 sustained "
-                                "(of measured). The fixed-point operands (three slices a side) issue eight FP16 MMAs "
-                                "per density product and six per adder product, so the useful ceiling is about 1/7 "
-                                "of that peak"}
+                                "dominant kernel over its CUDA-event time; peak = measured cuBLAS bf16 burst "
+                                "(of measured; the kernel is timed in isolation). The fixed-point operands (three "
+                                "slices a side) issue eight FP16 MMAs per density product and six per adder "
+                                "product, so the useful ceiling is about 1/7 of that peak"}
             else:
                 peak = fp64_peak_tflops(torch)
                 roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -473,7 +521,8 @@ def main():
             dt, Vc, excc, nelc = cpu_baseline(w, P, pts, threads=0)
             cpu = {"value": 1.0 / dt, "unit": "builds/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": "one full build of the same workload (grid, P) by the reference-algorithm "
-                             "restatement in oracle/ (FP64, OpenMP over 128-point blocks)"}
+                             "restatement in oracle/ (FP64, OpenMP over 128-point blocks, per-block "
+                             "register-blocked GEMMs)"}
             for name in ["fp64", "mixed"]:
                 if name in res:
                     acc["%s_vs_oracle" % name] = {"dExc": res[name]["exc"] - excc, "dNel": res[name]["nel"] - nelc,
@@ -484,10 +533,9 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if head == "fp64" else "fp32 basis, fp16 fixed-point slices on the tensor cores (f64 functional, sums, Vxc)",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "npoints": n, "nbf": res["nbf"], "nblocks": res["plan"]["nblocks"],
-                       "mean_active": res["plan"]["sum_active"] / res["plan"]["nblocks"], "precision": head,
-                       "parallelism": "replicas" if dist.world > 1 else "single",
-                       "l2": "flushed between steps (512 MB write, outside the timed events)"},
+            "config": bench_config(args.config, n, res["nbf"], res["plan"]["nblocks"],
+                                   res["plan"]["sum_active"] / res["plan"]["nblocks"], dist.world),
+            "precision": head,
             "mpts_per_s": H["mpts_per_s"], "latency_ms": H["latency_ms"], "roofline": H["roofline"],
             "kernel_ms_per_step": H["kernel_ms_per_step"],
             "e2e": {"value": replica_throughput(dist.world, len(res["e2e_ms"]), res["e2e_total_ms"]), "unit": "builds/s",

@@ -227,6 +227,99 @@ void block_on_grid(const Basis& B, const double* xyz, int npts, double thr, int 
   }
 }
 
+// Values (and, deriv = 1, gradients) of the block's non-negligible functions only, with
+// the screening and cut-offs of block_on_grid: act[] receives their global indices in
+// order, val[f * npts + p], grad[(3 f + k) * npts + p].  Monomials by repeated products
+// and no Hessians: the lean form of the reference's per-l unrolled point loop
+// (BasisFunctionOnGridController.cpp:259-1097) that the CPU baseline times.
+int block_active(const Basis& B, const double* xyz, int npts, double thr, int deriv, int* act, double* val,
+                 double* grad) {
+  std::vector<int> negl(B.nbf);
+  double c[3] = {0, 0, 0};
+  for (int p = 0; p < npts; ++p)
+    for (int k = 0; k < 3; ++k) c[k] += xyz[3 * p + k];
+  for (int k = 0; k < 3; ++k) c[k] /= npts;
+  double spread = 0.0;
+  for (int p = 0; p < npts; ++p) {
+    const double dx = xyz[3 * p] - c[0], dy = xyz[3 * p + 1] - c[1], dz = xyz[3 * p + 2] - c[2];
+    spread = std::max(spread, std::sqrt(dx * dx + dy * dy + dz * dz));
+  }
+  const double expthr = -std::log(thr);
+  int nact = 0;
+  double mono[28], dmono[3][28];
+  for (const auto& sh : B.shells) {
+    const double dx = c[0] - sh.O[0], dy = c[1] - sh.O[1], dz = c[2] - sh.O[2];
+    double d = std::sqrt(dx * dx + dy * dy + dz * dz) - spread;
+    if (d >= 1.0) {
+      d = d * d;
+      double radial = 0.0;
+      for (size_t q = 0; q < sh.alpha.size(); ++q) radial += sh.coef[q] * std::exp(-sh.alpha[q] * d);
+      if (std::fabs(radial) < thr) continue;
+    }
+    const int f0 = nact;
+    for (int i = 0; i < sh.nfunc; ++i) act[nact++] = sh.first + i;
+    const int L = sh.l, nc = ncart(L), np = (int)sh.alpha.size();
+    for (int p = 0; p < npts; ++p) {
+      const double x = xyz[3 * p] - sh.O[0], y = xyz[3 * p + 1] - sh.O[1], z = xyz[3 * p + 2] - sh.O[2];
+      const double r2 = x * x + y * y + z * z;
+      double R = 0.0, dR = 0.0;
+      for (int q = 0; q < np; ++q) {
+        const double t = sh.alpha[q] * r2;
+        if (t < expthr) {
+          const double e = sh.coef[q] * std::exp(-t);
+          R += e;
+          dR -= 2.0 * sh.alpha[q] * e;
+        }
+      }
+      if (std::fabs(R) < thr) {
+        for (int f = 0; f < sh.nfunc; ++f) {
+          val[(size_t)(f0 + f) * npts + p] = 0.0;
+          if (deriv >= 1)
+            for (int k = 0; k < 3; ++k) grad[((size_t)3 * (f0 + f) + k) * npts + p] = 0.0;
+        }
+        continue;
+      }
+      double px[8], py[8], pz[8];
+      px[0] = py[0] = pz[0] = 1.0;
+      for (int k = 1; k <= L; ++k) {
+        px[k] = px[k - 1] * x;
+        py[k] = py[k - 1] * y;
+        pz[k] = pz[k - 1] * z;
+      }
+      for (int k = 0; k < nc; ++k) {
+        const int a = sh.ax[k], b = sh.ay[k], cc = sh.az[k];
+        mono[k] = px[a] * py[b] * pz[cc];
+        if (deriv >= 1) {
+          dmono[0][k] = a ? a * px[a - 1] * py[b] * pz[cc] : 0.0;
+          dmono[1][k] = b ? b * px[a] * py[b - 1] * pz[cc] : 0.0;
+          dmono[2][k] = cc ? cc * px[a] * py[b] * pz[cc - 1] : 0.0;
+        }
+      }
+      const double r[3] = {x, y, z};
+      for (int f = 0; f < sh.nfunc; ++f) {
+        double s = 0.0, sd[3] = {0.0, 0.0, 0.0};
+        if (sh.pure) {
+          const double* T = &sh.sph[(size_t)f * nc];
+          for (int k = 0; k < nc; ++k) {
+            if (T[k] == 0.0) continue;
+            s += T[k] * mono[k];
+            if (deriv >= 1)
+              for (int q = 0; q < 3; ++q) sd[q] += T[k] * dmono[q][k];
+          }
+        } else {
+          s = sh.cartnorm[f] * mono[f];
+          if (deriv >= 1)
+            for (int q = 0; q < 3; ++q) sd[q] = sh.cartnorm[f] * dmono[q][f];
+        }
+        val[(size_t)(f0 + f) * npts + p] = s * R;
+        if (deriv >= 1)
+          for (int q = 0; q < 3; ++q) grad[((size_t)3 * (f0 + f) + q) * npts + p] = sd[q] * R + s * dR * r[q];
+      }
+    }
+  }
+  return nact;
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* grids                                                                                      */
 

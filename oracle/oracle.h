@@ -69,6 +69,8 @@ int orc_functional(int func, int nspin, long npts, int max_block, const double* 
                    double* epuv, double* dfdrho, double* dfdgrad);
 /* is the functional a GGA (needs gradients)? */
 int orc_functional_is_gga(int func);
+/* sum over blocks of the non-negligible function count (the screening of the block data) */
+long orc_active_functions(const void* basis, const double* xyz, long npts, int max_block, double thr);
 
 /* F += sum_p w v phi phi (+ GGA term), ScalarOperatorToMatrixAdder.cpp:178-303. */
 int orc_add_scalar(const void* basis, const double* xyz, const double* w, long npts, int max_block,

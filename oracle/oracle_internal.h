@@ -28,6 +28,8 @@ struct Basis {
 int ncart(int l);
 void block_on_grid(const Basis& B, const double* xyz, int npts, double thr, int deriv, double* val, double* grad,
                    double* hess, int* negligible);
+int block_active(const Basis& B, const double* xyz, int npts, double thr, int deriv, int* act, double* val,
+                 double* grad);
 
 /* per-point functional evaluation (GRADIENTS data, order 1).
  * restricted: in = {n, gx, gy, gz}; out = {e, dF/dn, dF/dgx, dF/dgy, dF/dgz}

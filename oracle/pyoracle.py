@@ -43,6 +43,8 @@ def lib():
         L.orc_functional.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, ctypes.c_int, _dp, ctypes.c_void_p,
                                      _dp, _dp, ctypes.c_void_p]
         L.orc_functional_is_gga.argtypes = [ctypes.c_int]
+        L.orc_active_functions.restype = ctypes.c_long
+        L.orc_active_functions.argtypes = [ctypes.c_void_p, _dp, ctypes.c_long, ctypes.c_int, ctypes.c_double]
         L.orc_add_scalar.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_long, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_int, _dp, ctypes.c_void_p, _dp]
         L.orc_vxc.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_long, ctypes.c_int, ctypes.c_double,
@@ -117,6 +119,11 @@ class Basis:
                              nspin, v, _ptr(gg), F)
         F = F.reshape(nspin, self.nbf, self.nbf).transpose(0, 2, 1)
         return F
+
+    def active_functions(self, xyz, max_block=128, thr=1e-9):
+        """Sum over blocks of the non-negligible function count."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        return int(lib().orc_active_functions(self.h, xyz, len(xyz), max_block, thr))
 
     def vxc(self, xyz, w, func, P, max_block=128, thr=1e-9, ave_thr=1e-11, threads=0):
         """Whole build: returns (V [nspin,nbf,nbf], Exc, Nel)."""

@@ -32,30 +32,43 @@ struct ActiveBlock {
   std::vector<double> phi, grad;
 };
 
-static void eval_active(const Basis& B, const double* xyz, int npts, double thr, int deriv, ActiveBlock& out,
-                        std::vector<double>& full_v, std::vector<double>& full_g, std::vector<int>& negl) {
+static void eval_active(const Basis& B, const double* xyz, int npts, double thr, int deriv, ActiveBlock& out) {
   const int nbf = B.nbf;
-  full_v.resize((size_t)npts * nbf);
-  if (deriv >= 1) full_g.resize((size_t)3 * npts * nbf);
-  negl.resize(nbf);
-  block_on_grid(B, xyz, npts, thr, deriv, full_v.data(), deriv >= 1 ? full_g.data() : nullptr, nullptr, negl.data());
+  out.idx.resize(nbf);
+  out.phi.resize((size_t)nbf * npts);
+  if (deriv >= 1) out.grad.resize((size_t)3 * nbf * npts);
   out.npts = npts;
-  out.idx.clear();
-  for (int i = 0; i < nbf; ++i)
-    if (!negl[i]) out.idx.push_back(i);
-  out.nact = (int)out.idx.size();
-  out.phi.resize((size_t)out.nact * npts);
-  if (deriv >= 1) out.grad.resize((size_t)3 * out.nact * npts);
-  for (int f = 0; f < out.nact; ++f) {
-    const int mu = out.idx[f];
-    std::memcpy(&out.phi[(size_t)f * npts], &full_v[(size_t)mu * npts], sizeof(double) * npts);
-    if (deriv >= 1)
-      for (int k = 0; k < 3; ++k)
-        std::memcpy(&out.grad[((size_t)3 * f + k) * npts], &full_g[(size_t)k * npts * nbf + (size_t)mu * npts],
-                    sizeof(double) * npts);
-  }
+  out.nact = block_active(B, xyz, npts, thr, deriv, out.idx.data(), out.phi.data(), deriv >= 1 ? out.grad.data() : nullptr);
+  out.idx.resize(out.nact);
 }
 
+// C (m x n, row stride ldc) = A (m x k, row stride lda) B (k x n, row stride ldb), all
+// row-major, m a multiple of 4 and n of 8 (callers pad with zeros).  Register tiles of
+// 4 x 8 accumulators over the whole k, the 8-wide rows of B contiguous: the per-block
+// GEMMs of the reference's Eigen path (MatrixOperatorToGridTransformer.cpp:131-146,
+// ScalarOperatorToMatrixAdder.cpp:224-303) in portable, auto-vectorised C++.
+static void gemm_nn(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc) {
+  for (int j0 = 0; j0 < n; j0 += 8)
+    for (int i0 = 0; i0 < m; i0 += 4) {
+      double acc[4][8] = {};
+      const double* a0 = A + (size_t)i0 * lda;
+      for (int kk = 0; kk < k; ++kk) {
+        const double* b = B + (size_t)kk * ldb + j0;
+        for (int i = 0; i < 4; ++i) {
+          const double a = a0[(size_t)i * lda + kk];
+          for (int j = 0; j < 8; ++j) acc[i][j] += a * b[j];
+        }
+      }
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 8; ++j) C[(size_t)(i0 + i) * ldc + j0 + j] = acc[i][j];
+    }
+}
+
+static inline int pad4(int x) { return (x + 3) & ~3; }
+static inline int pad8(int x) { return (x + 7) & ~7; }
+
+// X = P_b Phi (P_b the block's active rows and columns of P, symmetric), then
+// rho = rowsum(X o Phi), grad rho = 2 rowsum(X o grad Phi)
 static void density_block(const ActiveBlock& A, int nbf, const double* P, double* rho, double* grad, long gstride) {
   const int n = A.npts, m = A.nact;
   if (m == 0) {
@@ -65,20 +78,17 @@ static void density_block(const ActiveBlock& A, int nbf, const double* P, double
         for (int p = 0; p < n; ++p) grad[k * gstride + p] = 0.0;
     return;
   }
-  // X[nu][p] = sum_mu P[mu,nu] phi[mu][p]
-  std::vector<double> X((size_t)m * n, 0.0);
+  const int mp = pad4(m), np = pad8(n);
+  std::vector<double> Pb((size_t)mp * m, 0.0), Ph((size_t)m * np, 0.0), X((size_t)mp * np);
   for (int nu = 0; nu < m; ++nu) {
-    double* x = &X[(size_t)nu * n];
     const double* Pcol = P + (size_t)A.idx[nu] * nbf;
-    for (int mu = 0; mu < m; ++mu) {
-      const double pm = Pcol[A.idx[mu]];
-      const double* ph = &A.phi[(size_t)mu * n];
-      for (int p = 0; p < n; ++p) x[p] += pm * ph[p];
-    }
+    for (int mu = 0; mu < m; ++mu) Pb[(size_t)nu * m + mu] = Pcol[A.idx[mu]];
+    std::memcpy(&Ph[(size_t)nu * np], &A.phi[(size_t)nu * n], sizeof(double) * n);
   }
+  gemm_nn(mp, np, m, Pb.data(), m, Ph.data(), np, X.data(), np);
   for (int p = 0; p < n; ++p) rho[p] = 0.0;
   for (int nu = 0; nu < m; ++nu) {
-    const double* x = &X[(size_t)nu * n];
+    const double* x = &X[(size_t)nu * np];
     const double* ph = &A.phi[(size_t)nu * n];
     for (int p = 0; p < n; ++p) rho[p] += x[p] * ph[p];
   }
@@ -87,7 +97,7 @@ static void density_block(const ActiveBlock& A, int nbf, const double* P, double
       double* g = grad + k * gstride;
       for (int p = 0; p < n; ++p) g[p] = 0.0;
       for (int nu = 0; nu < m; ++nu) {
-        const double* x = &X[(size_t)nu * n];
+        const double* x = &X[(size_t)nu * np];
         const double* gp = &A.grad[((size_t)3 * nu + k) * n];
         for (int p = 0; p < n; ++p) g[p] += x[p] * gp[p];
       }
@@ -96,39 +106,39 @@ static void density_block(const ActiveBlock& A, int nbf, const double* P, double
   }
 }
 
-// adds the block's contribution of one spin into F (nbf x nbf, column-major)
+// adds the block's contribution of one spin into F (nbf x nbf, column-major):
+// tmp = Phi^T G by one GEMM over the block's points, F_b = tmp (LDA, G = w v Phi) or
+// tmp + tmp^T (GGA, G = w (v/2 Phi + g . grad Phi))
 static void adder_block(const ActiveBlock& A, int nbf, const double* wv, const double* wg /*3*npts or null*/,
                         double* F) {
   const int n = A.npts, m = A.nact;
   if (m == 0) return;
-  std::vector<double> G((size_t)m * n);
+  const int mp4 = pad4(m), mp8 = pad8(m);
+  std::vector<double> Ph((size_t)mp4 * n, 0.0), GT((size_t)n * mp8, 0.0), T((size_t)mp4 * mp8);
   for (int f = 0; f < m; ++f) {
     const double* ph = &A.phi[(size_t)f * n];
-    double* g = &G[(size_t)f * n];
+    std::memcpy(&Ph[(size_t)f * n], ph, sizeof(double) * n);
     if (wg) {
       const double* gx = &A.grad[((size_t)3 * f + 0) * n];
       const double* gy = &A.grad[((size_t)3 * f + 1) * n];
       const double* gz = &A.grad[((size_t)3 * f + 2) * n];
       for (int p = 0; p < n; ++p)
-        g[p] = wg[p] * gx[p] + wg[n + p] * gy[p] + wg[2 * n + p] * gz[p] + 0.5 * wv[p] * ph[p];
+        GT[(size_t)p * mp8 + f] = wg[p] * gx[p] + wg[n + p] * gy[p] + wg[2 * n + p] * gz[p] + 0.5 * wv[p] * ph[p];
     } else {
-      for (int p = 0; p < n; ++p) g[p] = wv[p] * ph[p];
+      for (int p = 0; p < n; ++p) GT[(size_t)p * mp8 + f] = wv[p] * ph[p];
     }
   }
+  gemm_nn(mp4, mp8, n, Ph.data(), n, GT.data(), mp8, T.data(), mp8);
   for (int a = 0; a < m; ++a) {
-    const double* pa = &A.phi[(size_t)a * n];
     double* Fcol = F + (size_t)A.idx[a] * nbf;
-    for (int b = 0; b < m; ++b) {
-      const double* gb = &G[(size_t)b * n];
-      double s = 0.0;
-      for (int p = 0; p < n; ++p) s += pa[p] * gb[p];
-      if (wg) {
-        // F_b = tmp + tmp^T with tmp = phi^T G
-        Fcol[A.idx[b]] += s;
-        F[(size_t)A.idx[b] * nbf + A.idx[a]] += s;
-      } else {
-        Fcol[A.idx[b]] += s;
+    const double* t = &T[(size_t)a * mp8];
+    if (wg) {
+      for (int b = 0; b < m; ++b) {
+        Fcol[A.idx[b]] += t[b];
+        F[(size_t)A.idx[b] * nbf + A.idx[a]] += t[b];
       }
+    } else {
+      for (int b = 0; b < m; ++b) Fcol[A.idx[b]] += t[b];
     }
   }
 }
@@ -150,14 +160,13 @@ static void add_scalar(const Basis& B, const double* xyz, const double* w, long 
 #pragma omp parallel
   {
     ActiveBlock A;
-    std::vector<double> fv, fg, wv, wg;
-    std::vector<int> negl;
+    std::vector<double> wv, wg;
     double* myF = Ft[omp_get_thread_num()].data();
 #pragma omp for schedule(dynamic)
     for (long b = 0; b < nblocks; ++b) {
       const long first = b * maxb;
       const int n = block_size(b, nblocks, npts, maxb);
-      eval_active(B, xyz + 3 * first, n, thr, g ? 1 : 0, A, fv, fg, negl);
+      eval_active(B, xyz + 3 * first, n, thr, g ? 1 : 0, A);
       for (int s = 0; s < nspin; ++s) {
         wv.resize(n);
         double ave = 0.0;
@@ -189,13 +198,11 @@ static void density(const Basis& B, const double* xyz, long npts, int maxb, doub
 #pragma omp parallel
   {
     ActiveBlock A;
-    std::vector<double> fv, fg;
-    std::vector<int> negl;
 #pragma omp for schedule(dynamic)
     for (long b = 0; b < nblocks; ++b) {
       const long first = b * maxb;
       const int n = block_size(b, nblocks, npts, maxb);
-      eval_active(B, xyz + 3 * first, n, thr, 1, A, fv, fg, negl);
+      eval_active(B, xyz + 3 * first, n, thr, 1, A);
       for (int s = 0; s < nspin; ++s)
         density_block(A, nbf, P + (size_t)s * nbf * nbf, rho + s * npts + first,
                       grad ? grad + (size_t)s * 3 * npts + first : nullptr, npts);
@@ -346,6 +353,25 @@ int orc_functional(int func, int nspin, long npts, int max_block, const double* 
 }
 
 int orc_functional_is_gga(int func) { return orc::functional_is_gga(func) ? 1 : 0; }
+
+long orc_active_functions(const void* basis, const double* xyz, long npts, int max_block, double thr) {
+  const orc::Basis& B = *static_cast<const orc::Basis*>(basis);
+  const long nblocks = (npts + max_block - 1) / max_block;
+  long total = 0;
+#pragma omp parallel reduction(+ : total)
+  {
+    std::vector<int> act(B.nbf);
+    std::vector<double> val;
+#pragma omp for schedule(dynamic)
+    for (long b = 0; b < nblocks; ++b) {
+      const long first = b * max_block;
+      const int n = (int)std::min((long)max_block, npts - first);
+      val.resize((size_t)B.nbf * n);
+      total += orc::block_active(B, xyz + 3 * first, n, thr, 0, act.data(), val.data(), nullptr);
+    }
+  }
+  return total;
+}
 
 int orc_add_scalar(const void* basis, const double* xyz, const double* w, long npts, int max_block, double thr,
                    double ave_thr, int nspin, const double* v, const double* g, double* F) {
