@@ -8,6 +8,12 @@ heavy stage (``xcgpu_vxc_batch``).  Batches alternate between compute streams so
 next batch's kernels start on SMs the previous batch's tail leaves idle, and the
 setup of new geometries (grid, screening) runs on its own stream while batches
 compute.  Latency is measured from a request's arrival to the completion of its batch.
+
+Under load two bounds keep latency from growing with the queue: a batch takes waiting
+requests only up to a cap on its estimated work (the plans' contraction flops), so a
+large build does not hold many small ones until it ends; and with a latency budget a
+request whose predicted completion (the work queued ahead of it at the measured service
+rate) lies beyond the budget is rejected on arrival instead of joining the queue.
 """
 import collections
 import math
@@ -23,7 +29,7 @@ class Request:
     """One Vxc request.  Its density matrix is the request payload: it is formed on the
     GPU when the request arrives (seeded), so that only requests in the system hold one."""
     __slots__ = ("rid", "arrival", "key", "workload", "P_dev", "V_dev", "en_dev", "func", "done", "latency",
-                 "nbytes", "plan_slot", "exc", "nel", "seed", "ready")
+                 "nbytes", "plan_slot", "exc", "nel", "seed", "ready", "flops", "rejected")
 
     def __init__(self, rid, arrival, key, workload, func, seed):
         self.rid, self.arrival, self.key, self.workload = rid, arrival, key, workload
@@ -32,6 +38,8 @@ class Request:
         self.done = None
         self.latency = None
         self.exc = self.nel = None
+        self.flops = 0.0
+        self.rejected = False
 
     def fresh(self):
         """The same request, not yet served."""
@@ -54,7 +62,6 @@ class Resident:
         self.plans = [xcgpu.Plan(ctx, self.grid, self.basis, 128, 1e-9)]
         self.busy = 0  # requests admitted and not yet retired
         self.ctx = ctx
-        self.S = None
 
     def plan(self):
         self.busy += 1
@@ -65,7 +72,8 @@ class Resident:
 
 
 class Server:
-    def __init__(self, ctx, hbm_budget, precision=xcgpu.PREC_MIXED, max_batch=64, nstreams=2):
+    def __init__(self, ctx, hbm_budget, precision=xcgpu.PREC_MIXED, max_batch=64, nstreams=2, max_batch_flops=None,
+                 latency_budget_s=None):
         import torch
         self.torch = torch
         self.ctx = ctx
@@ -79,6 +87,14 @@ class Server:
         self.inflight = []
         self.reserved = 0
         self.residents_built = 0
+        # overlap matrices (the request generator's metric) by geometry key: kept apart from
+        # the evictable cache, so a request that arrives after its geometry was evicted still
+        # finds it
+        self.overlaps = {}
+        self.max_batch_flops = max_batch_flops
+        self.latency_budget_s = latency_budget_s
+        self.queued_flops = 0.0  # estimated work admitted and not yet retired
+        self.rate_flops = None  # measured service rate (flops/s), a running average
 
     # -- resident data --------------------------------------------------------------------
     def resident(self, key, w):
@@ -94,6 +110,14 @@ class Server:
         self.cache.move_to_end(key)
         return r
 
+    def overlap(self, key, w):
+        """The geometry's overlap matrix on the GPU, from its resident plan on first use."""
+        S = self.overlaps.get(key)
+        if S is None:
+            S = overlap_on_gpu(self.ctx, self.resident(key, w))
+            self.overlaps[key] = S
+        return S
+
     def _evict(self):
         while self.ctx.bytes_in_use + self.reserved > self.budget and self.cache:
             key, r = next(iter(self.cache.items()))
@@ -106,13 +130,23 @@ class Server:
 
     # -- batches --------------------------------------------------------------------------
     def _arrive(self, rq):
-        """Form the request's density matrix on the setup stream (no host synchronisation)."""
+        """Admit the request (or reject it if its predicted completion exceeds the latency
+        budget) and form its density matrix on the setup stream (no host synchronisation).
+        Returns False for a rejected request."""
         torch = self.torch
         r = self.resident(rq.key, rq.workload)
+        rq.flops = _plan_flops(r.plans[0], rq.workload.nspin)
+        if self.latency_budget_s is not None and self.rate_flops:
+            if (self.queued_flops + rq.flops) / self.rate_flops > self.latency_budget_s:
+                rq.rejected = True
+                return False
+        self.queued_flops += rq.flops
+        S = self.overlap(rq.key, rq.workload)
         with torch.cuda.stream(self.setup_stream):
-            rq.P_dev = density_on_gpu(r.S, rq.workload.nocc, rq.seed)
+            rq.P_dev = density_on_gpu(S, rq.workload.nocc, rq.seed)
             rq.ready = torch.cuda.Event()
             rq.ready.record(self.setup_stream)
+        return True
 
     def _launch(self, batch, stream):
         torch = self.torch
@@ -128,15 +162,21 @@ class Server:
         self.ctx.vxc_batch(items, self.precision)
         ev = torch.cuda.Event()
         ev.record(stream)
-        self.inflight.append((batch, ev, stream))
+        self.inflight.append((batch, ev, stream, time.perf_counter()))
 
     def _retire(self, now_fn, keep_results):
         keep = []
-        for batch, ev, stream in self.inflight:
+        for batch, ev, stream, t_launch in self.inflight:
             if ev.query():
                 self.ctx.set_stream(stream.cuda_stream)
                 self.ctx.check_async()
                 t = now_fn()
+                work = sum(rq.flops for rq in batch)
+                self.queued_flops -= work
+                dt = time.perf_counter() - t_launch
+                if dt > 0 and work > 0:  # service rate, averaged over recent batches
+                    r_ = work / dt
+                    self.rate_flops = r_ if self.rate_flops is None else 0.8 * self.rate_flops + 0.2 * r_
                 for rq in batch:
                     rq.done = t
                     rq.latency = t - rq.arrival
@@ -148,7 +188,7 @@ class Server:
                         rq.P_dev = rq.V_dev = None
                 yield batch
             else:
-                keep.append((batch, ev, stream))
+                keep.append((batch, ev, stream, t_launch))
         self.inflight = keep
 
     def run(self, requests, on_complete=None, keep_results=True):
@@ -162,20 +202,26 @@ class Server:
         built0 = self.residents_built
         sidx = 0
         completed = 0
+        rejected = []
         while todo or pending or self.inflight:
             t = now()
             while todo and todo[0].arrival <= t:
                 rq = todo.popleft()
-                self._arrive(rq)
-                pending.append(rq)
+                if self._arrive(rq):
+                    pending.append(rq)
+                else:
+                    rejected.append(rq)
             for batch in self._retire(now, keep_results):
                 completed += len(batch)
                 if on_complete:
                     on_complete(batch)
             if pending and len(self.inflight) < len(self.streams):
                 batch = []
+                bflops = 0.0
                 while pending and len(batch) < self.max_batch:
                     rq = pending[0]
+                    if batch and self.max_batch_flops is not None and bflops + rq.flops > self.max_batch_flops:
+                        break
                     w = rq.workload
                     r = self.resident(rq.key, w)
                     slot = r.plan()
@@ -187,6 +233,7 @@ class Server:
                         break
                     rq.plan_slot = slot
                     self.reserved += rq.nbytes
+                    bflops += rq.flops
                     batch.append(pending.popleft())
                 if batch:
                     self._launch(batch, self.streams[sidx % len(self.streams)])
@@ -197,8 +244,10 @@ class Server:
             else:
                 time.sleep(0.0002)
         total = now()
-        lat = np.array([r.latency for r in requests])
-        return {"requests": len(requests), "wall_s": total, "throughput_req_s": len(requests) / total,
+        served = [r for r in requests if r.latency is not None]
+        lat = np.array([r.latency for r in served]) if served else np.zeros(1)
+        return {"requests": len(requests), "served": len(served), "rejected": len(rejected), "wall_s": total,
+                "throughput_req_s": len(served) / total,
                 "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
                 "mean_ms": float(lat.mean() * 1e3), "batches": sidx, "resident_geometries": len(self.cache),
                 "residents_built_while_serving": self.residents_built - built0}
@@ -222,13 +271,17 @@ def density_on_gpu(S_dev, nocc, seed):
     return P.contiguous().reshape(1, n, n)
 
 
-def overlap_on_gpu(ctx, resident, n):
+def overlap_on_gpu(ctx, resident):
     """Overlap matrix of a resident geometry by grid integration (adder with v = 1)."""
     import torch
-    if resident.S is None:
-        S = resident.plans[0].add_scalar(np.ones(resident.grid.n), block_ave_threshold=0.0, precision=xcgpu.PREC_MIXED)[0]
-        resident.S = torch.from_numpy(np.ascontiguousarray(S)).cuda()
-    return resident.S
+    S = resident.plans[0].add_scalar(np.ones(resident.grid.n), block_ave_threshold=0.0, precision=xcgpu.PREC_MIXED)[0]
+    return torch.from_numpy(np.ascontiguousarray(S)).cuda()
+
+
+def _plan_flops(plan, nspin):
+    """Estimated work of a build on this plan: the contractions' flops (4 npts n_b^2 per
+    block and spin)."""
+    return float(plan.stats().get("flops_per_spin", 0.0)) * nspin
 
 
 def make_requests(server, n=2000, rate=200.0, seed=0, max_waters=128, n_rad=50, n_ang=110, geometries=32):
@@ -251,8 +304,7 @@ def make_requests(server, n=2000, rate=200.0, seed=0, max_waters=128, n_rad=50, 
         key = (m, basis)
         sym, xyz = wl.water_cluster(m, seed=1000 + m, jitter=0.2)
         w = wl.Workload(sym, xyz, basis, func, 5 * m, n_rad, n_ang, seed)
-        r = server.resident(key, w)
-        overlap_on_gpu(server.ctx, r, w.nbf)
+        server.overlap(key, w)
         reqs.append(Request(i, t, key, w, func, seed * 100000 + i))
     server.ctx.set_stream(server.streams[0].cuda_stream)
     return reqs, time.perf_counter() - t0

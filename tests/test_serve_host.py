@@ -1,7 +1,8 @@
 """Host logic of the serving loop (serenity_gb300/serve.py) on the CPU: admission of waiting
-requests into batches under the HBM budget and the batch cap, continuous batching over two
-streams, LRU eviction that never drops a geometry with requests in flight, and the
-bookkeeping of reserved bytes and latencies.  The GPU pieces (streams, events, the library's
+requests into batches under the HBM budget, the batch cap and the work cap, continuous
+batching over two streams, LRU eviction that never drops a geometry with requests in
+flight (and whose evicted geometries still serve later requests), rejection beyond a
+latency budget, and the bookkeeping of reserved bytes and latencies.  The GPU pieces (streams, events, the library's
 batched build, the request's density matrix) are replaced by fakes that record what the loop
 asks of them; the builds themselves are covered by tests/test_gpu_batch.py."""
 import sys
@@ -53,7 +54,7 @@ def fake_torch(polls):
 
 class FakePlan:
     def __init__(self, npoints, nblocks):
-        self.st = {"npoints": npoints, "nblocks": nblocks}
+        self.st = {"npoints": npoints, "nblocks": nblocks, "flops_per_spin": 1000.0}
 
     def stats(self):
         return dict(self.st)
@@ -99,12 +100,16 @@ def workload(nbf=24):
 
 @pytest.fixture
 def make_server(monkeypatch):
-    def make(budget, max_batch=64, polls=1, npoints=1000, nblocks=8):
+    def make(budget, max_batch=64, polls=1, npoints=1000, nblocks=8, **kw):
         monkeypatch.setitem(sys.modules, "torch", fake_torch(polls))
         monkeypatch.setattr(serve, "xcgpu", fake_xcgpu(npoints, nblocks))
-        monkeypatch.setattr(serve, "density_on_gpu", lambda S, nocc, seed: object())
+        def density(S, nocc, seed):
+            assert S is not None  # every arriving request finds its geometry's overlap
+            return object()
+        monkeypatch.setattr(serve, "density_on_gpu", density)
+        monkeypatch.setattr(serve, "overlap_on_gpu", lambda ctx, r: ("S", id(r)))
         ctx = FakeCtx()
-        return serve.Server(ctx, budget, precision=1, max_batch=max_batch, nstreams=2), ctx
+        return serve.Server(ctx, budget, precision=1, max_batch=max_batch, nstreams=2, **kw), ctx
     return make
 
 
@@ -175,3 +180,33 @@ def test_work_bytes_grow_with_points_functions_and_spins():
     assert serve._work_bytes(1000, 48, 1, True, 8) > base
     assert serve._work_bytes(1000, 24, 2, True, 8) > base
     assert serve._work_bytes(1000, 24, 1, False, 8) < base
+
+
+def test_evicted_geometry_serves_later_requests(make_server):
+    srv, ctx = make_server(budget=10 ** 9)
+    srv.run(_requests(2, 1))
+    srv.budget = 0
+    srv._evict()  # the geometry's resident data goes, its overlap stays
+    assert not srv.cache and (0, "SVP") in srv.overlaps
+    srv.budget = 10 ** 9
+    later = [serve.Request(5, 0.0, (0, "SVP"), workload(), "PBE", 5)]
+    stats = srv.run(later)
+    assert stats["served"] == 1 and later[0].latency is not None
+
+
+def test_work_cap_splits_batches(make_server):
+    srv, ctx = make_server(budget=10 ** 9, max_batch_flops=2500.0)  # each request: 1000 flops
+    srv.run(_requests(7, 2))
+    sizes = [len(p) for _, p in ctx.batches]
+    assert sum(sizes) == 7 and max(sizes) <= 2
+
+
+def test_latency_budget_rejects_beyond_the_predicted_wait(make_server):
+    srv, ctx = make_server(budget=10 ** 9, latency_budget_s=2.5e-3)
+    srv.rate_flops = 1e6  # measured service rate: each request (1000 flops) takes 1 ms
+    reqs = _requests(6, 2)
+    stats = srv.run(reqs)
+    # arriving together, the first two fit the 2.5 ms budget and the rest would wait longer
+    assert stats["served"] == 2 and stats["rejected"] == 4
+    assert all((r.latency is None) == r.rejected for r in reqs)
+    assert srv.queued_flops == 0 and srv.reserved == 0
