@@ -10,7 +10,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 #include <string>
 
 #include "internal.h"
@@ -25,22 +24,15 @@ constexpr long kNoAllocDoubles = (long)(kNoAllocScratchBytes / sizeof(double));
 constexpr long kNoAllocMaxBlocks = 4096;  // slab offsets kept at the front of the array
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 
-constexpr int kMaxDevices = 64;
-static void* g_scratch_addr[kMaxDevices] = {nullptr};
-static std::mutex g_scratch_mutex;
-
-// Device address of the static scratch on the current device (set up once per
-// device; the host-side name of the array is only a stand-in, not a device address).
+// Device address of the static scratch in the current context.  The host-side name of
+// the array is only a stand-in, not a device address, and the array's address belongs
+// to the context that loaded the module, so it is looked up on every call (which
+// allocates nothing) rather than remembered per device ordinal.
 static xcgpu_status scratch_address(Ctx* c, double** out) {
-  if (c->device < 0 || c->device >= kMaxDevices) return c->fail(XCGPU_ERR_INVALID, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_addr[c->device]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return c->cuda(e, "cudaGetSymbolAddress(no-allocation scratch)");
-    g_scratch_addr[c->device] = p;
-  }
-  *out = static_cast<double*>(g_scratch_addr[c->device]);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return c->cuda(e, "cudaGetSymbolAddress(no-allocation scratch)");
+  *out = static_cast<double*>(p);
   return XCGPU_OK;
 }
 
