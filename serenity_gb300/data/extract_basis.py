@@ -49,5 +49,6 @@ def extract(ref_root, out_dir):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    extract(ref, os.path.join(os.path.dirname(os.path.abspath(__file__)), "basis"))
+    if len(sys.argv) < 2:
+        sys.exit("usage: python serenity_gb300/data/extract_basis.py <path of the reference source tree>")
+    extract(sys.argv[1], os.path.join(os.path.dirname(os.path.abspath(__file__)), "basis"))

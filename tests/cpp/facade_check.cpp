@@ -1,7 +1,7 @@
 // Drives the C++ facade (include/serenity_xc.hpp) the way Serenity's own tests drive
 // its classes: SMALL_MIXED basis on the TINY / VERY_SMALL grids
 // (testsupply/BasisController__TEST_SUPPLY.cpp:59-84, GridController__TEST_SUPPLY.cpp:31-46).
-// Prints the results as JSON; tests/test_gpu_facade.py compares them with the golden
+// Prints the results as JSON; tests/test_facade.py compares them with the golden
 // vectors of the reference tests.
 #include <cstdio>
 #include <memory>

@@ -5,10 +5,11 @@ products), what the mixed build kernel computes for rho and grad rho, so that it
 against FP64 can be attributed stage by stage without a GPU:
 
   * basis values (serenity_gb300/csrc/xc_mixed.cu: shell_rec_at; basis_eval.cuh:
-    shell_functions_cx): point and centre as FP32 high + remainder, r^2 and alpha r^2 as
-    FP32 pairs, the radial sum as a pair (the exponential taken exact: the kernel's pair
-    exponential is accurate to 2e-11), solid harmonics in FP32 with the coefficients' low
-    parts, the value's low part fma(v, R_lo / R, v_low);
+    shell_functions_px): point and centre as FP32 high + remainder, the point-centre
+    offset as an FP32 pair (two-sum), r^2 and alpha r^2 as FP32 pairs, the radial sum as
+    a pair (the exponential taken exact: the kernel's pair exponential is accurate to
+    2e-11), the monomials, the coefficients and the solid-harmonic sums as FP32 pairs,
+    the value's low part fma(v, R_lo / R, v_low), the gradients in FP32;
   * the plan's screening (xc_fp64.cu: screen_kernel) and 128-point blocks;
   * the fixed-point slices of A (density_slices: row scale from the point's largest |phi|,
     dithered last digit, point_dither / function_dither) and of P (split_p_kernel);
@@ -16,13 +17,11 @@ against FP64 can be attributed stage by stage without a GPU:
     s0t1 + s1t0, s1t1, s0t2 + s2t0 + s1t2 + s2t1), their FP32 combination, and the
     epilogue's per-quarter FP32 sums over 8 columns with the low parts summed apart.
 
-On (H2O)32 def2-SVP PBE it reproduces the GPU's N_el error to four digits. The oracle
-(oracle/pyoracle.py) supplies the exact basis values check and the functional derivatives
-for the first-order E_xc error.  Run as a script for the full-size attribution:
-
-    python tests/mixed_emulation.py --config 1 --basis kernel     # about 15 min on 8 cores
+On (H2O)32 def2-SVP PBE its former FP32 form ("fp32", the angular part and the offset
+rounded once per operation) reproduced the GPU's N_el error to four digits and named
+the pair arithmetic the kernel now uses.  The oracle (oracle/pyoracle.py) supplies the
+exact basis values check and the functional derivatives for the first-order E_xc error.
 """
-import argparse
 import math
 import os
 import sys
@@ -87,12 +86,11 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
     """Pure shell l at points xyz [n, 3]: (exact values [n, 2l+1], exact gradients [3, n, 2l+1],
     FP32 values, their FP32 low parts, FP32 gradients [3, n, 2l+1]).
 
-    mode "kernel": the kernel's arithmetic; "offset_pair_p": the point-centre offset as an
-    FP32 pair entering r^2, and p functions compensated (value = x R to second order);
-    "pairs": the offset pair, and the whole angular part (powers, monomials, x R, the
-    solid-harmonic sums) carried as FP32 pairs (error-free products by FMA, two-sum);
-    "pairs_sterbenz": as "pairs" with the high parts' difference taken as exact;
-    "exact": the exact value split into FP32 high and low parts (gradients as in "kernel")."""
+    mode "kernel": the kernel's arithmetic, the offset and the whole angular part
+    (powers, monomials, the solid-harmonic sums) carried as FP32 pairs (error-free
+    products by FMA, two-sum); "fp32": the kernel's former arithmetic, offset and angular
+    part rounded to FP32 at every operation; "exact": the exact value split into FP32
+    high and low parts (gradients as in "kernel")."""
     ethr = -math.log(thr)
     d = xyz - A[None, :]
     r2e = (d * d).sum(1)
@@ -124,12 +122,10 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
     al = fl(A - ah.astype(f64))
     X = [(qh[:, i] - ah[i]) + (ql[:, i] - al[i]) for i in range(3)]
     XL = None
-    if mode in ("offset_pair_p", "pairs", "pairs_sterbenz"):
+    if mode == "kernel":
         XL = []
         for i in range(3):
             s, e = two_sum(qh[:, i], -np.full_like(qh[:, i], ah[i]))
-            if mode == "pairs_sterbenz":  # qh - ah taken as exact (it is when qh / ah is in [1/2, 2])
-                e = np.zeros_like(e)
             dl = (ql[:, i] - al[i]) + e
             X[i] = s + dl
             XL.append(dl - (X[i] - s))
@@ -197,7 +193,7 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
                 svl[m] = fma(tl * np.ones_like(v), v, svl[m])
             for ax in range(3):
                 sg[ax][m] = fma(t * np.ones_like(v), g[ax], sg[ax][m])
-    if mode in ("pairs", "pairs_sterbenz"):
+    if mode == "kernel":
         def pmul(ah_, al_, bh_, bl_):
             h = ah_ * bh_
             return h, fma(ah_, bh_, -h) + fma(ah_, bl_, al_ * bh_)
@@ -223,10 +219,6 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
                 sh_[m], e = two_sum(sh_[m], ph)
                 sl_[m] = sl_[m] + (e + pl)
         sv, svl = sh_, sl_
-    if XL is not None and l == 1 and mode == "offset_pair_p":
-        for m in range(NS):
-            ax = [i for i in range(3) if ks[int(np.nonzero(TS[1][m])[0][0])][i] == 1][0]
-            svl[m] = fma(XL[ax], Rv, fma(X[ax], Rv, -sv[m]))
     V = np.zeros((len(xyz), NS), f32)
     VL = np.zeros_like(V)
     G32 = np.zeros((3, len(xyz), NS), f32)
@@ -409,26 +401,3 @@ def density_errors(sh, pts, wts, P, func="PBE", basis_mode="kernel", chunk=8192,
         if blocks is not None and nblk >= blocks:
             break
     return dN, dE, N
-
-
-def main():
-    from oracle import pyoracle as po
-    from serenity_gb300 import workload as wl
-    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--basis", default="kernel", choices=["kernel", "offset_pair_p", "pairs", "pairs_sterbenz", "exact"])
-    ap.add_argument("--chunk-stride", type=int, default=1, help="emulate every k-th chunk of 8192 points (sampled)")
-    ap.add_argument("--p-exact", action="store_true", help="P unsliced (bounds the cost of its 27-bit slices)")
-    args = ap.parse_args()
-    w = wl.config(args.config)
-    pts, wts = po.becke_grid(w.Z, w.coords, n_rad=w.n_rad, n_ang=w.n_ang)
-    P = np.asarray(w.density()).reshape(w.nspin, w.nbf, w.nbf)
-    dN, dE, N = density_errors(w.shells, pts, wts, P, w.func, args.basis, log=lambda m: print(m, flush=True),
-                               chunk_stride=args.chunk_stride, p_exact=args.p_exact)
-    print("basis %s%s%s: N_el %.10f  dN_el %+.4e  dE_xc (first order) %+.4e" % (
-        args.basis, ", P exact" if args.p_exact else "",
-        " (every %d-th chunk, scaled)" % args.chunk_stride if args.chunk_stride > 1 else "", N, dN, dE))
-
-
-if __name__ == "__main__":
-    main()

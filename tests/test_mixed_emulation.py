@@ -1,7 +1,9 @@
 """The CPU emulation of the mixed density arithmetic (tests/mixed_emulation.py): its exact
-part equals the oracle's basis values and gradients, its FP32 basis values carry the
-errors the kernel's arithmetic has (and none in the exact mode), and on one water the
-emulated mixed density integrates to the FP64 electron count within the slices' noise."""
+part equals the oracle's basis values and gradients; the kernel's pair arithmetic carries
+the basis values (high + low part) to about 2^-44 of the shell's largest value, the
+former per-operation FP32 form to 1e-10..1e-6 (the error the pairs remove), the exact
+mode to FP64; and on one water the emulated mixed density integrates to the FP64
+electron count within the slices' noise."""
 import numpy as np
 import pytest
 
@@ -42,11 +44,11 @@ def test_exact_part_matches_oracle(water):
         j += n
 
 
-def test_fp32_values_carry_kernel_errors_and_exact_mode_none(water):
+def test_basis_value_errors_by_mode(water):
     w, pts, _ = water
     sh, b, off, cen = _shells(w)
     xyz = pts[::3]
-    worst = {"kernel": 0.0, "exact": 0.0}
+    worst = {"kernel": 0.0, "fp32": 0.0, "exact": 0.0}
     for s in range(sh.nshell):
         for mode in worst:
             phi, _, V, VL, _ = me.shell_values(xyz, cen[s], int(sh.l[s]), sh.alpha[off[s]:off[s + 1]], b.shell_coefs(s),
@@ -54,7 +56,8 @@ def test_fp32_values_carry_kernel_errors_and_exact_mode_none(water):
             scale = max(np.abs(phi).max(), 1e-300)
             worst[mode] = max(worst[mode], np.abs(V.astype(np.float64) + VL - phi).max() / scale)
     assert worst["exact"] < 1e-14
-    assert 1e-10 < worst["kernel"] < 1e-6  # FP32 rounding of the offsets and angular parts
+    assert worst["kernel"] < 1e-12  # the radial factor's pair and the pair angular part
+    assert 1e-10 < worst["fp32"] < 1e-6  # FP32 rounding of the offsets and angular parts
 
 
 def test_emulated_mixed_density_of_one_water(water):
