@@ -4,6 +4,11 @@
  *
  *   BasisFunctionOnGridController     src/data/grid/BasisFunctionOnGridController.h:44-308
  *   DensityOnGridCalculator<M>        src/data/grid/DensityOnGridCalculator.h:45-135
+ *   DensityMatrixController<M>        src/data/matrices/DensityMatrixController.h (the density
+ *                                     matrix and its notification of dependent objects)
+ *   DensityOnGridController<M>        src/data/grid/DensityOnGridController.h:40-140
+ *   DensityMatrixDensityOnGridController<M>  src/data/grid/DensityMatrixDensityOnGridController.h:37-136
+ *   Functional, CompositeFunctionals  src/dft/Functional.h, src/dft/functionals/CompositeFunctionals.h
  *   FunctionalLibrary<M>              src/dft/functionals/FunctionalLibrary.h:51-64
  *   ScalarOperatorToMatrixAdder<M>    src/data/grid/ScalarOperatorToMatrixAdder.h:56-93
  *   FuncPotential<M> (getMatrix, getEnergy)  src/potentials/FuncPotential.h
@@ -19,6 +24,7 @@
 #ifndef SERENITY_XC_HPP
 #define SERENITY_XC_HPP
 
+#include <cstdio>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -36,6 +42,61 @@ class SerenityError : public std::runtime_error {
 namespace Options {
 enum class SCF_MODES { RESTRICTED, UNRESTRICTED };
 }
+
+/* The reference's IO switches that this path reads (src/settings/IOOptions.h):
+ * gridAccuracyCheck prints the electron count integrated over the grid whenever a
+ * DensityMatrixDensityOnGridController forms a density. */
+struct IOOptions {
+  bool gridAccuracyCheck = false;
+};
+inline IOOptions iOOptions;
+
+/* Notification (src/notification/ObjectSensitiveClass.h, NotifyingClass.h): an object
+ * whose data depends on another registers with it and is told when that data changes.
+ * _self is a non-owning handle to the object itself, expiring with it. */
+class ObjectSensitiveClass {
+ public:
+  ObjectSensitiveClass() : _self(this, [](ObjectSensitiveClass*) {}) {}
+  virtual ~ObjectSensitiveClass() = default;
+  virtual void notify() = 0;
+
+ protected:
+  std::shared_ptr<ObjectSensitiveClass> _self;
+};
+class NotifyingClass {
+ public:
+  virtual ~NotifyingClass() = default;
+  void addSensitiveObject(std::weak_ptr<ObjectSensitiveClass> object) { sensitive_.push_back(std::move(object)); }
+
+ protected:
+  void notifyObjects() {
+    for (size_t i = 0; i < sensitive_.size();) {
+      if (auto o = sensitive_[i].lock()) {
+        o->notify();
+        ++i;
+      } else {
+        sensitive_.erase(sensitive_.begin() + (long)i);
+      }
+    }
+  }
+
+ private:
+  std::vector<std::weak_ptr<ObjectSensitiveClass>> sensitive_;
+};
+
+/* Eigen::SparseVector<int> as returned by getNonNegligibleBlocks: rows() entries, the
+ * non-zero ones listed in increasing index order */
+struct SparseVectorInt {
+  long size = 0;
+  std::vector<int> indices, values;
+  long rows() const { return size; }
+  long nonZeros() const { return (long)indices.size(); }
+  int coeff(long i) const {
+    for (size_t k = 0; k < indices.size(); ++k)
+      if (indices[k] == i) return values[k];
+    return 0;
+  }
+};
 constexpr Options::SCF_MODES RESTRICTED = Options::SCF_MODES::RESTRICTED;
 constexpr Options::SCF_MODES UNRESTRICTED = Options::SCF_MODES::UNRESTRICTED;
 
@@ -276,6 +337,8 @@ class DensityOnGridCalculator {
   DensityOnGridCalculator(std::shared_ptr<BasisFunctionOnGridController> bfog, double blockAverageThreshold,
                           int precision = XCGPU_PREC_FP64)
       : bfog_(bfog), thr_(blockAverageThreshold), precision_(precision) {}
+  /* calcDensityOnGrid(P, densityOnGrid) (DensityOnGridCalculator.cpp:38-44) */
+  void calcDensityOnGrid(const DensityMatrix<M>& P, DensityOnGrid<M>& rho) { run(P, rho, nullptr); }
   DensityOnGrid<M> calcDensityOnGrid(const DensityMatrix<M>& P) {
     DensityOnGrid<M> rho;
     run(P, rho, nullptr);
@@ -285,6 +348,11 @@ class DensityOnGridCalculator {
                                     Gradient<DensityOnGrid<M>>& grad) {
     run(P, rho, &grad);
   }
+  std::shared_ptr<BasisFunctionOnGridController> getBasisFunctionOnGridController() const { return bfog_; }
+  std::shared_ptr<GridController> getGridController() const { return bfog_->getGridController(); }
+  /* the blocks with at least one non-negligible basis function in the last transform
+   * (MatrixOperatorToGridTransformer.cpp:102-124, DensityOnGridCalculator.h:126-128) */
+  SparseVectorInt getNonNegligibleBlocks() { return nonNegligible_; }
 
  private:
   void run(const DensityMatrix<M>& P, DensityOnGrid<M>& rho, Gradient<DensityOnGrid<M>>* grad) {
@@ -310,40 +378,219 @@ class DensityOnGridCalculator {
       detail::unpack(gy.data(), n, grad->y);
       detail::unpack(gz.data(), n, grad->z);
     }
+    const unsigned nb = bfog_->getNBlocks();
+    nonNegligible_ = SparseVectorInt{};
+    nonNegligible_.size = nb;
+    for (unsigned b = 0; b < nb; ++b)
+      if (xcgpu_block_active(bfog_->handle(), b, nullptr) > 0) {
+        nonNegligible_.indices.push_back((int)b);
+        nonNegligible_.values.push_back(1);
+      }
   }
   std::shared_ptr<BasisFunctionOnGridController> bfog_;
   double thr_;
   int precision_;
+  SparseVectorInt nonNegligible_;
+};
+
+/* DensityMatrixController<M>: holds the density matrix; setting a new one notifies the
+ * objects built on it (a DensityMatrixDensityOnGridController, say) */
+template <Options::SCF_MODES M>
+class DensityMatrixController : public NotifyingClass {
+ public:
+  explicit DensityMatrixController(const DensityMatrix<M>& P) : P_(P) {}
+  const DensityMatrix<M>& getDensityMatrix() const { return P_; }
+  void setDensityMatrix(const DensityMatrix<M>& P) {
+    P_ = P;
+    this->notifyObjects();
+  }
+
+ private:
+  DensityMatrix<M> P_;
+};
+
+/* DensityOnGridController<M> (DensityOnGridController.h:40-140): a density on a grid,
+ * formed lazily, invalidated through notify() */
+template <Options::SCF_MODES M>
+class DensityOnGridController : public NotifyingClass, public ObjectSensitiveClass {
+ public:
+  DensityOnGridController(std::shared_ptr<GridController> grid, unsigned int highestDerivative)
+      : _gridController(grid), _highestDerivative(highestDerivative), _nGridPoints(grid->getNGridPoints()) {}
+  virtual const DensityOnGrid<M>& getDensityOnGrid() = 0;
+  virtual const Gradient<DensityOnGrid<M>>& getDensityGradientOnGrid() = 0;
+  virtual const Hessian<DensityOnGrid<M>>& getDensityHessianOnGrid() {
+    throw SerenityError("Density Hessians on the grid are not part of this XC path.");
+  }
+  unsigned int getNGridPoints() const { return _nGridPoints; }
+  unsigned int getHighestDerivative() const { return _highestDerivative; }
+  virtual void setHighestDerivative(unsigned int newHighestDerivative) = 0;
+  std::shared_ptr<GridController> getGridController() const { return _gridController; }
+  void notify() override {
+    _upToDate = false;
+    this->notifyObjects();
+  }
+  virtual SparseVectorInt getNonNegligibleBlocks() {
+    throw SerenityError("Overwrite this function in the specific realizations, please!");
+  }
+  virtual unsigned int getNBlocks() { throw SerenityError("Overwrite this function in the specific realizations, please!"); }
+  virtual unsigned int getMaxBlockSize() {
+    throw SerenityError("Overwrite this function in the specific realizations, please!");
+  }
+
+ protected:
+  const std::shared_ptr<GridController> _gridController;
+  unsigned int _highestDerivative;
+  unsigned int _nGridPoints;
+  bool _upToDate = false;
+  DensityOnGrid<M> _densityOnGrid;
+  Gradient<DensityOnGrid<M>> _densityGradientOnGrid;
+};
+
+/* DensityMatrixDensityOnGridController<M> (DensityMatrixDensityOnGridController.cpp:28-187):
+ * the density of a DensityMatrixController's matrix on the grid, formed on first use after
+ * every change of the matrix (it registers with the controller); with
+ * iOOptions.gridAccuracyCheck it prints the electrons integrated over the grid per spin. */
+template <Options::SCF_MODES M>
+class DensityMatrixDensityOnGridController : public DensityOnGridController<M> {
+ public:
+  DensityMatrixDensityOnGridController(std::shared_ptr<DensityOnGridCalculator<M>> calc,
+                                       std::shared_ptr<DensityMatrixController<M>> dmat)
+      : DensityMatrixDensityOnGridController(calc, dmat,
+                                             calc->getBasisFunctionOnGridController()->getHighestDerivative()) {}
+  DensityMatrixDensityOnGridController(std::shared_ptr<DensityOnGridCalculator<M>> calc,
+                                       std::shared_ptr<DensityMatrixController<M>> dmat, unsigned int highestDerivative)
+      : DensityOnGridController<M>(calc->getGridController(), highestDerivative), calc_(calc), dmat_(dmat) {
+    if (highestDerivative > calc->getBasisFunctionOnGridController()->getHighestDerivative())
+      throw SerenityError("DensityMatrixDensityOnGridController: derivative beyond the basis data's");
+    dmat_->addSensitiveObject(this->_self);
+  }
+  const DensityOnGrid<M>& getDensityOnGrid() override {
+    if (!this->_upToDate) calculateData();
+    return this->_densityOnGrid;
+  }
+  const Gradient<DensityOnGrid<M>>& getDensityGradientOnGrid() override {
+    if (this->_highestDerivative < 1) setHighestDerivative(1);
+    if (!this->_upToDate) calculateData();
+    return this->_densityGradientOnGrid;
+  }
+  void setHighestDerivative(unsigned int d) override {
+    if (d > 1) throw SerenityError("Density Hessians on the grid are not part of this XC path.");
+    if (d != this->_highestDerivative) this->notify();
+    this->_highestDerivative = d;
+  }
+  SparseVectorInt getNonNegligibleBlocks() override { return calc_->getNonNegligibleBlocks(); }
+  unsigned int getNBlocks() override { return calc_->getBasisFunctionOnGridController()->getNBlocks(); }
+  unsigned int getMaxBlockSize() override { return calc_->getBasisFunctionOnGridController()->getMaxBlockSize(); }
+  std::shared_ptr<DensityOnGridCalculator<M>> getDensityOnGridCalculator() const { return calc_; }
+  /* electrons integrated over the grid per spin at the last evaluation (what
+   * gridAccuracyCheck prints) */
+  const std::vector<double>& getLastElectronCount() const { return nel_; }
+
+ private:
+  void calculateData() {
+    const auto& P = dmat_->getDensityMatrix();
+    if (this->_highestDerivative == 0)
+      calc_->calcDensityOnGrid(P, this->_densityOnGrid);
+    else
+      calc_->calcDensityAndGradientOnGrid(P, this->_densityOnGrid, this->_densityGradientOnGrid);
+    const auto& w = this->_gridController->getWeights();
+    std::vector<double> r;
+    detail::pack(this->_densityOnGrid, r);
+    const int ns = detail::nspin<M>();
+    nel_.assign(ns, 0.0);
+    for (int s = 0; s < ns; ++s)
+      for (size_t p = 0; p < w.size(); ++p) nel_[s] += r[s * w.size() + p] * w[p];
+    if (iOOptions.gridAccuracyCheck)
+      for (int s = 0; s < ns; ++s) std::printf("nElectrons from integration over grid: %.10f\n", nel_[s]);
+    this->_upToDate = true;
+  }
+  std::shared_ptr<DensityOnGridCalculator<M>> calc_;
+  std::shared_ptr<DensityMatrixController<M>> dmat_;
+  std::vector<double> nel_;
 };
 
 enum class FUNCTIONAL_DATA_TYPE { GRADIENTS };
-/* composite functionals of this path (CompositeFunctionals.cpp:233-246) */
-enum class Functional { LDA = XCGPU_FUNC_LDA, PBE = XCGPU_FUNC_PBE, BLYP = XCGPU_FUNC_BLYP, BP86 = XCGPU_FUNC_BP86 };
 
+namespace CompositeFunctionals {
+/* the composite functionals of this path (CompositeFunctionals.cpp:233-246) */
+enum class FUNCTIONALS { LDA, PBE, BLYP, BP86 };
+enum class CLASSES { NONE, LDA, GGA, MODELL };
+}  // namespace CompositeFunctionals
+
+/* A resolved functional (src/dft/Functional.h): its library identifier and class */
+class Functional {
+ public:
+  explicit constexpr Functional(int id = XCGPU_FUNC_LDA) : id_(id) {}
+  int id() const { return id_; }
+  bool isGGA() const { return xcgpu_functional_is_gga(id_) != 0; }
+  CompositeFunctionals::CLASSES getFunctionalClass() const {
+    return isGGA() ? CompositeFunctionals::CLASSES::GGA : CompositeFunctionals::CLASSES::LDA;
+  }
+  explicit operator int() const { return id_; }
+  bool operator==(const Functional& o) const { return id_ == o.id_; }
+  static const Functional LDA, PBE, BLYP, BP86;
+
+ private:
+  int id_;
+};
+inline const Functional Functional::LDA{XCGPU_FUNC_LDA};
+inline const Functional Functional::PBE{XCGPU_FUNC_PBE};
+inline const Functional Functional::BLYP{XCGPU_FUNC_BLYP};
+inline const Functional Functional::BP86{XCGPU_FUNC_BP86};
+
+namespace CompositeFunctionals {
+/* CompositeFunctionals::resolveFunctional (CompositeFunctionals.cpp:42-73) */
+inline Functional resolveFunctional(FUNCTIONALS f) {
+  switch (f) {
+    case FUNCTIONALS::LDA: return Functional::LDA;
+    case FUNCTIONALS::PBE: return Functional::PBE;
+    case FUNCTIONALS::BLYP: return Functional::BLYP;
+    case FUNCTIONALS::BP86: return Functional::BP86;
+  }
+  throw SerenityError("You have requested a functional that this path cannot provide.");
+}
+}  // namespace CompositeFunctionals
+
+/* FunctionalData<M> (PartialDerivatives.h:931-1090): the energy, the energy per volume and
+ * the first derivatives, held by shared pointers as in the reference */
 template <Options::SCF_MODES M>
 struct FunctionalData {
   double energy = 0.0;
-  Vector epuv;
-  DensityOnGrid<M> dFdRho;
-  std::shared_ptr<Gradient<DensityOnGrid<M>>> dFdGradRho;
+  std::shared_ptr<Vector> epuv;
+  std::shared_ptr<GridPotential<M>> dFdRho;
+  std::shared_ptr<Gradient<GridPotential<M>>> dFdGradRho;
 };
 
 template <Options::SCF_MODES M>
 class FunctionalLibrary {
  public:
   explicit FunctionalLibrary(unsigned int maxBlockSize) : block_(maxBlockSize) {}
-  FunctionalData<M> calcData(FUNCTIONAL_DATA_TYPE, Functional f, const GridController& grid,
+  /* FunctionalLibrary<M>::calcData (FunctionalLibrary.h:60-62): the density (and, for a
+   * GGA, its gradient) comes from the controller, formed there on demand */
+  FunctionalData<M> calcData(FUNCTIONAL_DATA_TYPE type, const Functional& f,
+                             std::shared_ptr<DensityOnGridController<M>> densityOnGridController,
+                             unsigned int order = 1) {
+    const bool gga = f.isGGA();
+    if (gga && densityOnGridController->getHighestDerivative() < 1)
+      throw SerenityError("XCFun: Density gradient required for GGA functional, but DensityOnGridController does not have it.");
+    const auto& rho = densityOnGridController->getDensityOnGrid();
+    const Gradient<DensityOnGrid<M>>* grad = gga ? &densityOnGridController->getDensityGradientOnGrid() : nullptr;
+    return calcData(type, f, *densityOnGridController->getGridController(), rho, grad, order);
+  }
+  /* the same from a density already on the grid */
+  FunctionalData<M> calcData(FUNCTIONAL_DATA_TYPE, const Functional& f, const GridController& grid,
                              const DensityOnGrid<M>& rho, const Gradient<DensityOnGrid<M>>* grad,
                              unsigned int order = 1) {
     if (order != 1) throw SerenityError("only first functional derivatives are available on this path");
     const int ns = detail::nspin<M>();
     const long n = grid.getNGridPoints();
-    const int func = (int)f;
-    const bool gga = xcgpu_functional_is_gga(func) != 0;
+    const int func = f.id();
+    const bool gga = f.isGGA();
     if (gga && !grad)
       throw SerenityError("XCFun: Density gradient required for GGA functional, but DensityOnGridController does not have it.");
     std::vector<double> r, g;
     detail::pack(rho, r);
+    if (r.size() != (size_t)ns * n) throw SerenityError("FunctionalLibrary: density and grid do not match");
     if (gga) {
       for (int s = 0; s < ns; ++s)
         for (const auto* comp : {&grad->x, &grad->y, &grad->z}) {
@@ -353,16 +600,17 @@ class FunctionalLibrary {
         }
     }
     FunctionalData<M> out;
-    out.epuv.assign(n, 0.0);
+    out.epuv = std::make_shared<Vector>(n, 0.0);
+    out.dFdRho = std::make_shared<GridPotential<M>>();
     std::vector<double> dr((size_t)ns * n), dg(gga ? (size_t)ns * 3 * n : 0);
     auto ctx = grid.context();
     detail::check(ctx->get(), xcgpu_functional(ctx->get(), func, ns, n, block_, r.data(), gga ? g.data() : nullptr,
-                                               out.epuv.data(), dr.data(), gga ? dg.data() : nullptr, XCGPU_MEM_HOST));
-    detail::unpack(dr.data(), n, out.dFdRho);
+                                               out.epuv->data(), dr.data(), gga ? dg.data() : nullptr, XCGPU_MEM_HOST));
+    detail::unpack(dr.data(), n, *out.dFdRho);
     const auto& w = grid.getWeights();
-    for (long p = 0; p < n; ++p) out.energy += out.epuv[p] * w[p];
+    for (long p = 0; p < n; ++p) out.energy += (*out.epuv)[p] * w[p];
     if (gga) {
-      out.dFdGradRho = std::make_shared<Gradient<DensityOnGrid<M>>>();
+      out.dFdGradRho = std::make_shared<Gradient<GridPotential<M>>>();
       std::vector<double> cx, cy, cz;
       for (int s = 0; s < ns; ++s) {
         cx.insert(cx.end(), dg.begin() + (s * 3 + 0) * n, dg.begin() + (s * 3 + 1) * n);
@@ -432,7 +680,7 @@ class FuncPotential {
     const long nbf = bfog_->getNBasisFunctions();
     std::vector<double> Pv, Vv((size_t)ns * nbf * nbf);
     detail::pack(P, Pv);
-    detail::check(bfog_->ctx(), xcgpu_vxc(bfog_->handle(), (int)f_, ns, precision_, thr_, Pv.data(), Vv.data(),
+    detail::check(bfog_->ctx(), xcgpu_vxc(bfog_->handle(), f_.id(), ns, precision_, thr_, Pv.data(), Vv.data(),
                                           &energy_, &nel_, XCGPU_MEM_HOST));
     FockMatrix<M> F = P;
     detail::unpack(Vv.data(), F);
@@ -447,7 +695,7 @@ class FuncPotential {
     std::vector<double> Pv;
     detail::pack(P, Pv);
     Matrix G(natoms, 3);
-    detail::check(bfog_->ctx(), xcgpu_xc_gradient(bfog_->handle(), (int)f_, ns, Pv.data(), shellAtoms.data(), natoms,
+    detail::check(bfog_->ctx(), xcgpu_xc_gradient(bfog_->handle(), f_.id(), ns, Pv.data(), shellAtoms.data(), natoms,
                                                   G.data(), XCGPU_MEM_HOST));
     return G;
   }
@@ -478,7 +726,7 @@ class KernelSigmavector {
       d.push_back(trials[t].data());
       f.push_back(F[t].data());
     }
-    detail::check(bfog_->ctx(), xcgpu_lr_kernel(bfog_->handle(), (int)f_, P0.data(), (uint32_t)trials.size(), d.data(),
+    detail::check(bfog_->ctx(), xcgpu_lr_kernel(bfog_->handle(), f_.id(), P0.data(), (uint32_t)trials.size(), d.data(),
                                                 f.data(), precision_, thr_, XCGPU_MEM_HOST));
     return F;
   }
@@ -517,7 +765,7 @@ class NAddFuncPotential {
       plans.push_back(env_[i]->handle());
       ptrs.push_back(Pe[i].data());
     }
-    detail::check(active_->ctx(), xcgpu_nadd_vxc(active_->handle(), plans.data(), (uint32_t)plans.size(), (int)f_, ns,
+    detail::check(active_->ctx(), xcgpu_nadd_vxc(active_->handle(), plans.data(), (uint32_t)plans.size(), f_.id(), ns,
                                                  precision_, thr_, Pv.data(), ptrs.data(), Vv.data(), &energy_,
                                                  XCGPU_MEM_HOST));
     FockMatrix<M> F = P;

@@ -3,6 +3,7 @@
 // (testsupply/BasisController__TEST_SUPPLY.cpp:59-84, GridController__TEST_SUPPLY.cpp:31-46).
 // Prints the results as JSON; tests/test_facade.py compares them with the golden
 // vectors of the reference tests.
+#include <cmath>
 #include <cstdio>
 #include <memory>
 
@@ -11,6 +12,10 @@
 using namespace Serenity;
 
 // every member of the class templates compiles against the C ABI
+template class Serenity::DensityMatrixDensityOnGridController<RESTRICTED>;
+template class Serenity::DensityMatrixDensityOnGridController<UNRESTRICTED>;
+template class Serenity::FunctionalLibrary<RESTRICTED>;
+template class Serenity::FunctionalLibrary<UNRESTRICTED>;
 template class Serenity::NAddFuncPotential<RESTRICTED>;
 template class Serenity::NAddFuncPotential<UNRESTRICTED>;
 template class Serenity::FuncPotential<RESTRICTED>;
@@ -31,7 +36,64 @@ static void print_vec(const char* name, const std::vector<double>& v, bool last 
 int main() {
   auto ctx = std::make_shared<XcContext>(0);
   auto basis = std::make_shared<BasisController>(ctx, small_mixed());
+  // The reference's FuncPotential::getMatrix chain (FuncPotential.cpp:57-105) on the facade,
+  // call for call: a DensityMatrixController, a DensityOnGridCalculator and the lazy
+  // DensityMatrixDensityOnGridController, FunctionalLibrary(128).calcData(GRADIENTS, f,
+  // controller) and the adder; against the fused build (FuncPotential::getMatrix here).
+  // gridAccuracyCheck prints its electron counts before the JSON below.
+  std::vector<double> staged_F, fused_F, rho_before, rho_after;
+  double staged_E = 0.0, fused_E = 0.0, nel_grid = 0.0, nel_sum = 0.0;
+  long nonneg = 0, nblocks_lazy = 0;
+  {
+    std::vector<double> xyz, w;
+    for (int i = 0; i < 200; ++i) {  // 200 points around the SMALL_MIXED centres
+      const double t = 0.37 * i;
+      xyz.insert(xyz.end(), {-1.5 + 0.02 * i, 2.0 * std::sin(t), 1.5 * std::cos(1.3 * t)});
+      w.push_back(0.05 + 0.001 * (i % 7));
+    }
+    auto grid = std::make_shared<GridController>(ctx, xyz, w);
+    auto bfog = std::make_shared<BasisFunctionOnGridController>(basis, grid, 128, 1e-9, 1);
+    Matrix P(10, 10);
+    for (int i = 0; i < 10; ++i)
+      for (int j = 0; j < 10; ++j) P(i, j) = (i == j ? 0.6 : 0.0) + 0.05 / (1.0 + i + j);
+    auto dmat = std::make_shared<DensityMatrixController<RESTRICTED>>(P);
+    auto calc = std::make_shared<DensityOnGridCalculator<RESTRICTED>>(bfog, 1e-11);
+    auto dens = std::make_shared<DensityMatrixDensityOnGridController<RESTRICTED>>(calc, dmat);
+    auto adder = std::make_shared<ScalarOperatorToMatrixAdder<RESTRICTED>>(bfog, 1e-11);
+    const Functional f = CompositeFunctionals::resolveFunctional(CompositeFunctionals::FUNCTIONALS::PBE);
+    iOOptions.gridAccuracyCheck = true;
+    FunctionalLibrary<RESTRICTED> flib(128);
+    auto funcData = flib.calcData(FUNCTIONAL_DATA_TYPE::GRADIENTS, f, dens);
+    iOOptions.gridAccuracyCheck = false;
+    FockMatrix<RESTRICTED> pot(10, 10);
+    if (f.getFunctionalClass() == CompositeFunctionals::CLASSES::GGA)
+      adder->addScalarOperatorToMatrix(pot, *funcData.dFdRho, *funcData.dFdGradRho);
+    else
+      adder->addScalarOperatorToMatrix(pot, *funcData.dFdRho);
+    staged_E = funcData.energy;
+    staged_F.assign(pot.data(), pot.data() + 100);
+    FuncPotential<RESTRICTED> fused(bfog, f);
+    auto F = fused.getMatrix(P);
+    fused_E = fused.getEnergy();
+    fused_F.assign(F.data(), F.data() + 100);
+    nel_grid = dens->getLastElectronCount()[0];
+    for (size_t p = 0; p < w.size(); ++p) nel_sum += dens->getDensityOnGrid()[p] * w[p];
+    rho_before = dens->getDensityOnGrid();
+    Matrix P2 = P;
+    for (int i = 0; i < 10; ++i) P2(i, i) *= 2.0;
+    dmat->setDensityMatrix(P2);  // notifies the controller: the next read recomputes
+    rho_after = dens->getDensityOnGrid();
+    nonneg = dens->getNonNegligibleBlocks().nonZeros();
+    nblocks_lazy = dens->getNBlocks();
+  }
   std::printf("{\n");
+  print_vec("staged_F", staged_F);
+  print_vec("fused_F", fused_F);
+  print_vec("rho_before", rho_before);
+  print_vec("rho_after", rho_after);
+  std::printf("\"staged_E\": %.17g, \"fused_E\": %.17g, \"nel_grid\": %.17g, \"nel_sum\": %.17g,\n", staged_E,
+              fused_E, nel_grid, nel_sum);
+  std::printf("\"nonnegligible_blocks\": %ld, \"nblocks_lazy\": %ld,\n", nonneg, nblocks_lazy);
   {  // density on TINY, blocks of 3, no radial cut-off (DensityOnGridCalculator_test.cpp:43-256)
     std::vector<double> xyz = {0.0, 0.0, 0.0, 1.0, 0.0, 0.0, -2.0, 1.0, 1.0, 3.0, 0.5, -1.0};
     auto grid = std::make_shared<GridController>(ctx, xyz, std::vector<double>(4, 1.0));

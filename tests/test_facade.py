@@ -1,5 +1,9 @@
 """The C++ facade (include/serenity_xc.hpp): compiles against the C ABI here, and on a
-GPU reproduces the reference's golden density and adder vectors."""
+GPU reproduces the reference's golden density and adder vectors; runs the reference's
+FuncPotential::getMatrix chain (lazy DensityMatrixDensityOnGridController,
+FunctionalLibrary::calcData with the controller, the adder) to the fused build's result;
+recomputes the density after the density matrix changes; prints the grid electron count
+with gridAccuracyCheck; lists the non-negligible blocks."""
 import json
 import os
 import subprocess
@@ -32,7 +36,15 @@ def test_facade_matches_reference_golden(tmp_path, golden):
     np.savetxt(pfile, np.array(d["P"]).T.reshape(-1))  # column-major
     out = subprocess.run([exe], check=True, capture_output=True, text=True,
                          env=dict(os.environ, FACADE_P=str(pfile))).stdout
-    r = json.loads(out)
+    printed = out[:out.index("{\n")]
+    r = json.loads(out[out.index("{\n"):])
+    # staged chain = fused build (both FP64)
+    np.testing.assert_allclose(r["staged_F"], r["fused_F"], rtol=1e-12, atol=1e-14)
+    assert abs(r["staged_E"] - r["fused_E"]) <= 1e-12 * abs(r["fused_E"])
+    assert "nElectrons from integration over grid" in printed
+    assert abs(r["nel_grid"] - r["nel_sum"]) <= 1e-12 * abs(r["nel_sum"])
+    assert not np.allclose(r["rho_before"], r["rho_after"])  # invalidated and recomputed
+    assert 0 < r["nonnegligible_blocks"] <= r["nblocks_lazy"] == 2
     np.testing.assert_allclose(r["rho"], d["rho"], rtol=0, atol=d["tolerance"])
     np.testing.assert_allclose(r["grad_x"], d["grad"][0], rtol=0, atol=d["tolerance"])
     assert r["nblocks"] == 2
