@@ -14,7 +14,7 @@
  *   FuncPotential<M> (getMatrix, getEnergy)  src/potentials/FuncPotential.h
  *   NAddFuncPotential<M> (getMatrix, getEnergy)  src/potentials/NAddFuncPotential.h
  *   FuncPotential<M>::getGeomGradients           src/potentials/FuncPotential.cpp:113-241
- *   KernelSigmavector (restricted singlet calcF)  src/postHF/LRSCF/Sigmavectors/KernelSigmavector.h
+ *   KernelSigmavector<M>::calcF (singlet, triplet, unrestricted)  src/postHF/LRSCF/Sigmavectors/KernelSigmavector.h
  *
  * Errors are thrown as SerenityError, as in the reference.  Matrices and grid data are
  * plain column-major containers with the memory layout of Eigen's defaults
@@ -708,26 +708,42 @@ class FuncPotential {
   double energy_ = 0.0, nel_ = 0.0;
 };
 
-// The XC kernel part of restricted (singlet) linear-response sigma vectors
-// (KernelSigmavector<RESTRICTED>::calcF, src/postHF/LRSCF/Sigmavectors/KernelSigmavector.cpp:128-392):
-// calcF(P0, trials) returns one matrix per trial matrix.
+// The XC kernel part of linear-response sigma vectors (KernelSigmavector<M>::calcF,
+// src/postHF/LRSCF/Sigmavectors/KernelSigmavector.cpp:127-253, contractBlock :363-499):
+// calcF(P0, trials) returns one matrix per trial matrix.  Restricted: the singlet kernel,
+// or with triplet = true the triplet's f_aa - f_ab; unrestricted: alpha and beta trial
+// and result matrices.
+template <Options::SCF_MODES M>
 class KernelSigmavector {
  public:
   KernelSigmavector(std::shared_ptr<BasisFunctionOnGridController> bfog, Functional f,
-                    double blockAveThreshold = 1e-11, int precision = XCGPU_PREC_FP64)
-      : bfog_(bfog), f_(f), thr_(blockAveThreshold), precision_(precision) {}
-  std::vector<Matrix> calcF(const Matrix& P0, const std::vector<Matrix>& trials) {
+                    double blockAveThreshold = 1e-11, int precision = XCGPU_PREC_FP64, bool triplet = false)
+      : bfog_(bfog), f_(f), thr_(blockAveThreshold), precision_(precision), triplet_(triplet) {
+    if (triplet && M == Options::SCF_MODES::UNRESTRICTED)
+      throw SerenityError("KernelSigmavector: the triplet kernel belongs to a restricted ground state");
+  }
+  std::vector<SPMatrix<M>> calcF(const SPMatrix<M>& P0, const std::vector<SPMatrix<M>>& trials) {
     const long nbf = bfog_->getNBasisFunctions();
-    std::vector<Matrix> F(trials.size(), Matrix(nbf, nbf));
+    const int ns = detail::nspin<M>();
+    std::vector<double> P0v;
+    detail::pack(P0, P0v);
+    if (P0v.size() != (size_t)ns * nbf * nbf) throw SerenityError("KernelSigmavector: size mismatch");
+    std::vector<std::vector<double>> Dv(trials.size()), Fv(trials.size(), std::vector<double>((size_t)ns * nbf * nbf));
     std::vector<const double*> d;
     std::vector<double*> f;
     for (size_t t = 0; t < trials.size(); ++t) {
-      if (trials[t].rows() != nbf || trials[t].cols() != nbf) throw SerenityError("KernelSigmavector: size mismatch");
-      d.push_back(trials[t].data());
-      f.push_back(F[t].data());
+      detail::pack(trials[t], Dv[t]);
+      if (Dv[t].size() != (size_t)ns * nbf * nbf) throw SerenityError("KernelSigmavector: size mismatch");
+      d.push_back(Dv[t].data());
+      f.push_back(Fv[t].data());
     }
-    detail::check(bfog_->ctx(), xcgpu_lr_kernel(bfog_->handle(), f_.id(), P0.data(), (uint32_t)trials.size(), d.data(),
-                                                f.data(), precision_, thr_, XCGPU_MEM_HOST));
+    const int kind = M == Options::SCF_MODES::UNRESTRICTED ? XCGPU_LR_UNRESTRICTED
+                     : triplet_                             ? XCGPU_LR_TRIPLET
+                                                            : XCGPU_LR_SINGLET;
+    detail::check(bfog_->ctx(), xcgpu_lr_kernel_spin(bfog_->handle(), f_.id(), kind, P0v.data(), (uint32_t)trials.size(),
+                                                     d.data(), f.data(), precision_, thr_, XCGPU_MEM_HOST));
+    std::vector<SPMatrix<M>> F(trials.begin(), trials.end());
+    for (size_t t = 0; t < trials.size(); ++t) detail::unpack(Fv[t].data(), F[t]);
     return F;
   }
 
@@ -736,6 +752,7 @@ class KernelSigmavector {
   Functional f_;
   double thr_;
   int precision_;
+  bool triplet_;
 };
 
 // NAddFuncPotential<M> (src/potentials/NAddFuncPotential.h:93-200): the non-additive XC

@@ -216,6 +216,19 @@ xcgpu_status xcgpu_vxc(xcgpu_plan* plan, int func, int nspin, int precision, dou
  * adder's block skip.  All matrices in `mem` space. */
 xcgpu_status xcgpu_lr_kernel(xcgpu_plan* plan, int func, const double* P0, uint32_t ntrial, const double* const* D,
                              double* const* F, int precision, double block_ave_threshold, int mem);
+/* The kinds of xcgpu_lr_kernel_spin */
+enum { XCGPU_LR_SINGLET = 0, XCGPU_LR_TRIPLET = 1, XCGPU_LR_UNRESTRICTED = 2 };
+/* KernelSigmavector<M>::calcF with the spin kernels (KernelSigmavector.cpp:127-253 with
+ * contractBlock :363-499): XCGPU_LR_SINGLET is xcgpu_lr_kernel; XCGPU_LR_TRIPLET contracts
+ * (f_aa - f_ab) of the restricted ground state P0 (total density, nbf x nbf) with each
+ * symmetrised trial matrix D[t] (nbf x nbf) into F[t] (nbf x nbf); XCGPU_LR_UNRESTRICTED
+ * takes P0 = (P_alpha, P_beta), D[t] = (D_alpha, D_beta) and returns F[t] = (F_alpha,
+ * F_beta), each 2 x nbf x nbf, the spin blocks consecutive.  Each F is the directional
+ * derivative of the XC matrix: F_s(D) = d/de Vxc_s[P_a + e D_a, P_b + e D_b] with the
+ * triplet's perturbation (+D, -D) about (P0/2, P0/2).  F is overwritten. */
+xcgpu_status xcgpu_lr_kernel_spin(xcgpu_plan* plan, int func, int kind, const double* P0, uint32_t ntrial,
+                                  const double* const* D, double* const* F, int precision,
+                                  double block_ave_threshold, int mem);
 
 /* ---- XC part of the nuclear gradient ------------------------------------------------
  * FuncPotential<M>::getGeomGradients (FuncPotential.cpp:113-241): for every pair of active

@@ -434,6 +434,50 @@ void lr_kernel_point(int func, double n0, const double* g0, double n1, const dou
     for (int k = 0; k < 3; ++k) gg1[k] = 2.0 * (e.h[1][0] * n1 + e.h[1][1] * sig1) * g0[k] + 2.0 * e.d[1] * g1[k];
 }
 
+// Spin-resolved kernel contraction (KernelSigmavector<UNRESTRICTED>::contractBlock,
+// KernelSigmavector.cpp:422-499; the triplet's f_aa - f_ab of :367-391 is the alpha part of
+// the perturbation (+rho1, -rho1) about (rho0/2, rho0/2)): with x = (n_a, n_b, s_aa, s_ab,
+// s_bb) and x1 its first-order change, dd_i = sum_j E_ij x1_j, and
+//   v1_a = dd_0, v1_b = dd_1,
+//   g1_a = 2 dd_2 grad n_a + 2 E_2 grad n1_a + dd_3 grad n_b + E_3 grad n1_b, alike for b.
+// n0[2], g0[2][3] (ground state per spin), n1[2], g1[2][3]; v1[2], gg1[2][3] out.
+void lr_kernel_spin_point(int func, const double* n0, const double* g0, const double* n1, const double* g1,
+                          double* v1, double* gg1) {
+  const bool gga = functional_is_gga(func);
+  for (int s = 0; s < 2; ++s) {
+    v1[s] = 0.0;
+    for (int k = 0; k < 3; ++k) gg1[3 * s + k] = 0.0;
+  }
+  const double na0 = n0[0] > 0 ? n0[0] : 0.0, nb0 = n0[1] > 0 ? n0[1] : 0.0;
+  if (!(na0 + nb0 >= kDensTiny)) return;
+  const double na1 = n0[0] > 0 ? n1[0] : 0.0, nb1 = n0[1] > 0 ? n1[1] : 0.0;
+  double x1[5] = {na1, nb1, 0.0, 0.0, 0.0}, s[3] = {0.0, 0.0, 0.0};
+  const double *ga = g0, *gb = g0 + 3, *da = g1, *db = g1 + 3;
+  if (gga)
+    for (int k = 0; k < 3; ++k) {
+      s[0] += ga[k] * ga[k];
+      s[1] += ga[k] * gb[k];
+      s[2] += gb[k] * gb[k];
+      x1[2] += 2.0 * ga[k] * da[k];
+      x1[3] += ga[k] * db[k] + da[k] * gb[k];
+      x1[4] += 2.0 * gb[k] * db[k];
+    }
+  typedef H<5> T;
+  T e = energy(func, T::var(na0, 0), T::var(nb0, 1), T::var(s[0], 2), T::var(s[1], 3), T::var(s[2], 4));
+  double dd[5];
+  for (int i = 0; i < 5; ++i) {
+    dd[i] = 0.0;
+    for (int j = 0; j < 5; ++j) dd[i] += e.h[i][j] * x1[j];
+  }
+  v1[0] = dd[0];
+  v1[1] = dd[1];
+  if (gga)
+    for (int k = 0; k < 3; ++k) {
+      gg1[k] = 2.0 * dd[2] * ga[k] + 2.0 * e.d[2] * da[k] + dd[3] * gb[k] + e.d[3] * db[k];
+      gg1[3 + k] = 2.0 * dd[4] * gb[k] + 2.0 * e.d[4] * db[k] + dd[3] * ga[k] + e.d[3] * da[k];
+    }
+}
+
 void functional_point(int func, int nspin, const double* in, double* out) {
   const bool gga = functional_is_gga(func);
   if (nspin == 1) {

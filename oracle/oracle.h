@@ -110,6 +110,10 @@ int orc_xc_gradient(const void* basis, const int* shell_atom, int natoms, const 
  * rho0 as the functional data.  grad arrays [3][npts] (GGA). */
 int orc_lr_kernel(int func, long npts, const double* rho0, const double* grad0, const double* rho1,
                   const double* grad1, double* v1, double* g1);
+/* The spin-resolved contraction: kind 2 unrestricted (per-spin inputs and outputs), kind 1
+ * triplet (restricted ground state, perturbation (+rho1, -rho1), alpha outputs). */
+int orc_lr_kernel_spin(int func, int kind, long npts, const double* rho0, const double* grad0, const double* rho1,
+                       const double* grad1, double* v1, double* g1);
 
 #ifdef __cplusplus
 }

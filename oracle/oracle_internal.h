@@ -39,6 +39,8 @@ void functional_point(int func, int nspin, const double* in, double* out);
 bool functional_is_gga(int func);
 /* restricted linear-response kernel contracted with (rho1, grad rho1): v1, g1[3] */
 void lr_kernel_point(int func, double n0, const double* g0, double n1, const double* g1, double* v1, double* gg1);
+void lr_kernel_spin_point(int func, const double* n0, const double* g0, const double* n1, const double* g1,
+                          double* v1, double* gg1);
 
 }  // namespace orc
 #endif

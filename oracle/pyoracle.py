@@ -263,3 +263,30 @@ def lr_fock(basis, xyz, w, func, P0, D, max_block=128, thr=1e-9, ave_thr=1e-11):
     r1, g1 = basis.density(xyz, Ds, max_block, thr, grad=gga)
     v1, gv1 = lr_kernel(func, r0[0], g0[0] if gga else None, r1[0], g1[0] if gga else None)
     return basis.add_scalar(xyz, w, v1, gv1.reshape(1, 3, -1) if gga else None, max_block, thr, ave_thr)[0]
+
+
+def lr_fock_spin(basis, xyz, w, func, P0, D, kind, max_block=128, thr=1e-9, ave_thr=1e-11):
+    """XC-kernel part of a linear-response sigma vector with the spin kernels
+    (KernelSigmavector.cpp:127-253, contractBlock :363-499).  kind "unrestricted": P0 and D
+    [2, nbf, nbf], returns [2, nbf, nbf]; "triplet": P0 (restricted total) and D [nbf, nbf],
+    returns [nbf, nbf].  Each spin's D is symmetrised."""
+    fid = FUNC[func] if isinstance(func, str) else int(func)
+    gga = bool(lib().orc_functional_is_gga(fid))
+    code = {"triplet": 1, "unrestricted": 2}[kind]
+    ns = 2 if kind == "unrestricted" else 1
+    D = np.asarray(D, dtype=np.float64).reshape(ns, basis.nbf, basis.nbf)
+    Ds = 0.5 * (D + np.swapaxes(D, 1, 2))
+    P0 = np.asarray(P0, dtype=np.float64).reshape(ns, basis.nbf, basis.nbf)
+    r0, g0 = basis.density(xyz, P0 if ns == 2 else P0[0], max_block, thr, grad=gga)
+    r1, g1 = basis.density(xyz, Ds if ns == 2 else Ds[0], max_block, thr, grad=gga)
+    n = r0.shape[1]
+    v1 = np.zeros(ns * n)
+    go = np.zeros(ns * 3 * n) if gga else None
+    L = lib()
+    L.orc_lr_kernel_spin.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, _dp, ctypes.c_void_p, _dp,
+                                     ctypes.c_void_p, _dp, ctypes.c_void_p]
+    c = np.ascontiguousarray
+    L.orc_lr_kernel_spin(fid, code, n, c(r0.reshape(-1)), _ptr(c(g0.reshape(-1)) if gga else None),
+                         c(r1.reshape(-1)), _ptr(c(g1.reshape(-1)) if gga else None), v1, _ptr(go))
+    F = basis.add_scalar(xyz, w, v1.reshape(ns, n), go.reshape(ns, 3, n) if gga else None, max_block, thr, ave_thr)
+    return F if ns == 2 else F[0]

@@ -450,3 +450,48 @@ extern "C" int orc_lr_kernel(int func, long npts, const double* rho0, const doub
   return 0;
 }
 
+
+// The spin-resolved kernel contraction on points, the layout of the GPU's: kind 2
+// (unrestricted) rho0, rho1 [2][n], grad0, grad1 [2][3][n], v1 [2][n], g1 [2][3][n];
+// kind 1 (triplet) rho0, grad0 the restricted total density (each spin half), rho1, grad1
+// one perturbation taken as (+, -), v1 [n], g1 [3][n] the alpha parts.  Blocks of 128
+// points whose spin densities all sum below n 1e-12 give zero (XCFun.cpp:136-140).
+extern "C" int orc_lr_kernel_spin(int func, int kind, long npts, const double* rho0, const double* grad0,
+                                  const double* rho1, const double* grad1, double* v1, double* g1) {
+  const bool gga = orc::functional_is_gga(func), trip = kind == 1;
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < (npts + 127) / 128; ++b) {
+    const long first = b * 128, n = std::min<long>(128, npts - first);
+    double sa = 0.0, sb = 0.0;
+    for (long p = first; p < first + n; ++p) {
+      sa += std::fabs(trip ? 0.5 * rho0[p] : rho0[p]);
+      sb += std::fabs(trip ? 0.5 * rho0[p] : rho0[npts + p]);
+    }
+    const bool skip = sa < n * 1e-12 && sb < n * 1e-12;
+    for (long p = first; p < first + n; ++p) {
+      double n0[2], n1[2], a0[6] = {0, 0, 0, 0, 0, 0}, a1[6] = {0, 0, 0, 0, 0, 0}, v[2] = {0, 0},
+                               out[6] = {0, 0, 0, 0, 0, 0};
+      if (!skip) {
+        n0[0] = trip ? 0.5 * rho0[p] : rho0[p];
+        n0[1] = trip ? n0[0] : rho0[npts + p];
+        n1[0] = rho1[p];
+        n1[1] = trip ? -n1[0] : rho1[npts + p];
+        if (gga)
+          for (int k = 0; k < 3; ++k) {
+            a0[k] = trip ? 0.5 * grad0[k * npts + p] : grad0[k * npts + p];
+            a0[3 + k] = trip ? a0[k] : grad0[(3 + k) * npts + p];
+            a1[k] = grad1[k * npts + p];
+            a1[3 + k] = trip ? -a1[k] : grad1[(3 + k) * npts + p];
+          }
+        orc::lr_kernel_spin_point(func, n0, a0, n1, a1, v, out);
+      }
+      const int nout = trip ? 1 : 2;
+      for (int s = 0; s < nout; ++s) {
+        v1[s * npts + p] = v[s];
+        if (gga)
+          for (int k = 0; k < 3; ++k) g1[(s * 3 + k) * npts + p] = out[3 * s + k];
+      }
+    }
+  }
+  return 0;
+}

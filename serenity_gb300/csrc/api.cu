@@ -1278,6 +1278,91 @@ xcgpu_status xcgpu_lr_kernel(xcgpu_plan* P, int func, const double* P0, uint32_t
   return device_error(c, herr, "lr_kernel");
 }
 
+xcgpu_status xcgpu_lr_kernel_spin(xcgpu_plan* P, int func, int kind, const double* P0, uint32_t ntrial,
+                                  const double* const* D, double* const* F, int precision, double thr, int mem) {
+  if (!P) return XCGPU_ERR_INVALID;
+  Ctx* c = P->ctx;
+  if (kind == XCGPU_LR_SINGLET) return xcgpu_lr_kernel(P, func, P0, ntrial, D, F, precision, thr, mem);
+  if (kind != XCGPU_LR_TRIPLET && kind != XCGPU_LR_UNRESTRICTED)
+    return c->fail(XCGPU_ERR_INVALID, "lr_kernel_spin: unknown kind");
+  if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "lr_kernel_spin: unknown functional");
+  if (!P0 || (ntrial > 0 && (!D || !F))) return c->fail(XCGPU_ERR_INVALID, "lr_kernel_spin: bad arguments");
+  if (precision != XCGPU_PREC_FP64 && precision != XCGPU_PREC_MIXED)
+    return c->fail(XCGPU_ERR_INVALID, "lr_kernel_spin: unknown precision");
+  for (uint32_t t = 0; t < ntrial; ++t)
+    if (!D[t] || !F[t]) return c->fail(XCGPU_ERR_INVALID, "lr_kernel_spin: null trial or output matrix");
+  cudaSetDevice(c->device);
+  const bool gga = xc::is_gga(func), mixed = precision == XCGPU_PREC_MIXED;
+  const int ns = kind == XCGPU_LR_UNRESTRICTED ? 2 : 1;  // spins of P0, of each trial and of each F
+  const long n = P->grid->n;
+  const int nbf = P->basis->nbf;
+  const size_t nn = (size_t)nbf * nbf;
+  XC_TRY(ensure_work(P, ns, gga, mixed));
+  XC_TRY(P->n_rho.alloc(c, (size_t)ns * n * sizeof(double)));
+  XC_TRY(P->n_dfdrho.alloc(c, (size_t)ns * n * sizeof(double)));
+  if (gga) {
+    XC_TRY(P->n_grad.alloc(c, (size_t)ns * 3 * n * sizeof(double)));
+    XC_TRY(P->n_dfdgrad.alloc(c, (size_t)ns * 3 * n * sizeof(double)));
+  }
+  const double* P0d = P0;
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(upload(c, P->w_P, P0, ns * nn));
+    P0d = P->w_P.as<double>();
+  }
+  DevBuf dD, dS, dF;
+  XC_TRY(dS.alloc(c, ns * nn * sizeof(double)));
+  if (mem == XCGPU_MEM_HOST) {
+    XC_TRY(dD.alloc(c, ns * nn * sizeof(double)));
+    XC_TRY(dF.alloc(c, ns * nn * sizeof(double)));
+  }
+  int* counter = nullptr;
+  XC_TRY(c->aux(&counter));
+  int* err = counter + 2;
+  XC_TRY(c->cuda(cudaMemsetAsync(counter, 0, 4 * sizeof(int), c->stream), "memset aux"));
+  auto density = [&](const double* M, double* rho, double* grad) -> xcgpu_status {
+    if (!mixed) return stage_density(P, ns, M, rho, grad);
+    xcgpu_status st = mixed_split(c, M, ns, nbf, P->w_psplit.as<float>());
+    if (st) return st;
+    std::vector<MixedWork> work(1);
+    work[0] = MixedWork{&P->basis->dev, &P->dev, ns, P->w_psplit.as<float>(), rho, grad, nullptr, nullptr, nullptr, nullptr};
+    return mixed_density_batch(c, work, counter, err);
+  };
+  // ground state: per spin (unrestricted), or the restricted total density (triplet)
+  XC_TRY(density(P0d, P->w_rho.as<double>(), gga ? P->w_grad.as<double>() : nullptr));
+  for (uint32_t t = 0; t < ntrial; ++t) {
+    const double* Dd = D[t];
+    double* Fd = F[t];
+    if (mem == XCGPU_MEM_HOST) {
+      XC_TRY(c->cuda(cudaMemcpyAsync(dD.p, D[t], ns * nn * sizeof(double), cudaMemcpyHostToDevice, c->stream), "trial"));
+      Dd = dD.as<double>();
+      Fd = dF.as<double>();
+    }
+    // every spin's trial matrix symmetrised (KernelSigmavector.cpp:202-208)
+    for (int sp = 0; sp < ns; ++sp) XC_TRY(launch_symmetrise_half(c, Dd + sp * nn, dS.as<double>() + sp * nn, nbf));
+    XC_TRY(density(dS.as<double>(), P->n_rho.as<double>(), gga ? P->n_grad.as<double>() : nullptr));
+    XC_TRY(launch_lr_kernel_spin(c, func, kind, n, P->w_rho.as<double>(), gga ? P->w_grad.as<double>() : nullptr,
+                                 P->n_rho.as<double>(), gga ? P->n_grad.as<double>() : nullptr,
+                                 P->n_dfdrho.as<double>(), gga ? P->n_dfdgrad.as<double>() : nullptr));
+    XC_TRY(c->cuda(cudaMemsetAsync(Fd, 0, ns * nn * sizeof(double), c->stream), "memset F"));
+    const double* gv = gga ? P->n_dfdgrad.as<double>() : nullptr;
+    if (mixed) {
+      XC_TRY(launch_block_skip_flags(c, P->dev, ns, P->n_dfdrho.as<double>(), gv, thr, P->w_skip.as<unsigned char>()));
+      std::vector<MixedWork> work(1);
+      work[0] = MixedWork{&P->basis->dev, &P->dev, ns, nullptr, nullptr, nullptr, P->n_dfdrho.as<double>(), gv,
+                          P->w_skip.as<unsigned char>(), Fd};
+      XC_TRY(mixed_adder_batch(c, work, counter + 1, err));
+    } else {
+      XC_TRY(stage_adder(P, ns, P->n_dfdrho.as<double>(), gv, thr, Fd));
+    }
+    if (mem == XCGPU_MEM_HOST)
+      XC_TRY(c->cuda(cudaMemcpyAsync(F[t], Fd, ns * nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "F"));
+  }
+  int herr = 0;
+  XC_TRY(c->cuda(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error word"));
+  XC_TRY(c->cuda(cudaStreamSynchronize(c->stream), "lr_kernel_spin"));
+  return device_error(c, herr, "lr_kernel_spin");
+}
+
 xcgpu_status xcgpu_nadd_vxc_all(xcgpu_plan* const* plans, uint32_t n_sub, int func, int nspin, int precision,
                                 double thr, const double* const* P, double* const* V, double* E_nadd, int mem) {
   if (!plans || n_sub == 0 || !plans[0]) return XCGPU_ERR_INVALID;

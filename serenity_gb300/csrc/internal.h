@@ -240,6 +240,8 @@ xcgpu_status fp64_xc_gradient_chunk(Ctx* c, const DevBasis& B, const DevPlan& P,
                                     const double* g, const int* fatom, int natoms, double* G);
 xcgpu_status launch_lr_kernel(Ctx* c, int func, long n, const double* rho0, const double* grad0, const double* rho1,
                               const double* grad1, double* v1, double* g1);
+xcgpu_status launch_lr_kernel_spin(Ctx* c, int func, int kind, long n, const double* rho0, const double* grad0,
+                                   const double* rho1, const double* grad1, double* v1, double* g1);
 xcgpu_status launch_symmetrise_half(Ctx* c, const double* D, double* S, int n);
 xcgpu_status launch_scale_add(Ctx* c, long n, double a, const double* x, double* y);  // y += a x
 xcgpu_status launch_sum_partials(Ctx* c, const double* partials, int nparts, int ncomp, double* out /*device*/);

@@ -116,6 +116,99 @@ __global__ void __launch_bounds__(128) lr_kernel_kernel(int func, long n, int sk
     for (int k = 0; k < 3; ++k) g1[k * n + p] = out_g[k];
 }
 
+// Per point, the spin-resolved kernel contracted with a perturbation of both spin
+// densities: with x = (rho_a, rho_b, s_aa, s_ab, s_bb) the dual numbers carry x1 =
+// (rho1_a, rho1_b, 2 grad rho_a . grad rho1_a, grad rho_a . grad rho1_b + grad rho1_a .
+// grad rho_b, 2 grad rho_b . grad rho1_b), so one evaluation of the first derivatives gives
+//   v1_a = d(dF/drho_a)                 (KernelSigmavector.cpp:422-499, pp and pg terms)
+//   g1_a = d(2 F_saa grad rho_a + F_sab grad rho_b)   (the pg and gg terms), alike for b.
+// kind 2 (unrestricted): rho0 [2][n], grad0 [2][3][n], rho1 [2][n], grad1 [2][3][n], both
+//   spins out (v1 [2][n], g1 [2][3][n]).
+// kind 1 (triplet, KernelSigmavector<RESTRICTED> with the spin kernel, :367-391): rho0,
+//   grad0 the restricted total density (each spin half of it), the perturbation (+rho1,
+//   -rho1); the alpha outputs (f_aa - f_ab contracted with rho1) are written.
+// The block skip is the unrestricted functional data's: every spin's |rho| sums below
+// n 1e-12 over the block (XCFun.cpp:136-140).
+__global__ void __launch_bounds__(128) lr_kernel_spin_kernel(int func, int kind, long n, int skip_block,
+                                                             const double* __restrict__ rho0,
+                                                             const double* __restrict__ grad0,
+                                                             const double* __restrict__ rho1,
+                                                             const double* __restrict__ grad1,
+                                                             double* __restrict__ v1, double* __restrict__ g1) {
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool gga = xc::is_gga(func), trip = kind == 1;
+  __shared__ double red[2][128];
+  double ra = 0.0, rb = 0.0;
+  if (p < n) {
+    ra = trip ? 0.5 * rho0[p] : rho0[p];
+    rb = trip ? ra : rho0[n + p];
+  }
+  red[0][threadIdx.x] = fabs(ra);
+  red[1][threadIdx.x] = fabs(rb);
+  __syncthreads();
+  for (int s = 64; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + s];
+      red[1][threadIdx.x] += red[1][threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  const long first = (long)blockIdx.x * blockDim.x;
+  const long cnt = min((long)skip_block, n - first);
+  const bool skip = red[0][0] < cnt * 1e-12 && red[1][0] < cnt * 1e-12;
+  if (p >= n) return;
+  double ov[2] = {0.0, 0.0}, og[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+  if (!skip) {
+    double a0[3] = {0, 0, 0}, b0[3] = {0, 0, 0}, a1[3] = {0, 0, 0}, b1[3] = {0, 0, 0};
+    double ra1, rb1;
+    if (trip) {
+      ra1 = rho1[p];
+      rb1 = -ra1;
+    } else {
+      ra1 = rho1[p];
+      rb1 = rho1[n + p];
+    }
+    if (gga)
+      for (int k = 0; k < 3; ++k) {
+        if (trip) {
+          a0[k] = b0[k] = 0.5 * grad0[k * n + p];
+          a1[k] = grad1[k * n + p];
+          b1[k] = -a1[k];
+        } else {
+          a0[k] = grad0[k * n + p];
+          b0[k] = grad0[(3 + k) * n + p];
+          a1[k] = grad1[k * n + p];
+          b1[k] = grad1[(3 + k) * n + p];
+        }
+      }
+    double saa = 0, sab = 0, sbb = 0, daa = 0, dab = 0, dbb = 0;
+    for (int k = 0; k < 3; ++k) {
+      saa += a0[k] * a0[k];
+      sab += a0[k] * b0[k];
+      sbb += b0[k] * b0[k];
+      daa += 2.0 * a0[k] * a1[k];
+      dab += a0[k] * b1[k] + a1[k] * b0[k];
+      dbb += 2.0 * b0[k] * b1[k];
+    }
+    xc::Dual e, va, vb, vaa, vab, vbb;
+    xc::eval_unrestricted<xc::Dual>(func, xc::Dual(ra, ra1), xc::Dual(rb, rb1), xc::Dual(saa, daa),
+                                    xc::Dual(sab, dab), xc::Dual(sbb, dbb), e, va, vb, vaa, vab, vbb);
+    ov[0] = va.d;
+    ov[1] = vb.d;
+    if (gga)
+      for (int k = 0; k < 3; ++k) {
+        og[0][k] = 2.0 * vaa.d * a0[k] + 2.0 * vaa.v * a1[k] + vab.d * b0[k] + vab.v * b1[k];
+        og[1][k] = 2.0 * vbb.d * b0[k] + 2.0 * vbb.v * b1[k] + vab.d * a0[k] + vab.v * a1[k];
+      }
+  }
+  const int nout = trip ? 1 : 2;
+  for (int s = 0; s < nout; ++s) {
+    v1[(long)s * n + p] = ov[s];
+    if (gga)
+      for (int k = 0; k < 3; ++k) g1[((long)s * 3 + k) * n + p] = og[s][k];
+  }
+}
+
 // D -> (D + D^T) / 2, column-major n x n
 __global__ void symmetrise_half_kernel(const double* __restrict__ D, double* __restrict__ S, int n) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -131,6 +224,15 @@ xcgpu_status launch_lr_kernel(Ctx* c, int func, long n, const double* rho0, cons
   lr_kernel_kernel<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(func, n, kSkipBlock, rho0, grad0, rho1, grad1,
                                                                        v1, g1);
   return c->check_launch("lr_kernel_kernel");
+}
+
+xcgpu_status launch_lr_kernel_spin(Ctx* c, int func, int kind, long n, const double* rho0, const double* grad0,
+                                   const double* rho1, const double* grad1, double* v1, double* g1) {
+  if (n == 0) return XCGPU_OK;
+  KernelTimer kt(c, kFunctional);
+  lr_kernel_spin_kernel<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(func, kind, n, kSkipBlock, rho0, grad0,
+                                                                            rho1, grad1, v1, g1);
+  return c->check_launch("lr_kernel_spin_kernel");
 }
 
 xcgpu_status launch_symmetrise_half(Ctx* c, const double* D, double* S, int n) {

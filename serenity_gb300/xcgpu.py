@@ -106,6 +106,8 @@ def library(build_if_needed=True):
     L.xcgpu_xc_gradient.argtypes = [vp, S, S, vp, vp, S, vp, S]
     L.xcgpu_lr_kernel.argtypes = [vp, S, vp, ctypes.c_uint32, ctypes.POINTER(vp), ctypes.POINTER(vp), S,
                                   ctypes.c_double, S]
+    L.xcgpu_lr_kernel_spin.argtypes = [vp, S, S, vp, ctypes.c_uint32, ctypes.POINTER(vp), ctypes.POINTER(vp), S,
+                                       ctypes.c_double, S]
     L.xcgpu_nadd_vxc_all.argtypes = [ctypes.POINTER(vp), ctypes.c_uint32, S, S, S, ctypes.c_double,
                                      ctypes.POINTER(vp), ctypes.POINTER(vp), dp, S]
     L.xcgpu_check_async.argtypes = [vp]
@@ -115,7 +117,7 @@ def library(build_if_needed=True):
     L.xcgpu_graph_destroy.argtypes = [vp]
     L.xcgpu_set_timing.argtypes = [vp, S]
     L.xcgpu_get_timing.argtypes = [vp, vp, vp]
-    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_nadd_vxc_all", "xcgpu_xc_gradient", "xcgpu_lr_kernel", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
+    for name in ["xcgpu_vxc_batch", "xcgpu_nadd_vxc", "xcgpu_nadd_vxc_all", "xcgpu_xc_gradient", "xcgpu_lr_kernel", "xcgpu_lr_kernel_spin", "xcgpu_check_async", "xcgpu_graph_begin", "xcgpu_graph_end",
                  "xcgpu_graph_launch", "xcgpu_set_timing", "xcgpu_get_timing"]:
         getattr(L, name).restype = S
     for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
@@ -407,20 +409,30 @@ class Plan:
                                             ctypes.byref(exc), ctypes.byref(nel), MEM_HOST))
         return V.transpose(0, 2, 1), exc.value, nel.value
 
-    def lr_kernel(self, func, P0, trials, precision=PREC_FP64, block_ave_threshold=1e-11):
-        """XC kernel part of restricted (singlet) linear-response sigma vectors: for each
-        trial matrix D (host [nbf, nbf]) the matrix F (KernelSigmavector<RESTRICTED>::calcF).
-        P0: ground-state total density matrix."""
+    def lr_kernel(self, func, P0, trials, precision=PREC_FP64, block_ave_threshold=1e-11, kind="singlet"):
+        """XC kernel part of linear-response sigma vectors (KernelSigmavector::calcF): for
+        each trial matrix the matrix F.  kind "singlet" or "triplet": P0 the restricted
+        ground-state total density, trials and results [nbf, nbf]; "unrestricted": P0 and
+        each trial [2, nbf, nbf] (alpha, beta), results [2, nbf, nbf]."""
         fid = FUNC[func] if isinstance(func, str) else int(func)
-        P0c = np.ascontiguousarray(np.asarray(P0, dtype=np.float64).T)
-        Ds = [np.ascontiguousarray(np.asarray(D, dtype=np.float64).T) for D in trials]
-        Fs = [np.zeros((self.nbf, self.nbf)) for _ in trials]
+        ns = 2 if kind == "unrestricted" else 1
+        colmajor = lambda M: np.ascontiguousarray(np.stack(  # noqa: E731
+            [m.T for m in np.asarray(M, dtype=np.float64).reshape(ns, self.nbf, self.nbf)]))
+        P0c = colmajor(P0)
+        Ds = [colmajor(D) for D in trials]
+        Fs = [np.zeros((ns, self.nbf, self.nbf)) for _ in trials]
         k = len(trials)
         dp = (vp * max(1, k))(*[x.ctypes.data for x in Ds])
         fp = (vp * max(1, k))(*[x.ctypes.data for x in Fs])
-        self.ctx.check(self.ctx.L.xcgpu_lr_kernel(self.h, fid, _ptr(P0c), k, dp, fp, precision, block_ave_threshold,
-                                                  MEM_HOST))
-        return [F.T for F in Fs]
+        if kind == "singlet":
+            self.ctx.check(self.ctx.L.xcgpu_lr_kernel(self.h, fid, _ptr(P0c), k, dp, fp, precision,
+                                                      block_ave_threshold, MEM_HOST))
+        else:
+            code = {"triplet": 1, "unrestricted": 2}[kind]
+            self.ctx.check(self.ctx.L.xcgpu_lr_kernel_spin(self.h, fid, code, _ptr(P0c), k, dp, fp, precision,
+                                                           block_ave_threshold, MEM_HOST))
+        out = [np.swapaxes(F, 1, 2) for F in Fs]
+        return out if ns == 2 else [F[0] for F in out]
 
     def xc_gradient(self, func, P, shell_atom, natoms):
         """XC part of the nuclear gradient (FuncPotential<M>::getGeomGradients), FP64:

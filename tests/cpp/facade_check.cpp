@@ -16,6 +16,8 @@ template class Serenity::DensityMatrixDensityOnGridController<RESTRICTED>;
 template class Serenity::DensityMatrixDensityOnGridController<UNRESTRICTED>;
 template class Serenity::FunctionalLibrary<RESTRICTED>;
 template class Serenity::FunctionalLibrary<UNRESTRICTED>;
+template class Serenity::KernelSigmavector<RESTRICTED>;
+template class Serenity::KernelSigmavector<UNRESTRICTED>;
 template class Serenity::NAddFuncPotential<RESTRICTED>;
 template class Serenity::NAddFuncPotential<UNRESTRICTED>;
 template class Serenity::FuncPotential<RESTRICTED>;

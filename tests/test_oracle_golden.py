@@ -161,3 +161,38 @@ def test_lr_kernel_is_the_derivative_of_the_xc_matrix(func):
     Vm = B.vxc(pts, wts, func, P0 - h * D, thr=0.0, ave_thr=0.0)[0][0]
     fd = (Vp - Vm) / (2 * h)
     assert np.abs(F - fd).max() <= 1e-6 * max(1.0, np.abs(fd).max()), np.abs(F - fd).max()
+
+
+@pytest.mark.parametrize("func", ["LDA", "PBE", "BLYP", "BP86"])
+@pytest.mark.parametrize("kind", ["unrestricted", "triplet"])
+def test_spin_lr_kernel_is_the_derivative_of_the_xc_matrix(func, kind):
+    """The spin-resolved kernel contraction (KernelSigmavector<UNRESTRICTED>::contractBlock,
+    and the triplet's f_aa - f_ab of KernelSigmavector<RESTRICTED>) is the derivative of the
+    unrestricted XC matrix along the trial densities: F_s(D) = d/de Vxc_s[P_a + e D_a,
+    P_b + e D_b]; the triplet's perturbation is (+D, -D) about (P0/2, P0/2), alpha part."""
+    from serenity_gb300 import workload as wl
+    sym, xyz = wl.water_cluster(1, 5, jitter=0.1)
+    rng = np.random.default_rng(11)
+    pts, wts = po.becke_grid([8, 1, 1], xyz, n_rad=30, n_ang=110)
+    h = 1e-5
+    if kind == "unrestricted":
+        w = wl.Workload(sym, xyz, "DEF2-SVP", func, (5, 4), 30, 110, 6)
+        P0 = np.asarray(w.density())
+        D = rng.standard_normal(P0.shape) * 0.05
+        D = D + np.swapaxes(D, 1, 2)
+        B = po.Basis(w.shells)
+        F = po.lr_fock_spin(B, pts, wts, func, P0, D, kind, thr=0.0, ave_thr=0.0)
+        Vp = B.vxc(pts, wts, func, P0 + h * D, thr=0.0, ave_thr=0.0)[0]
+        Vm = B.vxc(pts, wts, func, P0 - h * D, thr=0.0, ave_thr=0.0)[0]
+    else:
+        w = wl.Workload(sym, xyz, "DEF2-SVP", func, 5, 30, 110, 6)
+        P0 = np.asarray(w.density())
+        D = rng.standard_normal(P0.shape) * 0.05
+        D = D + D.T
+        B = po.Basis(w.shells)
+        F = po.lr_fock_spin(B, pts, wts, func, P0, D, kind, thr=0.0, ave_thr=0.0)
+        Vp = B.vxc(pts, wts, func, np.stack([0.5 * P0 + h * D, 0.5 * P0 - h * D]), thr=0.0, ave_thr=0.0)[0][0]
+        Vm = B.vxc(pts, wts, func, np.stack([0.5 * P0 - h * D, 0.5 * P0 + h * D]), thr=0.0, ave_thr=0.0)[0][0]
+    fd = (Vp - Vm) / (2 * h)
+    assert np.abs(fd).max() > 1e-2  # a perturbation that moves the potential
+    assert np.abs(F - fd).max() <= 1e-8 * max(1.0, np.abs(fd).max()), np.abs(F - fd).max()
