@@ -294,7 +294,8 @@ __device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, f
   }
 }
 
-template <int DERIV, class Emit>
+// dispatch on l <= MAXL at run time (the callers select MAXL from the basis)
+template <int DERIV, int MAXL, class Emit>
 __device__ __forceinline__ void shell_functions_px_l(int l, F2 x, F2 y, F2 z, float Rv, float dR, bool pure,
                                                      Emit&& emit) {
   switch (l) {
@@ -302,10 +303,16 @@ __device__ __forceinline__ void shell_functions_px_l(int l, F2 x, F2 y, F2 z, fl
     case 1: shell_functions_px<1, DERIV>(x, y, z, Rv, dR, pure, emit); break;
     case 2: shell_functions_px<2, DERIV>(x, y, z, Rv, dR, pure, emit); break;
     case 3: shell_functions_px<3, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 4: shell_functions_px<4, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 5: shell_functions_px<5, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 6: shell_functions_px<6, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    default: break;
+    default:
+      if constexpr (MAXL >= 4) {
+        switch (l) {
+          case 4: shell_functions_px<4, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+          case 5: shell_functions_px<5, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+          case 6: shell_functions_px<6, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+          default: break;
+        }
+      }
+      break;
   }
 }
 

@@ -82,6 +82,15 @@ __device__ __forceinline__ void fzeta(R z, R& f, R& df) {
   df = R(4.0 / 3.0) * (a - b) * k;
 }
 
+// zeta == 0 exactly: the spin-polarised formulas then reduce to the unpolarised ones.
+// A number type that also carries derivatives (the response kernel's dual numbers)
+// specialises this to require a zero derivative as well: along a spin-flip
+// perturbation zeta is 0 but its derivative is not, and the zeta terms matter.
+template <class R>
+__device__ __forceinline__ bool zeta_is_zero(R z) {
+  return z == R(0);
+}
+
 // |zeta| is capped at 1 - 1e-12; where the cap applies, zeta no longer depends on
 // the spin densities, so the zeta-derivative terms vanish (scale = 0).
 template <class R>
@@ -108,7 +117,7 @@ __device__ __forceinline__ void vwn5(R na, R nb, R& e, R& va, R& vb) {
   vwn_g(x, 0.0310907, -0.10498, 3.72744, 12.9352, eP, dP);
   R zs;
   const R z = clampz((na - nb) / n, zs);
-  if (z == R(0)) {
+  if (zeta_is_zero(z)) {
     const R deps_drs = dP / (R(2) * x);
     e += n * eP;
     const R v = eP - rs / R(3) * deps_drs;
@@ -149,7 +158,7 @@ __device__ __forceinline__ void pw92_eps(R rs, R z, R& eps, R& deps_drs, R& deps
   const R srs = sqrt_<R>(rs);
   R e0, d0;
   pw92_g(rs, srs, 0.031091, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294, e0, d0);
-  if (z == R(0)) {
+  if (zeta_is_zero(z)) {
     eps = e0;
     deps_drs = d0;
     deps_dz = R(0);
@@ -214,7 +223,7 @@ __device__ __forceinline__ void pbec(R na, R nb, R saa, R sab, R sbb, R& e, R& v
   R eps, deps_drs, deps_dz;
   pw92_eps(rs, z, eps, deps_drs, deps_dz);
   R phi = R(1), dphi = R(0);
-  if (z != R(0)) {
+  if (!zeta_is_zero(z)) {
     const R a = cbrt_<R>(R(1) + z), b = cbrt_<R>(R(1) - z);
     phi = R(0.5) * (a * a + b * b);
     dphi = R(1.0 / 3.0) * (R(1) / a - R(1) / b);
@@ -251,6 +260,60 @@ __device__ __forceinline__ void pbec(R na, R nb, R saa, R sab, R sbb, R& e, R& v
   vsaa += vs;
   vsab += R(2) * vs;
   vsbb += vs;
+}
+
+// ---- PBE exchange + correlation of an unpolarised density in one pass: the same
+// expressions as pbex_unpol + pbec at zeta = 0 (phi = 1), with n^(1/3) taken once and
+// the divisions shared (FP64 division and the cube root dominate the functional's cost
+// on a GPU whose FP64 rate is a small fraction of its FP32 rate) ----
+template <class R>
+__device__ __forceinline__ void pbe_unpol(R n, R sigma, R& e, R& vn, R& vs) {
+  constexpr double A0 = 0.031091, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382, b4 = 0.49294;
+  const R n13 = cbrt_<R>(n);
+  const R r13 = R(1) / n13, rn = r13 * r13 * r13;
+  // exchange: e = -Cx n^(4/3) Fx(s^2), s^2 = sigma / (4 (3 pi^2)^(2/3) n^(8/3))
+  const R n43 = n * n13;
+  const R k8 = R(1.0 / (4.0 * 9.570780000627305)) * (rn * rn * r13 * r13);  // 1 / (4 (3 pi^2)^(2/3) n^(8/3))
+  const R s2 = sigma * k8;
+  const R rden = R(1) / (R(1) + R(kMu / kKappa) * s2);
+  const R Fx = R(1 + kKappa) - R(kKappa) * rden;
+  const R dFx = R(kMu) * rden * rden;
+  const R Cx = R(0.7385587663820224);  // (3/4)(3/pi)^(1/3)
+  e = -Cx * n43 * Fx;
+  vn = -Cx * (R(4.0 / 3.0) * n13 * Fx - R(8.0 / 3.0) * n13 * dFx * s2);
+  vs = -Cx * n43 * dFx * k8;
+  // correlation: PW92 eps(rs) and the PBE gradient term H(t^2)
+  const R rs = R(0.6203504908994001) * r13;  // (3 / (4 pi n))^(1/3)
+  const R srs = sqrt_<R>(rs);
+  const R Q1 = R(2 * A0) * (R(b1) * srs + R(b2) * rs + R(b3) * rs * srs + R(b4) * rs * rs);
+  const R dQ1 = R(2 * A0) * (R(0.5 * b1) * srs * (n13 * R(1.0 / 0.6203504908994001)) + R(b2) + R(1.5 * b3) * srs +
+                              R(2 * b4) * rs);
+  const R rq = R(1) / (Q1 * (Q1 + R(1)));  // 1 / (Q1^2 + Q1)
+  const R L = log_<R>(R(1) + rq * (Q1 + R(1)));
+  const R eps = R(-2 * A0) * (R(1) + R(a1) * rs) * L;
+  const R deps_drs = R(-2 * A0 * a1) * L + R(2 * A0) * (R(1) + R(a1) * rs) * dQ1 * rq;
+  const R dt2_dsig = R(kPi / 16.0 / 3.0936677262801355) * r13 * rn * rn;  // pi / (16 kF n^2)
+  const R t2 = sigma * dt2_dsig;
+  const R E = exp_<R>(-eps * R(1.0 / kGamma));
+  const R rE = R(1) / (E - R(1));
+  const R A = R(kBeta / kGamma) * rE;
+  const R y = A * t2;
+  const R N = R(1) + y;
+  const R rD = R(1) / (R(1) + y + y * y);
+  const R Q = t2 * N * rD;
+  const R arg = R(1) + R(kBeta / kGamma) * Q;
+  const R rarg = R(1) / arg;
+  const R H = R(kGamma) * log_<R>(arg);
+  const R pref = R(kBeta) * rarg;
+  const R y2y = y * (R(2) + y) * rD * rD;
+  const R dH_dt2 = pref * (N * rD - y * y2y);
+  const R dH_dA = -pref * t2 * t2 * y2y;
+  const R dA_deps = A * A * E * R(1.0 / kBeta);
+  const R deps_dn = R(-1.0 / 3.0) * rs * rn * deps_drs;
+  const R dH_dn = dH_dt2 * (R(-7.0 / 3.0) * t2 * rn) + dH_dA * dA_deps * deps_dn;
+  e += n * (eps + H);
+  vn += eps + H + n * (deps_dn + dH_dn);
+  vs += n * dH_dt2 * dt2_dsig;
 }
 
 // ---- B88 gradient correction per spin (without the Slater part) ----
@@ -347,7 +410,7 @@ __device__ __forceinline__ void pz81(R na, R nb, R& e, R& va, R& vb) {
   const R z = clampz((na - nb) / n, zs);
   R eps, dr, dz = R(0);
   pz81_g(rs, -0.1423, 1.0529, 0.3334, 0.0311, -0.048, 0.0020, -0.0116, eps, dr);
-  if (z != R(0)) {
+  if (!zeta_is_zero(z)) {
     R eP, dP, f, df;
     pz81_g(rs, -0.0843, 1.3981, 0.2611, 0.01555, -0.0269, 0.0007, -0.0048, eP, dP);
     fzeta(z, f, df);
@@ -388,7 +451,7 @@ __device__ __forceinline__ void p86corr(R na, R nb, R saa, R sab, R sbb, R& e, R
   R zs;
   const R z = clampz((na - nb) / n, zs);
   R dinv = R(1), dlog = R(0);  // 1/d and d'(z)/d
-  if (z != R(0)) {
+  if (!zeta_is_zero(z)) {
     const R up = R(0.5) * (R(1) + z), dn = R(0.5) * (R(1) - z);
     const R u23 = cbrt_<R>(up * up), d23 = cbrt_<R>(dn * dn);
     const R A = up * u23 + dn * d23;
@@ -439,6 +502,8 @@ __device__ __forceinline__ void eval_restricted(int func, R n, R sigma, R& e, R&
       break;
     }
     case XCGPU_FUNC_PBE:
+      pbe_unpol(n, sigma, e, vn, vs);
+      break;
     case XCGPU_FUNC_PBEX:
     case XCGPU_FUNC_PBEC: {
       if (func != XCGPU_FUNC_PBEC && n > R(kTiny)) {

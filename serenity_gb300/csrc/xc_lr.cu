@@ -44,6 +44,7 @@ __device__ __forceinline__ bool operator>=(Dual a, Dual b) { return a.v >= b.v; 
 __device__ __forceinline__ bool operator==(Dual a, Dual b) { return a.v == b.v; }
 __device__ __forceinline__ bool operator!=(Dual a, Dual b) { return a.v != b.v; }
 
+template <> __device__ __forceinline__ bool zeta_is_zero<Dual>(Dual z) { return z.v == 0.0 && z.d == 0.0; }
 template <> __device__ __forceinline__ Dual cbrt_<Dual>(Dual x) {
   const double c = cbrt(x.v);
   return Dual(c, x.d == 0.0 ? 0.0 : x.d * c / (3.0 * x.v));
