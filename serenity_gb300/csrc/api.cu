@@ -430,7 +430,7 @@ xcgpu_status xcgpu_plan_create(xcgpu_ctx* c, xcgpu_grid* g, xcgpu_basis* B, uint
     P->flops += 4.0 * npts * (double)nact * nact;
     const int nt = (nact + 63) / 64;
     for (int i = 0; i < nt; ++i)
-      for (int j = i; j < nt; ++j) {
+      for (int j = 0; j < nt; ++j) {
         P->work.push_back(b);
         P->work.push_back(i);
         P->work.push_back(j);
@@ -756,6 +756,42 @@ static xcgpu_status run_builds(Ctx* c, std::vector<BuildReq>& reqs, int precisio
       const int nb = reqs[i].plan->nblocks;
       if (nb) XC_TRY(launch_sum_partials(c, bw[i].partials, nb, 2, reqs[i].exc_nel));
       else XC_TRY(c->cuda(cudaMemsetAsync(reqs[i].exc_nel, 0, 2 * sizeof(double), c->stream), "memset sums"));
+    }
+    return XCGPU_OK;
+  }
+  bool chunked = !mixed;
+  for (const auto& r : reqs) chunked = chunked && r.plan->max_block == kSkipBlock;
+  if (chunked) {
+    // FP64 build chunk by chunk: the basis slabs of a chunk of blocks serve its density,
+    // and after the functional at the chunk's points, its Vxc (the basis is evaluated
+    // once per build).  Per point and block the same arithmetic as the three separate
+    // phases (FuncPotential.cpp:74-110): E_xc and N_el from the same 128-point partial
+    // sums in the same order; only the order of the FP64 atomic adds into V differs.
+    for (size_t i = 0; i < reqs.size(); ++i) {
+      const BuildReq& r = reqs[i];
+      const BuildWork& w = bw[i];
+      xcgpu_plan* P = r.plan;
+      const long n = P->grid->n;
+      const int nbf = P->basis->nbf;
+      XC_TRY(c->cuda(cudaMemsetAsync(r.V, 0, (size_t)r.nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
+      XC_TRY(prep_chunks(P));
+      double* scr = nullptr;
+      XC_TRY(fp64_scratch(P, &scr));
+      for (size_t k = 0; k + 1 < P->chunk_bounds.size(); ++k) {
+        const int b0 = P->chunk_bounds[k], b1 = P->chunk_bounds[k + 1];
+        const long* so = P->w_slab.as<long>() + b0;
+        const long p0 = (long)b0 * P->max_block, p1 = std::min(n, (long)b1 * P->max_block);
+        XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, scr, 1));
+        XC_TRY(fp64_density_chunk(c, P->dev, b0, b1, so, scr, r.nspin, r.P, w.rho, w.grad));
+        XC_TRY(launch_functional_range(c, r.func, r.nspin, n, kSkipBlock, p0, p1, w.rho, w.grad, w.epuv, w.dfdrho,
+                                       w.dfdgrad, P->dev.w, w.partials, w.fskip));
+        XC_TRY(launch_block_skip_flags_range(c, P->dev, r.nspin, w.dfdrho, w.dfdgrad, r.thr, w.skip, b0, b1));
+        XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, so, scr,
+                                r.nspin, w.dfdrho, w.dfdgrad, w.skip, r.V));
+      }
+      const int nparts = (int)((n + 127) / 128);
+      if (nparts) XC_TRY(launch_sum_partials(c, w.partials, nparts, 2, r.exc_nel));
+      else XC_TRY(c->cuda(cudaMemsetAsync(r.exc_nel, 0, 2 * sizeof(double), c->stream), "memset sums"));
     }
     return XCGPU_OK;
   }

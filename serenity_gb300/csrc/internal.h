@@ -196,7 +196,7 @@ struct xcgpu_plan {
   int max_active = 0;
   double flops = 0.0;
   xcgpu::DevBuf d_sh_off, d_sh_list, d_fn_off, d_fn_list, d_rec;
-  // adder tile work list (block, tile_i, tile_j) for 64-wide tiles, upper triangle
+  // adder tile work list (block, tile_i, tile_j) for 64-wide tiles, all pairs
   std::vector<int> work;  // 3 ints per item, sorted by block
   std::vector<long> work_off;  // [nblocks+1]
   xcgpu::DevBuf d_work;
@@ -225,6 +225,11 @@ xcgpu_status fp64_eval_chunk(Ctx* c, const DevBasis& B, const DevPlan& P, int b0
                              double* scratch, int deriv);
 xcgpu_status fp64_density_chunk(Ctx* c, const DevPlan& P, int b0, int b1, const long* slab_off, const double* scratch,
                                 int nspin, const double* Pm, double* rho, double* grad);
+xcgpu_status launch_functional_range(Ctx* c, int func, int nspin, long n, int skip_block, long p0, long p1,
+                                     const double* rho, const double* grad, double* epuv, double* dfdrho,
+                                     double* dfdgrad, const double* w, double* partials, unsigned char* skipbuf);
+xcgpu_status launch_block_skip_flags_range(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
+                                           double thr, unsigned char* skip, int b0, int b1);
 xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_block, const double* rho,
                                const double* grad, double* epuv, double* dfdrho, double* dfdgrad, const double* w,
                                double* partials /*2*nparts or null*/, int* nparts,

@@ -400,8 +400,9 @@ xcgpu_status fp64_xc_gradient_chunk(Ctx* c, const DevBasis& B, const DevPlan& P,
 // whose sum |rho_s| < n * 1e-12 for every spin gives zero outputs.
 __global__ void __launch_bounds__(128) skip_flags_kernel(long n, int skip_block, int nspin,
                                                          const double* __restrict__ rho,
-                                                         unsigned char* __restrict__ skip) {
-  const long first = (long)blockIdx.x * skip_block;
+                                                         unsigned char* __restrict__ skip, long sk0) {
+  const long sb = sk0 + blockIdx.x;  // skip block of this CTA
+  const long first = sb * skip_block;
   const int m = (int)min((long)skip_block, n - first);
   __shared__ double red[128];
   bool sk = true;
@@ -417,19 +418,22 @@ __global__ void __launch_bounds__(128) skip_flags_kernel(long n, int skip_block,
     sk = sk && (red[0] < m * 1e-12);
     __syncthreads();
   }
-  if (threadIdx.x == 0) skip[blockIdx.x] = sk ? 1 : 0;
+  if (threadIdx.x == 0) skip[sb] = sk ? 1 : 0;
 }
 
+// points [p0, p1) of n (p0 a multiple of 128); partials[k] and partials[nparts + k] get
+// the E_xc and N_el sums of the 128 points from 128 k
 __global__ void __launch_bounds__(128) functional_kernel(int func, int nspin, long n, int skip_block,
                                                          const unsigned char* __restrict__ skip,
                                                          const double* __restrict__ rho,
                                                          const double* __restrict__ grad, double* __restrict__ epuv,
                                                          double* __restrict__ dfdrho, double* __restrict__ dfdgrad,
-                                                         const double* __restrict__ w, double* __restrict__ partials) {
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+                                                         const double* __restrict__ w, double* __restrict__ partials,
+                                                         long p0, long p1, int nparts) {
+  const long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool gga = xc::is_gga(func);
   double e = 0.0, rtot = 0.0;
-  if (p < n) {
+  if (p < p1) {
     const bool sk = skip[p / skip_block] != 0;
     if (nspin == 1) {
       const double r = rho[p];
@@ -477,7 +481,7 @@ __global__ void __launch_bounds__(128) functional_kernel(int func, int nspin, lo
   }
   if (partials) {
     __shared__ double red[2][128];
-    const double wp = (p < n) ? w[p] : 0.0;
+    const double wp = (p < p1) ? w[p] : 0.0;
     red[0][threadIdx.x] = wp * e;
     red[1][threadIdx.x] = wp * rtot;
     __syncthreads();
@@ -489,19 +493,20 @@ __global__ void __launch_bounds__(128) functional_kernel(int func, int nspin, lo
       __syncthreads();
     }
     if (threadIdx.x == 0) {
-      partials[blockIdx.x] = red[0][0];
-      partials[gridDim.x + blockIdx.x] = red[1][0];
+      const long k = p0 / 128 + blockIdx.x;
+      partials[k] = red[0][0];
+      partials[nparts + k] = red[1][0];
     }
   }
 }
 
-xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_block, const double* rho,
-                               const double* grad, double* epuv, double* dfdrho, double* dfdgrad, const double* w,
-                               double* partials, int* nparts, unsigned char* skipbuf) {
-  if (n == 0) {
-    if (nparts) *nparts = 0;
-    return XCGPU_OK;
-  }
+// the functional at points [p0, p1) of an n-point grid (arrays strided by n); p0 a
+// multiple of 128 and, with the block skip, of skip_block.  partials: 2 x nparts sums of
+// 128-point groups (nparts = ceil(n / 128)), the groups of the range written.
+xcgpu_status launch_functional_range(Ctx* c, int func, int nspin, long n, int skip_block, long p0, long p1,
+                                     const double* rho, const double* grad, double* epuv, double* dfdrho,
+                                     double* dfdgrad, const double* w, double* partials, unsigned char* skipbuf) {
+  if (p1 <= p0) return XCGPU_OK;
   const int sb = skip_block > 0 ? skip_block : 1 << 30;
   const long nsk = (n + sb - 1) / sb;
   xcgpu_status st = XCGPU_OK;
@@ -512,16 +517,24 @@ xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_blo
   }
   KernelTimer kt(c, kFunctional);
   if (skip_block > 0) {
-    skip_flags_kernel<<<(unsigned)nsk, 128, 0, c->stream>>>(n, sb, nspin, rho, skip);
+    const long sk0 = p0 / sb, sk1 = (p1 + sb - 1) / sb;
+    skip_flags_kernel<<<(unsigned)(sk1 - sk0), 128, 0, c->stream>>>(n, sb, nspin, rho, skip, sk0);
     if ((st = c->check_launch("skip_flags_kernel"))) return st;
   } else {
     if ((st = c->cuda(cudaMemsetAsync(skip, 0, nsk, c->stream), "memset skip"))) return st;
   }
-  const unsigned grid = (unsigned)((n + 127) / 128);
-  functional_kernel<<<grid, 128, 0, c->stream>>>(func, nspin, n, sb, skip, rho, grad, epuv,
-                                                 dfdrho, dfdgrad, w, partials);
-  if (nparts) *nparts = (int)grid;
+  const unsigned grid = (unsigned)((p1 - p0 + 127) / 128);
+  functional_kernel<<<grid, 128, 0, c->stream>>>(func, nspin, n, sb, skip, rho, grad, epuv, dfdrho, dfdgrad, w,
+                                                 partials, p0, p1, (int)((n + 127) / 128));
   return c->check_launch("functional_kernel");
+}
+
+xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_block, const double* rho,
+                               const double* grad, double* epuv, double* dfdrho, double* dfdgrad, const double* w,
+                               double* partials, int* nparts, unsigned char* skipbuf) {
+  if (nparts) *nparts = (int)((n + 127) / 128);
+  return launch_functional_range(c, func, nspin, n, skip_block, 0, n, rho, grad, epuv, dfdrho, dfdgrad, w, partials,
+                                 skipbuf);
 }
 
 // ------------------------------------------------------------------------------------
@@ -529,8 +542,8 @@ xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_blo
 // sum_p (|w v| + |w g_x| + |w g_y| + |w g_z|) / n < threshold.
 __global__ void __launch_bounds__(128) adder_skip_kernel(DevPlan P, int nspin, const double* __restrict__ v,
                                                          const double* __restrict__ g, double thr,
-                                                         unsigned char* __restrict__ skip) {
-  const int b = blockIdx.x;
+                                                         unsigned char* __restrict__ skip, int b0) {
+  const int b = b0 + blockIdx.x;
   const long first = (long)b * P.max_block;
   const int n = (int)min((long)P.max_block, P.npoints - first);
   __shared__ double red[128];
@@ -554,19 +567,27 @@ __global__ void __launch_bounds__(128) adder_skip_kernel(DevPlan P, int nspin, c
   }
 }
 
-xcgpu_status launch_block_skip_flags(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
-                                     double thr, unsigned char* skip) {
-  if (P.nblocks == 0) return XCGPU_OK;
+xcgpu_status launch_block_skip_flags_range(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
+                                           double thr, unsigned char* skip, int b0, int b1) {
+  if (b1 <= b0) return XCGPU_OK;
   KernelTimer kt(c, kOther);
-  adder_skip_kernel<<<P.nblocks, 128, 0, c->stream>>>(P, nspin, v, g, thr, skip);
+  adder_skip_kernel<<<b1 - b0, 128, 0, c->stream>>>(P, nspin, v, g, thr, skip, b0);
   return c->check_launch("adder_skip_kernel");
 }
 
+xcgpu_status launch_block_skip_flags(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
+                                     double thr, unsigned char* skip) {
+  return launch_block_skip_flags_range(c, P, nspin, v, g, thr, skip, 0, P.nblocks);
+}
+
 // ------------------------------------------------------------------------------------
-// F_b = phi^T G + G^T phi with G = w (v/2 phi + g . grad phi)
-// (ScalarOperatorToMatrixAdder.cpp:178-303; the LDA form phi^T diag(w v) phi is the
-// same with g = 0).  One CTA per (block, 64-row tile i, 64-column tile j), i <= j;
-// 256 threads with 4x4 outputs each; results added into F with FP64 atomics.
+// F_b = T + T^T with T = phi^T G, G = w (v/2 phi + g . grad phi)
+// (ScalarOperatorToMatrixAdder.cpp:178-303: tmp = phi_b^T grad_A, F_b = tmp + tmp^T; the
+// LDA form phi^T diag(w v) phi is the same with g = 0).  One CTA per (block, 64-row tile
+// i, 64-column tile j) over all tile pairs, one product per output (a tile pair of the
+// upper triangle with both products would pad the diagonal tiles with their mirror
+// halves); 256 threads with 4x4 outputs each; T(a, b) is added into F at (a, b) and
+// (b, a) with FP64 atomics.
 constexpr int kAT = 64, kAK = 32, kAPad = kAK + 1;
 __global__ void __launch_bounds__(256) fp64_adder_kernel(DevPlan P, const int* __restrict__ work, long w0,
                                                          const long* __restrict__ slab_off, int chunk_b0,
@@ -575,10 +596,8 @@ __global__ void __launch_bounds__(256) fp64_adder_kernel(DevPlan P, const int* _
                                                          const unsigned char* __restrict__ skip,
                                                          double* __restrict__ F) {
   extern __shared__ double sm[];
-  double* Pi = sm;                      // phi rows of tile i   [64][33]
-  double* Gi = Pi + kAT * kAPad;        // G rows of tile i
-  double* Pj = Gi + kAT * kAPad;        // phi rows of tile j
-  double* Gj = Pj + kAT * kAPad;        // G rows of tile j
+  double* Pi = sm;                // phi rows of tile i   [64][33]
+  double* Gj = Pi + kAT * kAPad;  // G rows of tile j
   const long item = w0 + blockIdx.x;
   const int b = work[3 * item], ti = work[3 * item + 1], tj = work[3 * item + 2];
   const int s = blockIdx.y;
@@ -601,42 +620,40 @@ __global__ void __launch_bounds__(256) fp64_adder_kernel(DevPlan P, const int* _
   for (int k0 = 0; k0 < n; k0 += kAK) {
     __syncthreads();
     for (int e = threadIdx.x; e < 2 * kAT * kAK; e += blockDim.x) {
-      const int which = e / (kAT * kAK);  // 0: tile i, 1: tile j
+      const int which = e / (kAT * kAK);  // 0: phi of tile i, 1: G of tile j
       const int r = (e % (kAT * kAK)) / kAK, q = e % kAK;
-      const int tile = which ? tj : ti, cnt = which ? cj : ci;
-      const int f = tile * kAT + r;
       const int pk = k0 + q;
-      double ph = 0.0, gg = 0.0;
-      if (r < cnt && pk < n) {
-        const double w = P.w[first + pk];
-        ph = slab[(long)f * kBlockPoints + pk];
-        gg = 0.5 * vs[pk] * ph;
-        if (gs)
-          gg += gs[pk] * slab[(long)(nact + f) * kBlockPoints + pk] +
-                gs[gstride + pk] * slab[(long)(2 * nact + f) * kBlockPoints + pk] +
-                gs[2 * gstride + pk] * slab[(long)(3 * nact + f) * kBlockPoints + pk];
-        gg *= w;
+      double val = 0.0;
+      if (which == 0) {
+        if (r < ci && pk < n) val = slab[(long)(ti * kAT + r) * kBlockPoints + pk];
+        Pi[r * kAPad + q] = val;
+      } else {
+        if (r < cj && pk < n) {
+          const int f = tj * kAT + r;
+          const double w = P.w[first + pk];
+          double gg = 0.5 * vs[pk] * slab[(long)f * kBlockPoints + pk];
+          if (gs)
+            gg += gs[pk] * slab[(long)(nact + f) * kBlockPoints + pk] +
+                  gs[gstride + pk] * slab[(long)(2 * nact + f) * kBlockPoints + pk] +
+                  gs[2 * gstride + pk] * slab[(long)(3 * nact + f) * kBlockPoints + pk];
+          val = gg * w;
+        }
+        Gj[r * kAPad + q] = val;
       }
-      double* PP = which ? Pj : Pi;
-      double* GG = which ? Gj : Gi;
-      PP[r * kAPad + q] = ph;
-      GG[r * kAPad + q] = gg;
     }
     __syncthreads();
     const int kl = min(kAK, n - k0);
     for (int q = 0; q < kl; ++q) {
-      double pa[4], ga[4], pb[4], gb[4];
+      double pa[4], gb[4];
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
         pa[a] = Pi[(ty + 16 * a) * kAPad + q];
-        ga[a] = Gi[(ty + 16 * a) * kAPad + q];
-        pb[a] = Pj[(tx + 16 * a) * kAPad + q];
         gb[a] = Gj[(tx + 16 * a) * kAPad + q];
       }
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[a][c] = fma(pa[a], gb[c], fma(ga[a], pb[c], acc[a][c]));
+        for (int c = 0; c < 4; ++c) acc[a][c] = fma(pa[a], gb[c], acc[a][c]);
     }
   }
   const int nbf = P.nbf;
@@ -652,7 +669,7 @@ __global__ void __launch_bounds__(256) fp64_adder_kernel(DevPlan P, const int* _
       if (q >= cj) continue;
       const int nu = fn[tj * kAT + q];
       atomicAdd(&Fs[(long)nu * nbf + mu], acc[a][c]);
-      if (ti != tj) atomicAdd(&Fs[(long)mu * nbf + nu], acc[a][c]);
+      atomicAdd(&Fs[(long)mu * nbf + nu], acc[a][c]);
     }
   }
 }
@@ -661,7 +678,7 @@ xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0
                               const long* slab_off, const double* scratch, int nspin, const double* v,
                               const double* g, const unsigned char* skip, double* F) {
   if (w1 <= w0) return XCGPU_OK;
-  const size_t smem = 4 * kAT * kAPad * sizeof(double);
+  const size_t smem = 2 * kAT * kAPad * sizeof(double);
   xcgpu_status st = c->cuda(cudaFuncSetAttribute(fp64_adder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)smem), "adder smem attribute");
   if (st) return st;
