@@ -304,15 +304,16 @@ __device__ __forceinline__ void fixed_scale(float m, float& scale, float& inv) {
 }
 
 // the six slice products of one 64-wide K chunk: leading x leading into the accumulator
-// at column acc0, the five others into the one at accR (first0 / firstR: start them)
-__device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t acc0, uint32_t accR, uint32_t stage, int N,
-                                                  bool first0, bool firstR) {
+// at column acc0, the five others into the one at accR (first0 / firstR: start them);
+// the three A slice tiles at abase, the three B slice tiles at bbase (shared memory)
+__device__ __forceinline__ void issue_fixed_chunk2(uint32_t tmem, uint32_t acc0, uint32_t accR, uint32_t abase,
+                                                   uint32_t bbase, int N, bool first0, bool firstR) {
   const uint32_t idesc = tc::idesc_f16(128, N);
   uint64_t a[3], b[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    a[i] = tc::smem_desc_sw128(stage + i * kTileA);
-    b[i] = tc::smem_desc_sw128(stage + (3 + i) * kTileA);
+    a[i] = tc::smem_desc_sw128(abase + i * kTileA);
+    b[i] = tc::smem_desc_sw128(bbase + i * kTileA);
   }
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks) {  // 16 FP16 (32 bytes) per MMA
@@ -324,6 +325,12 @@ __device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t acc0, 
     tc::mma_f16(tmem + accR, a[1] + o, b[1] + o, idesc, 1u);
     tc::mma_f16(tmem + accR, a[2] + o, b[0] + o, idesc, 1u);
   }
+}
+
+// the same with the stage layout of a streamed step: A slices, then B slices
+__device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t acc0, uint32_t accR, uint32_t stage, int N,
+                                                  bool first0, bool firstR) {
+  issue_fixed_chunk2(tmem, acc0, accR, stage, stage + 3 * kTileA, N, first0, firstR);
 }
 
 // density: the six slice products of one 64-wide K chunk into four accumulators: s0 t0
@@ -398,7 +405,7 @@ __global__ void __launch_bounds__(kT, 1)
   constexpr bool HAS_D = MODE != kModeAdder, HAS_A = MODE != kModeDensity;
   constexpr int NOPS = TWO_SPINS ? 3 : 2;  // adder operands: Phi, G per spin
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t mbar[2], full[2], mdone[2];
+  __shared__ uint64_t mbar[2], full[2], mdone[2], fdone;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort, s_smask;
   __shared__ double s_part[4][kQ - 1][128];  // density: partial sums of a point's threads
@@ -419,6 +426,7 @@ __global__ void __launch_bounds__(kT, 1)
       tc::mbar_init(&full[i], 1);
       tc::mbar_init(&mdone[i], 1);
     }
+    tc::mbar_init(&fdone, 1);
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -431,6 +439,7 @@ __global__ void __launch_bounds__(kT, 1)
   int gc = 0;                         // density: chunks issued by this CTA (stage = gc & 1)
   int J0 = 0;                         // adder: steps of earlier blocks (uniform)
   int last_copy = -1, last_mma = -1;  // adder, thread 0: highest step copied / issued
+  uint32_t fphase = 0;                // parity of the shared-memory tile pair's barrier
   float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
   const long rows_pad = (long)bt.ft_max * 128;
   // adder scratch: (adder mode) FP32 operand rows [2][NOPS][rows_pad][128]: values, low
@@ -439,6 +448,40 @@ __global__ void __launch_bounds__(kT, 1)
   float* const stg = my;
   float* const tiles = my + (MODE == kModeBuild ? 5 : 2 * NOPS) * rows_pad * 128;
   float* const scl = tiles + NOPS * bt.ft_max * kOpTileFloats;
+
+  // a tile pair's four accumulators -> V of item It (its block's active functions fnb,
+  // nact_b of them), on and above the diagonal, FP64 red.add
+  auto pair_to_V = [&](const MxItem& It, const int* fnb, int nact_b, int spin, int a, int bb) {
+    const int nbf_b = It.P.nbf;
+    const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
+    const int ma = min(128, nact_b - 128 * a), nb = min(128, nact_b - 128 * bb);
+    const int N = (nb + 15) & ~15;
+    const bool rok = row < ma;
+    const int m = 128 * a + row;
+    const float sPm = rok ? scl[m] : 0.f, sGm = rok ? scl[(1 + spin) * rows_pad + m] : 0.f;
+    double* Vrow = It.V + (long)spin * nbf_b * nbf_b + (rok ? __ldg(fnb + m) : 0);
+    const float* sPn = scl + 128 * bb;
+    const float* sGn = scl + (1 + spin) * rows_pad + 128 * bb;
+    if (c0 < N) {  // warp-uniform
+#pragma unroll 1
+      for (int cb = c0; cb < c0 + 32; cb += 8) {
+        float p0[8], pr[8], q0[8], qr[8];
+        tc::tmem_ld8(tmem + trow + 0 + cb, p0);
+        tc::tmem_ld8(tmem + trow + 128 + cb, pr);
+        tc::tmem_ld8(tmem + trow + 256 + cb, q0);
+        tc::tmem_ld8(tmem + trow + 384 + cb, qr);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int n = cb + c;
+          if (rok && n < nb && (a < bb || n >= row)) {
+            const float f1 = __fmul_rn(__fadd_rn(p0[c], pr[c]), __fmul_rn(sPm, sGn[n]));
+            const float f2 = __fmul_rn(__fadd_rn(q0[c], qr[c]), __fmul_rn(sGm, sPn[n]));
+            atomicAdd(Vrow + (long)__ldg(fnb + 128 * bb + n) * nbf_b, (double)__fadd_rn(f1, f2));
+          }
+        }
+      }
+    }
+  };
 
   for (;;) {
     if (HAS_D && tid < 128) s_amax[tid] = 0u;
@@ -459,6 +502,11 @@ __global__ void __launch_bounds__(kT, 1)
     const int s0 = P.sh_off[b], s1 = P.sh_off[b + 1];
     const long cs = (long)nact * 128;  // plane stride of the density scratch: value, its low part, gradient
     const int nft = (nact + 127) >> 7;
+    // a restricted build block of at most 128 functions: its Phi and G slice tiles (2 x 96
+    // KB) take the place of the two MMA stages, so the slicing writes them straight to
+    // shared memory and the one tile pair's MMAs read them there (no round trip through
+    // the global scratch and no bulk copies)
+    const bool tiles_in_smem = MODE == kModeBuild && !TWO_SPINS && nft == 1;
     int smask = 0;
     if constexpr (MODE == kModeAdder) {
       for (int s = 0; s < nspin; ++s)
@@ -796,8 +844,9 @@ __global__ void __launch_bounds__(kT, 1)
           fixed_slices2<7, 8>(__fmul_rn(x.y, inv), __fmul_rn(xl.y, inv), h[0][1], h[1][1], h[2][1]);
           fixed_slices2<7, 8>(__fmul_rn(x.z, inv), __fmul_rn(xl.z, inv), h[0][2], h[1][2], h[2][2]);
           fixed_slices2<7, 8>(__fmul_rn(x.w, inv), __fmul_rn(xl.w, inv), h[0][3], h[1][3], h[2][3]);
-          uint8_t* tb = reinterpret_cast<uint8_t*>(tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 *
-                                                              kTileFloats);
+          uint8_t* tb = tiles_in_smem ? sm + ((o == 0 ? 0 : 2) + (k4 >> 6)) * 3 * kTileA
+                                      : reinterpret_cast<uint8_t*>(
+                                            tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 * kTileFloats);
           const uint32_t off = tc::swz_offset_h(m & 127, k4 & 63);
 #pragma unroll
           for (int i = 0; i < 3; ++i)
@@ -805,7 +854,8 @@ __global__ void __launch_bounds__(kT, 1)
                 (uint32_t)h[i][0] | ((uint32_t)h[i][1] << 16), (uint32_t)h[i][2] | ((uint32_t)h[i][3] << 16));
         }
       }
-      tc::fence_async_global();  // these generic writes are read by the bulk copies below
+      if (tiles_in_smem) tc::fence_async_smem();  // these generic writes are read by the MMAs below
+      else tc::fence_async_global();             // ... by the bulk copies below
     };
     if constexpr (MODE == kModeBuild) {
     // ---- the functional at the block's points (build): the reference's steps, with the
@@ -993,6 +1043,35 @@ __global__ void __launch_bounds__(kT, 1)
       slice_rows(nact, (1 + __popc(smask)) * nact, warp, kWarps);
     }
     __syncthreads();
+    if (tiles_in_smem) {
+      // ---- 2. the one tile pair from shared memory: Phi tiles at the first stage, G at
+      //      the second, both products of every chunk issued back to back ----
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const int N = (nact + 15) & ~15;
+        for (int kc = 0; kc < nkc; ++kc) {
+          const uint32_t tp = tc::smem_u32(sm + kc * 3 * kTileA), tg = tc::smem_u32(sm + (2 + kc) * 3 * kTileA);
+          issue_fixed_chunk2(tmem, 0u, 128u, tp, tg, N, kc == 0, kc == 0);
+          issue_fixed_chunk2(tmem, 256u, 384u, tg, tp, N, kc == 0, kc == 0);
+        }
+        tc::mma_commit(&fdone);
+      }
+      const bool fok = tc::mbar_wait_bounded(&fdone, fphase, kWaitLimitNs);
+      fphase ^= 1u;
+      if (__syncthreads_or(!fok)) {
+        if (tid == 0) {
+          atomicExch(err, kErrTimeout);
+          s_abort = 1;
+          tc::mbar_wait_bounded(&fdone, fphase ^ 1u, kWaitLimitNs);  // let the MMAs land
+        }
+        goto done;
+      }
+      tc::fence_after_sync();
+      pair_to_V(I, fn, nact, 0, 0, 0);
+      tc::fence_before_sync();
+      __syncthreads();  // the accumulators and the stages are reused by the next block
+      continue;
+    }
     // ---- 2. tile pairs ----
     const int spp = 2 * nkc;                              // steps per pair: 2 products x chunks
     const int npairs = __popc(smask) * (nft * (nft + 1) / 2);
@@ -1073,34 +1152,7 @@ __global__ void __launch_bounds__(kT, 1)
       {
         int spin, a, bb, ph, kc;
         decode(iL, spin, a, bb, ph, kc);
-        const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
-        const int ma = min(128, nact - 128 * a), nb = min(128, nact - 128 * bb);
-        const int N = (nb + 15) & ~15;
-        const bool rok = row < ma;
-        const int m = 128 * a + row;
-        const float sPm = rok ? scl[m] : 0.f, sGm = rok ? scl[(1 + spin) * rows_pad + m] : 0.f;
-        double* Vrow = I.V + (long)spin * nbf * nbf + (rok ? __ldg(fn + m) : 0);
-        const float* sPn = scl + 128 * bb;
-        const float* sGn = scl + (1 + spin) * rows_pad + 128 * bb;
-        if (c0 < N) {  // warp-uniform
-#pragma unroll 1
-          for (int cb = c0; cb < c0 + 32; cb += 8) {
-            float p0[8], pr[8], q0[8], qr[8];
-            tc::tmem_ld8(tmem + trow + 0 + cb, p0);
-            tc::tmem_ld8(tmem + trow + 128 + cb, pr);
-            tc::tmem_ld8(tmem + trow + 256 + cb, q0);
-            tc::tmem_ld8(tmem + trow + 384 + cb, qr);
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-              const int n = cb + c;
-              if (rok && n < nb && (a < bb || n >= row)) {
-                const float f1 = __fmul_rn(__fadd_rn(p0[c], pr[c]), __fmul_rn(sPm, sGn[n]));
-                const float f2 = __fmul_rn(__fadd_rn(q0[c], qr[c]), __fmul_rn(sGm, sPn[n]));
-                atomicAdd(Vrow + (long)__ldg(fn + 128 * bb + n) * nbf, (double)__fadd_rn(f1, f2));
-              }
-            }
-          }
-        }
+        pair_to_V(I, fn, nact, spin, a, bb);
       }
       tc::fence_before_sync();
       __syncthreads();  // the accumulators are reused by the next pair
