@@ -33,7 +33,7 @@ sys.path.insert(0, ROOT)
 METRIC = "XC builds/s & Mpts/s, (H2O)32 PBE, mixed vs FP64 GPU at 1e-7 Eh; p50/p99 latency"
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the whole-build mixed kernel
 # on the (H2O)32 workload, from one ncu capture of that kernel
-MIXED_DRAM_BYTES = {"build": 941.1e6 + 5.2e6}
+MIXED_DRAM_BYTES = {"build": 624.8e6 + 3662.2e6}
 WORKLOADS = {0: "(H2O)4 def2-SVP LDA restricted, 50x194 Becke grid, 128-point blocks",
              1: "(H2O)32 def2-SVP PBE restricted, 75x302 Becke grid, 128-point blocks",
              2: "(H2O)64 def2-TZVP PBE unrestricted, 99x434 Becke grid, 128-point blocks"}
@@ -268,10 +268,6 @@ def run_extra(args):
     ctx = xcgpu.Context(device=0)
     prec = xcgpu.PREC_MIXED if args.precision == "mixed" else xcgpu.PREC_FP64
     if args.workload == "batch":
-        ws = batch.subsystem_workloads(64, 3, 40, seed=args.seed)
-        best, timings = batch.autotune_block(ctx, ws, prec, cache_path=os.path.join(ROOT, "_build_autotune.json"))
-        b = batch.SubsystemBatch(ctx, ws, prec, best)
-        b.capture()
         def timed(fn, reps):
             ms = []
             for _ in range(reps):
@@ -281,17 +277,33 @@ def run_extra(args):
                 ctx.check_async()
                 ms.append((time.perf_counter() - t0) * 1e3)
             return ms
-        timed(b.replay, args.warmup)
-        g_ms = timed(b.replay, args.steps)
-        timed(b.loop, 1)
-        l_ms = timed(b.loop, max(3, args.steps // 4))
+
+        def measure(ws, block):
+            b = batch.SubsystemBatch(ctx, ws, prec, block)
+            b.capture()
+            timed(b.replay, args.warmup)
+            g_ms = timed(b.replay, args.steps)
+            timed(b.loop, 1)
+            l_ms = timed(b.loop, max(3, args.steps // 4))
+            g, lp = float(np.median(g_ms)), float(np.median(l_ms))
+            out = {"ms_per_step": g, "per_cluster_loop_ms": lp, "speedup_vs_loop": lp / g,
+                   "builds_per_s": 1e3 * len(ws) / g, "mpts_per_s": b.npoints / g / 1e3, "npoints": b.npoints,
+                   "blocks_per_build": [p.stats()["nblocks"] for p, *_ in b.items][:4] + ["..."]}
+            b.close()
+            return out
+
+        ws = batch.subsystem_workloads(64, 3, 40, seed=args.seed)
+        best, timings = batch.autotune_block(ctx, ws, prec, cache_path=os.path.join(ROOT, "_build_autotune.json"))
+        r = measure(ws, best)
+        # the same step for subsystems so small that one build leaves most SMs idle (64 single
+        # waters on 50 x 110 grids, about 130 blocks a build against 152 SMs): the regime in
+        # which one launch over all builds pays
+        small = measure(batch.subsystem_workloads(64, 1, 1, seed=args.seed, n_rad=50, n_ang=110), 128)
         line = {"metric": "batched subsystem step: 64 XC builds (3-40 waters, def2-SVP, PBE, 75x302)",
-                "value": 1e3 / np.median(g_ms), "unit": "steps/s", "ms_per_step": float(np.median(g_ms)),
-                "per_cluster_loop_ms": float(np.median(l_ms)), "speedup_vs_loop": float(np.median(l_ms) / np.median(g_ms)),
-                "builds_per_s": 64e3 / np.median(g_ms), "mpts_per_s": b.npoints / np.median(g_ms) / 1e3,
+                "value": 1e3 / r["ms_per_step"], "unit": "steps/s", **r,
                 "autotune": {"block_points": best, "timings_s": {str(k): v for k, v in timings.items()}},
-                "precision": args.precision, "npoints": b.npoints, "steps": args.steps, "warmup": args.warmup,
-                "data": "synthetic"}
+                "small_subsystems": dict(small, workload="64 single waters, def2-SVP, PBE, 50x110"),
+                "precision": args.precision, "steps": args.steps, "warmup": args.warmup, "data": "synthetic"}
         print(json.dumps(line))
         return
     if args.workload == "fat":
@@ -314,6 +326,11 @@ def run_extra(args):
             out.append(q)
         return out
 
+    # one untimed pass over the first requests brings every stream's work arena and the
+    # plans' lazily built state to their sizes
+    server.precision = xcgpu.PREC_MIXED
+    server.run(at_rate(args.rate, 300), keep_results=False)
+    torch.cuda.synchronize()
     # the FP64 leg serves the first --fp64-requests requests of the same stream (at the
     # same arrival rate it runs far behind, so the whole stream would take many minutes)
     for name, p, k in [("mixed", xcgpu.PREC_MIXED, len(reqs)), ("fp64", xcgpu.PREC_FP64, args.fp64_requests)]:
@@ -332,8 +349,14 @@ def run_extra(args):
         st["rate_req_s"] = rate
         sweep.append(st)
     line["rate_sweep"] = sweep
-    ok = [st["rate_req_s"] for st in sweep if st["p99_ms"] <= 10.0 * st["p50_ms"]]
+    # sustainable: the stream is served at its arrival rate and queueing at most doubles the
+    # p99 of the lightest load (the p99 there is the service time of the largest requests,
+    # 128-water TZVP builds, so a multiple of the p50 of this size mix is no measure of it)
+    base = sweep[0]["p99_ms"] if sweep else None
+    ok = [st["rate_req_s"] for st in sweep
+          if st["throughput_req_s"] >= 0.97 * st["rate_req_s"] and st["p99_ms"] <= 2.0 * base]
     line["sustainable_rate_req_s"] = max(ok) if ok else None
+    line["sustainable_rule"] = "throughput >= 0.97 x arrival rate and p99 <= 2 x the p99 at the lowest rate"
     if args.latency_budget_ms > 0:
         server.latency_budget_s = args.latency_budget_ms / 1e3
         adm = []
@@ -413,7 +436,8 @@ def main():
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rate", type=float, default=100.0)
     ap.add_argument("--fp64-requests", type=int, default=300, help="serving: requests of the FP64 comparison leg")
-    ap.add_argument("--rates", type=lambda x: [float(v) for v in x.split(",")], default=[25.0, 50.0, 75.0, 100.0],
+    ap.add_argument("--rates", type=lambda x: [float(v) for v in x.split(",")],
+                    default=[25.0, 50.0, 100.0, 150.0, 200.0, 300.0],
                     help="serving: arrival rates of the mixed-precision sweep")
     ap.add_argument("--latency-budget-ms", type=float, default=1000.0,
                     help="serving: admission's latency budget for the sweep's second pass (0: none)")
@@ -486,7 +510,8 @@ def main():
                         "frac": (achieved / peak) if peak else None,
                         "traffic": MIXED_DRAM_BYTES.get(names[dom]) if args.config == 1 else None,
                         "traffic_note": "DRAM read + write bytes per launch of this kernel on this workload, "
-                                        "one ncu capture",
+                                        "one ncu capture (mostly write-backs of the per-CTA basis-plane scratch; "
+                                        "algorithmic ~70 MB)",
                         "note": "useful FP32-equivalent flops (2 npts n_b^2 per block and product) of the "
                                 "dominant kernel over its CUDA-event time; peak = measured cuBLAS bf16 burst "
                                 "(of measured; the kernel is timed in isolation). The fixed-point operands (three "
