@@ -742,22 +742,15 @@ static xcgpu_status run_builds(Ctx* c, std::vector<BuildReq>& reqs, int precisio
     for (size_t i = 0; i < reqs.size(); ++i) {
       const BuildReq& r = reqs[i];
       xcgpu_plan* P = r.plan;
-      const int nbf = P->basis->nbf;
-      XC_TRY(mixed_split(c, r.P, r.nspin, nbf, bw[i].psplit));
-      XC_TRY(c->cuda(cudaMemsetAsync(r.V, 0, (size_t)r.nspin * nbf * nbf * sizeof(double), c->stream), "memset V"));
       MixedWork mw{&P->basis->dev, &P->dev, r.nspin, bw[i].psplit, nullptr, nullptr, nullptr, nullptr, nullptr, r.V};
       mw.func = r.func;
       mw.thr = r.thr;
       mw.partials = bw[i].partials;
+      mw.Pm = r.P;
+      mw.exc_nel = r.exc_nel;
       work.push_back(mw);
     }
-    XC_TRY(mixed_build_batch(c, work, counter, err));
-    for (size_t i = 0; i < reqs.size(); ++i) {
-      const int nb = reqs[i].plan->nblocks;
-      if (nb) XC_TRY(launch_sum_partials(c, bw[i].partials, nb, 2, reqs[i].exc_nel));
-      else XC_TRY(c->cuda(cudaMemsetAsync(reqs[i].exc_nel, 0, 2 * sizeof(double), c->stream), "memset sums"));
-    }
-    return XCGPU_OK;
+    return mixed_build_batch(c, work, counter, err);  // split, build kernel, mirror and sums
   }
   bool chunked = !mixed;
   for (const auto& r : reqs) chunked = chunked && r.plan->max_block == kSkipBlock;

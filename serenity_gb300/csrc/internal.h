@@ -267,7 +267,9 @@ struct MixedWork {
   double* V;
   int func = 0;               // whole builds: functional,
   double thr = 0.0;           // adder block-skip threshold,
-  double* partials = nullptr;  // per-block E_xc, N_el sums [2][nblocks]
+  double* partials = nullptr;  // per-block E_xc, N_el sums [2][nblocks],
+  const double* Pm = nullptr;  // the FP64 density matrices (split into Psplit by the build)
+  double* exc_nel = nullptr;   // and where E_xc, N_el go
 };
 xcgpu_status mixed_init(Ctx* c);
 // bytes of the density kernel's form of nspin density matrices: 8 bytes of FP16
@@ -275,8 +277,9 @@ xcgpu_status mixed_init(Ctx* c);
 inline size_t psplit_bytes(int nspin, int nbf) { return (size_t)nspin * nbf * nbf * 8 + (size_t)nspin * nbf * 4; }
 xcgpu_status mixed_split(Ctx* c, const double* Pm, int nspin, int nbf, float* Psplit);
 // whole builds (density, functional, Vxc per block) of the MixedWork items with func,
-// thr and partials set (plans of 128-point blocks); V is mirrored, partials hold the
-// per-block E_xc and N_el sums
+// thr, partials, Pm and exc_nel set (plans of 128-point blocks): one launch splits every
+// item's P and zeroes its V, the persistent build kernel runs over all blocks, one launch
+// mirrors every V and one sums every item's partials into its E_xc and N_el
 xcgpu_status mixed_build_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
 xcgpu_status mixed_density_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);
 xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err);

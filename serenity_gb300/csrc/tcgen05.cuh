@@ -155,6 +155,47 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// n loads of 32 lanes x 8 columns each (columns taddr[i] .. + 8), then one wait: the
+// destination registers pass through the wait so no use of them is scheduled before it
+#define XCGPU_TMEM_LD8(T, R)                                                                          \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"               \
+               : "=r"((R)[0]), "=r"((R)[1]), "=r"((R)[2]), "=r"((R)[3]), "=r"((R)[4]), "=r"((R)[5]), \
+                 "=r"((R)[6]), "=r"((R)[7])                                                           \
+               : "r"(T))
+#define XCGPU_TMEM_PASS8(R)                                                                             \
+  "+r"((R)[0]), "+r"((R)[1]), "+r"((R)[2]), "+r"((R)[3]), "+r"((R)[4]), "+r"((R)[5]), "+r"((R)[6]), \
+      "+r"((R)[7])
+__device__ __forceinline__ void tmem_ld8x2(uint32_t t0, uint32_t t1, float* a, float* b) {
+  uint32_t r0[8], r1[8];
+  XCGPU_TMEM_LD8(t0, r0);
+  XCGPU_TMEM_LD8(t1, r1);
+  asm volatile("tcgen05.wait::ld.sync.aligned;" : XCGPU_TMEM_PASS8(r0), XCGPU_TMEM_PASS8(r1)::"memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    a[i] = __uint_as_float(r0[i]);
+    b[i] = __uint_as_float(r1[i]);
+  }
+}
+__device__ __forceinline__ void tmem_ld8x4(uint32_t t0, uint32_t t1, uint32_t t2, uint32_t t3, float* a, float* b,
+                                           float* c, float* d) {
+  uint32_t r0[8], r1[8], r2[8], r3[8];
+  XCGPU_TMEM_LD8(t0, r0);
+  XCGPU_TMEM_LD8(t1, r1);
+  XCGPU_TMEM_LD8(t2, r2);
+  XCGPU_TMEM_LD8(t3, r3);
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : XCGPU_TMEM_PASS8(r0), XCGPU_TMEM_PASS8(r1), XCGPU_TMEM_PASS8(r2), XCGPU_TMEM_PASS8(r3)::"memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    a[i] = __uint_as_float(r0[i]);
+    b[i] = __uint_as_float(r1[i]);
+    c[i] = __uint_as_float(r2[i]);
+    d[i] = __uint_as_float(r3[i]);
+  }
+}
+#undef XCGPU_TMEM_LD8
+#undef XCGPU_TMEM_PASS8
+
 // byte offset of FP16 element (r, k), k < 64, in a 128-byte-swizzled K-major tile
 // (64 FP16 per 128-byte row; the same 16-byte chunk permutation as above)
 __device__ __forceinline__ uint32_t swz_offset_h(int r, int k) {

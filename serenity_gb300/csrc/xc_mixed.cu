@@ -17,12 +17,9 @@ namespace xcgpu {
 // column j) finds the column's largest |P_ij|, its power-of-two scale (the largest
 // scaled element below 256) and the three FP16 slices of density_slices of every scaled
 // element, taken from the FP64 value, so P enters to 2^-27 of its column maximum.
-__global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__ P, uint2* __restrict__ out,
-                                                      float* __restrict__ colscale, int nbf) {
-  __shared__ double red[8];
-  const long c = blockIdx.x;  // spin * nbf + j
-  const double* col = P + c * nbf;
-  uint2* o = out + c * nbf;
+// one column: its largest |P_ij| (block reduction through red[8]), the scale, the slices
+__device__ __forceinline__ void split_column(const double* __restrict__ col, uint2* __restrict__ o,
+                                             float* __restrict__ colscale, int nbf, double* red) {
   double m = 0.0;
   for (int i = threadIdx.x; i < nbf; i += blockDim.x) m = fmax(m, fabs(col[i]));
   for (int d = 16; d > 0; d >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, d));
@@ -34,7 +31,7 @@ __global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__
   frexp(m, &e);
   const bool zero = !(m > 0.0) || e < -100;
   const double inv = zero ? 0.0 : ldexp(1.0, 8 - e);
-  if (threadIdx.x == 0) colscale[c] = zero ? 0.f : ldexpf(1.f, e - 8);
+  if (threadIdx.x == 0) *colscale = zero ? 0.f : ldexpf(1.f, e - 8);
   for (int i = threadIdx.x; i < nbf; i += blockDim.x) {
     const double v = col[i] * inv;  // |v| < 256, exact
     const double s0 = rint(v);
@@ -45,6 +42,82 @@ __global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__
     const uint32_t h1 = __half_as_ushort(__float2half_rn((float)(s1 * (1.0 / 512.0))));
     const uint32_t h2 = __half_as_ushort(__float2half_rn((float)(s2 * (1.0 / 512.0))));
     o[i] = make_uint2(h0 | (h1 << 16), h2);
+  }
+}
+
+__global__ void __launch_bounds__(256) split_p_kernel(const double* __restrict__ P, uint2* __restrict__ out,
+                                                      float* __restrict__ colscale, int nbf) {
+  __shared__ double red[8];
+  const long c = blockIdx.x;  // spin * nbf + j
+  split_column(P + c * nbf, out + c * nbf, colscale + c, nbf, red);
+}
+
+// The small per-build steps of a batch of whole builds, one launch each over all its
+// builds (launched per build they would be most of a batch of small builds): the split
+// of P with the zeroing of V, the mirror of V, the E_xc and N_el sums.  The builds'
+// columns (spin, j) form one index space, build i owning [col0[i], col0[i + 1]).
+struct SmallItem {
+  const double* P;
+  uint2* psl;
+  float* pcs;
+  double* V;
+  const double* partials;
+  double* exc_nel;
+  int nspin, nbf, nparts;
+};
+struct SmallBatch {
+  SmallItem it[kMaxItems];
+  long col0[kMaxItems + 1];
+  int n;
+};
+
+__device__ __forceinline__ int small_locate(const SmallBatch& sb, long c) {
+  int lo = 0, hi = sb.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sb.col0[mid] <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// one CTA per (build, spin, column j): split column j of P, zero column j of V
+__global__ void __launch_bounds__(256) split_zero_batch_kernel(const __grid_constant__ SmallBatch sb) {
+  __shared__ double red[8];
+  const long c = blockIdx.x;
+  const SmallItem& I = sb.it[small_locate(sb, c)];
+  const long cl = c - sb.col0[&I - sb.it];  // spin * nbf + j within the build
+  split_column(I.P + cl * I.nbf, I.psl + cl * I.nbf, I.pcs + cl, I.nbf, red);
+  double* v = I.V + cl * I.nbf;
+  for (int i = threadIdx.x; i < I.nbf; i += blockDim.x) v[i] = 0.0;
+}
+
+// one CTA per (build, spin, column j): rows below the diagonal from the upper triangle
+__global__ void __launch_bounds__(256) mirror_batch_kernel(const __grid_constant__ SmallBatch sb) {
+  const long c = blockIdx.x;
+  const SmallItem& I = sb.it[small_locate(sb, c)];
+  const long cl = c - sb.col0[&I - sb.it];
+  const int n = I.nbf, s = (int)(cl / n), j = (int)(cl % n);
+  double* M = I.V + (long)s * n * n;
+  for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) M[(long)j * n + i] = M[(long)i * n + j];
+}
+
+// one CTA per build: E_xc and N_el from the per-block partial sums, in the order of
+// sum_partials_kernel
+__global__ void __launch_bounds__(256) sums_batch_kernel(const __grid_constant__ SmallBatch sb) {
+  __shared__ double red[256];
+  const SmallItem& I = sb.it[blockIdx.x];
+  for (int c = 0; c < 2; ++c) {
+    double a = 0.0;
+    for (int i = threadIdx.x; i < I.nparts; i += blockDim.x) a += I.partials[(long)c * I.nparts + i];
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) I.exc_nel[c] = red[0];
+    __syncthreads();
   }
 }
 
@@ -199,9 +272,47 @@ xcgpu_status mixed_adder_batch(Ctx* c, const std::vector<MixedWork>& work, int* 
   return st ? st : mirror_all(c, work);
 }
 
+// the batched small steps of whole builds: before (split P, zero V) or after (mirror V,
+// E_xc and N_el) the build kernel
+static xcgpu_status small_launches(Ctx* c, const std::vector<MixedWork>& work, bool before) {
+  static thread_local SmallBatch sb;  // host-side parameter block (the launch copies it)
+  KernelTimer kt(c, kOther);
+  for (size_t i0 = 0; i0 < work.size(); i0 += kMaxItems) {
+    const size_t i1 = std::min(work.size(), i0 + kMaxItems);
+    sb.n = (int)(i1 - i0);
+    sb.col0[0] = 0;
+    for (size_t i = i0; i < i1; ++i) {
+      const MixedWork& w = work[i];
+      const int nbf = w.P->nbf;
+      SmallItem& it = sb.it[i - i0];
+      it.P = w.Pm;
+      it.psl = reinterpret_cast<uint2*>(w.Psplit);
+      it.pcs = reinterpret_cast<float*>(it.psl + (long)w.nspin * nbf * nbf);
+      it.V = w.V;
+      it.partials = w.partials;
+      it.exc_nel = w.exc_nel;
+      it.nspin = w.nspin;
+      it.nbf = nbf;
+      it.nparts = w.P->nblocks;
+      sb.col0[i - i0 + 1] = sb.col0[i - i0] + (long)w.nspin * nbf;
+    }
+    const long ncol = sb.col0[sb.n];
+    if (before) {
+      if (ncol > 0) split_zero_batch_kernel<<<(unsigned)ncol, 256, 0, c->stream>>>(sb);
+    } else {
+      if (ncol > 0) mirror_batch_kernel<<<(unsigned)ncol, 256, 0, c->stream>>>(sb);
+      sums_batch_kernel<<<(unsigned)sb.n, 256, 0, c->stream>>>(sb);
+    }
+    xcgpu_status st = c->check_launch(before ? "split_zero_batch_kernel" : "mirror_batch_kernel / sums_batch_kernel");
+    if (st) return st;
+  }
+  return XCGPU_OK;
+}
+
 xcgpu_status mixed_build_batch(Ctx* c, const std::vector<MixedWork>& work, int* counter, int* err) {
-  xcgpu_status st = mixed_launch<kModeBuild>(c, work, counter, err, kBuild, "mx_kernel (build)");
-  return st ? st : mirror_all(c, work);
+  xcgpu_status st = small_launches(c, work, true);
+  if (!st) st = mixed_launch<kModeBuild>(c, work, counter, err, kBuild, "mx_kernel (build)");
+  return st ? st : small_launches(c, work, false);
 }
 
 }  // namespace xcgpu

@@ -119,7 +119,7 @@ __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __
     for (int f = 0; f < nf; ++f) emit(f, 0.f, 0.f, 0.f, 0.f, 0.f);
     return;
   }
-  *rlo = Rv != 0.f ? __fdiv_rn(Rl, Rv) : 0.f;
+  *rlo = Rv != 0.f ? __fdividef(Rl, Rv) : 0.f;  // a correction of ~2^-24 relative: a few ulp of it suffice
   shell_functions_px_l<DERIV, MAXL>(l, d[0], d[1], d[2], Rv, dR, rec_pure(r.info), emit);
 }
 
@@ -408,6 +408,7 @@ __global__ void __launch_bounds__(kT, 1)
   __shared__ uint64_t mbar[2], full[2], mdone[2], fdone;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort, s_smask;
+  __shared__ int s_next[4];  // basis phase: next shell of the block, per 32-point group
   __shared__ double s_part[4][kQ - 1][128];  // density: partial sums of a point's threads
   __shared__ unsigned s_amax[128];           // per point: largest |phi| (FP32 bits)
   __shared__ float s_bscale[kNT];            // per function nu of the pass: scale of its column of P
@@ -466,10 +467,8 @@ __global__ void __launch_bounds__(kT, 1)
 #pragma unroll 1
       for (int cb = c0; cb < c0 + 32; cb += 8) {
         float p0[8], pr[8], q0[8], qr[8];
-        tc::tmem_ld8(tmem + trow + 0 + cb, p0);
-        tc::tmem_ld8(tmem + trow + 128 + cb, pr);
-        tc::tmem_ld8(tmem + trow + 256 + cb, q0);
-        tc::tmem_ld8(tmem + trow + 384 + cb, qr);
+        tc::tmem_ld8x4(tmem + trow + 0 + cb, tmem + trow + 128 + cb, tmem + trow + 256 + cb, tmem + trow + 384 + cb, p0,
+                       pr, q0, qr);
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           const int n = cb + c;
@@ -483,8 +482,43 @@ __global__ void __launch_bounds__(kT, 1)
     }
   };
 
+  // the one tile pair of a restricted block of at most 128 functions: only T = Phi^T G is
+  // formed, since F = T + T^T (the other product, G^T Phi, is T transposed: the same slice
+  // products summed in another order); T goes through shared memory (the operand tiles,
+  // consumed by then) so that each thread pairs T(m, n) with T(n, m)
+  auto diag_to_V = [&](const MxItem& It, const int* fnb, int nact_b) {
+    const int nbf_b = It.P.nbf;
+    const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
+    const int N = (nact_b + 15) & ~15;
+    float* const T = reinterpret_cast<float*>(sm);  // [128][129]
+    if (c0 < N) {  // warp-uniform
+      const float sPm = row < nact_b ? scl[row] : 0.f;
+      const float* sGn = scl + rows_pad;
+#pragma unroll 1
+      for (int cb = c0; cb < c0 + 32; cb += 8) {
+        float p0[8], pr[8];
+        tc::tmem_ld8x2(tmem + trow + cb, tmem + trow + 128 + cb, p0, pr);
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          T[row * 129 + cb + c] = __fmul_rn(__fadd_rn(p0[c], pr[c]), __fmul_rn(sPm, sGn[cb + c]));
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (c0 < N && row < nact_b) {
+      double* Vrow = It.V + __ldg(fnb + row);
+#pragma unroll 4
+      for (int c = 0; c < 32; ++c) {
+        const int n = c0 + c;
+        if (n < nact_b && n >= row)
+          atomicAdd(Vrow + (long)__ldg(fnb + n) * nbf_b, (double)__fadd_rn(T[row * 129 + n], T[n * 129 + row]));
+      }
+    }
+  };
+
   for (;;) {
     if (HAS_D && tid < 128) s_amax[tid] = 0u;
+    if (tid < 4) s_next[tid] = 0;
     __syncthreads();
     if (tid == 0) s_block = atomicAdd(counter, 1);
     __syncthreads();
@@ -530,11 +564,22 @@ __global__ void __launch_bounds__(kT, 1)
       const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
       float* const col = my + p;
       float vmax = 0.f;
+      // the kQ warps of a 32-point group take the block's shells from a shared counter
+      // (shells differ in cost: a fixed split leaves warps waiting at the barrier)
+      const int nsh = s1 - s0;
+      auto grab = [&]() {
+        int v = 0;
+        if (lane == 0) v = atomicAdd(&s_next[warp & 3], 1);
+        return __shfl_sync(0xffffffffu, v, 0);
+      };
+      int cur = grab();
       ShellRec next;
-      if (s0 + quarter < s1) next = load_rec(P.rec + s0 + quarter);
-      for (int si = s0 + quarter; si < s1; si += kQ) {
+      if (cur < nsh) next = load_rec(P.rec + s0 + cur);
+      while (cur < nsh) {  // warp-uniform
         const ShellRec r = next;
-        if (si + kQ < s1) next = load_rec(P.rec + si + kQ);  // in flight while r is evaluated
+        const int nx = grab();
+        if (nx < nsh) next = load_rec(P.rec + s0 + nx);  // in flight while r is evaluated
+        cur = nx;
         float* const t0 = col + (long)rec_f0(r.info) * 128;
         float rlo = 0.f;
         auto put = [&](int f, float v, float vl, float dx, float dy, float dz) {
@@ -683,10 +728,8 @@ __global__ void __launch_bounds__(kT, 1)
 #pragma unroll 1
             for (int cb = c0; cb < c0 + 32; cb += 8) {
               float a0[8], a1[8], ar[8], a3[8];
-              tc::tmem_ld8(tmem + trow + cb, a0);
-              tc::tmem_ld8(tmem + trow + 128 + cb, a1);
-              tc::tmem_ld8(tmem + trow + 256 + cb, ar);
-              tc::tmem_ld8(tmem + trow + 384 + cb, a3);
+              tc::tmem_ld8x4(tmem + trow + cb, tmem + trow + 128 + cb, tmem + trow + 256 + cb, tmem + trow + 384 + cb,
+                             a0, a1, ar, a3);
 #pragma unroll
               for (int c = 0; c < 8; ++c)
                 ar[c] = __fadd_rn(__fadd_rn(a0[c], a1[c]), fmaf(a3[c], 1.f / 512.f, ar[c]));
@@ -1045,14 +1088,13 @@ __global__ void __launch_bounds__(kT, 1)
     __syncthreads();
     if (tiles_in_smem) {
       // ---- 2. the one tile pair from shared memory: Phi tiles at the first stage, G at
-      //      the second, both products of every chunk issued back to back ----
+      //      the second; T = Phi^T G over every chunk ----
       if (tid == 0) {
         tc::fence_after_sync();
         const int N = (nact + 15) & ~15;
         for (int kc = 0; kc < nkc; ++kc) {
           const uint32_t tp = tc::smem_u32(sm + kc * 3 * kTileA), tg = tc::smem_u32(sm + (2 + kc) * 3 * kTileA);
           issue_fixed_chunk2(tmem, 0u, 128u, tp, tg, N, kc == 0, kc == 0);
-          issue_fixed_chunk2(tmem, 256u, 384u, tg, tp, N, kc == 0, kc == 0);
         }
         tc::mma_commit(&fdone);
       }
@@ -1067,7 +1109,7 @@ __global__ void __launch_bounds__(kT, 1)
         goto done;
       }
       tc::fence_after_sync();
-      pair_to_V(I, fn, nact, 0, 0, 0);
+      diag_to_V(I, fn, nact);
       tc::fence_before_sync();
       __syncthreads();  // the accumulators and the stages are reused by the next block
       continue;
