@@ -192,6 +192,12 @@ xcgpu_status xcgpu_density_fp64_noalloc(xcgpu_plan* plan, int nspin, const doubl
 xcgpu_status xcgpu_functional(xcgpu_ctx* ctx, int func, int nspin, uint64_t npoints, uint32_t skip_block,
                               const double* rho, const double* grad, double* epuv, double* dfdrho, double* dfdgrad,
                               int mem);
+/* The same with the functional arithmetic of a precision: XCGPU_PREC_FP64 as above,
+ * XCGPU_PREC_MIXED as the mixed build evaluates it (restricted PBE in FP32 pairs, ~1e-13
+ * relative to FP64; every other functional and spin case in FP64). */
+xcgpu_status xcgpu_functional_prec(xcgpu_ctx* ctx, int func, int nspin, uint64_t npoints, uint32_t skip_block,
+                                   const double* rho, const double* grad, double* epuv, double* dfdrho,
+                                   double* dfdgrad, int precision, int mem);
 int xcgpu_functional_is_gga(int func);
 /* ScalarOperatorToMatrixAdder::addScalarOperatorToMatrix (ScalarOperatorToMatrixAdder.h:56-93,
  * .cpp:51-113,178-303): F += sum_p w (v phi phi^T) (+ the GGA term with g = dF/d grad rho

@@ -879,7 +879,15 @@ xcgpu_status xcgpu_density(xcgpu_plan* P, int nspin, const double* Pm, double* r
 
 xcgpu_status xcgpu_functional(xcgpu_ctx* c, int func, int nspin, uint64_t n, uint32_t skip_block, const double* rho,
                               const double* grad, double* epuv, double* dfdrho, double* dfdgrad, int mem) {
+  return xcgpu_functional_prec(c, func, nspin, n, skip_block, rho, grad, epuv, dfdrho, dfdgrad, XCGPU_PREC_FP64, mem);
+}
+
+xcgpu_status xcgpu_functional_prec(xcgpu_ctx* c, int func, int nspin, uint64_t n, uint32_t skip_block,
+                                   const double* rho, const double* grad, double* epuv, double* dfdrho,
+                                   double* dfdgrad, int precision, int mem) {
   if (!c) return XCGPU_ERR_INVALID;
+  if (precision != XCGPU_PREC_FP64 && precision != XCGPU_PREC_MIXED)
+    return c->fail(XCGPU_ERR_INVALID, "functional: unknown precision");
   if (!xc::is_known(func)) return c->fail(XCGPU_ERR_INVALID, "unknown functional");
   const bool gga = xc::is_gga(func);
   if ((nspin != 1 && nspin != 2) || !rho || !epuv || !dfdrho || (gga && (!grad || !dfdgrad)))
@@ -905,7 +913,7 @@ xcgpu_status xcgpu_functional(xcgpu_ctx* c, int func, int nspin, uint64_t n, uin
     }
   }
   XC_TRY(launch_functional(c, func, nspin, (long)n, (int)skip_block, dr, gga ? dg : nullptr, e, v, gga ? vg : nullptr,
-                           nullptr, nullptr, nullptr, nullptr));
+                           nullptr, nullptr, nullptr, nullptr, precision == XCGPU_PREC_MIXED));
   if (mem == XCGPU_MEM_HOST) {
     XC_TRY(c->cuda(cudaMemcpyAsync(epuv, e, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "epuv"));
     XC_TRY(c->cuda(cudaMemcpyAsync(dfdrho, v, (size_t)nspin * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/xcgpu.h"
+#include "df32.cuh"
 
 namespace xcgpu {
 namespace xc {
@@ -45,6 +46,20 @@ template <> __device__ __forceinline__ float sqrt_<float>(float x) { return sqrt
 template <class R> __device__ __forceinline__ R pow_(R x, R p);
 template <> __device__ __forceinline__ double pow_<double>(double x, double p) { return pow(x, p); }
 template <> __device__ __forceinline__ float pow_<float>(float x, float p) { return powf(x, p); }
+// E = exp(x) and Em1 = E - 1 (FP32 pairs: Em1 from expm1, free of the cancellation)
+template <class R> __device__ __forceinline__ void exp_em1_(R x, R& E, R& Em1) {
+  E = exp_<R>(x);
+  Em1 = E - R(1);
+}
+// FP32 pairs (df32.cuh): the functions restricted PBE needs
+template <> __device__ __forceinline__ DF cbrt_<DF>(DF x) { return df_cbrt(x); }
+template <> __device__ __forceinline__ DF sqrt_<DF>(DF x) { return df_sqrt(x); }
+template <> __device__ __forceinline__ DF log_<DF>(DF x) { return df_log(x); }
+template <> __device__ __forceinline__ DF exp_<DF>(DF x) { return df_exp(x); }
+template <> __device__ __forceinline__ void exp_em1_<DF>(DF x, DF& E, DF& Em1) {
+  Em1 = df_expm1(x);
+  E = Em1 + DF(1.f, 0.f);
+}
 
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kTiny = 1e-14;
@@ -294,8 +309,9 @@ __device__ __forceinline__ void pbe_unpol(R n, R sigma, R& e, R& vn, R& vs) {
   const R deps_drs = R(-2 * A0 * a1) * L + R(2 * A0) * (R(1) + R(a1) * rs) * dQ1 * rq;
   const R dt2_dsig = R(kPi / 16.0 / 3.0936677262801355) * r13 * rn * rn;  // pi / (16 kF n^2)
   const R t2 = sigma * dt2_dsig;
-  const R E = exp_<R>(-eps * R(1.0 / kGamma));
-  const R rE = R(1) / (E - R(1));
+  R E, Em1;
+  exp_em1_<R>(-eps * R(1.0 / kGamma), E, Em1);
+  const R rE = R(1) / Em1;
   const R A = R(kBeta / kGamma) * rE;
   const R y = A * t2;
   const R N = R(1) + y;
@@ -314,6 +330,19 @@ __device__ __forceinline__ void pbe_unpol(R n, R sigma, R& e, R& vn, R& vs) {
   e += n * (eps + H);
   vn += eps + H + n * (deps_dn + dH_dn);
   vs += n * dH_dt2 * dt2_dsig;
+}
+
+// restricted PBE in FP32 pairs (the mixed build's functional): the same expressions as
+// pbe_unpol<double> to ~1e-13 relative, at FP32 instruction rates.  Above the density
+// cut-off every intermediate stays inside the FP32 range (n^-8/3 <= 2e37 at n = 1e-14).
+__device__ __forceinline__ void pbe_restricted_pair(double n, double sigma, double& e, double& vn, double& vs) {
+  e = vn = vs = 0.0;
+  if (!(n >= kTiny)) return;
+  DF E = DF(0.f, 0.f), VN = DF(0.f, 0.f), VS = DF(0.f, 0.f);
+  pbe_unpol<DF>(df_from_double(n), df_from_double(sigma), E, VN, VS);
+  e = df_to_double(E);
+  vn = df_to_double(VN);
+  vs = df_to_double(VS);
 }
 
 // ---- B88 gradient correction per spin (without the Slater part) ----

@@ -227,13 +227,15 @@ xcgpu_status fp64_density_chunk(Ctx* c, const DevPlan& P, int b0, int b1, const 
                                 int nspin, const double* Pm, double* rho, double* grad);
 xcgpu_status launch_functional_range(Ctx* c, int func, int nspin, long n, int skip_block, long p0, long p1,
                                      const double* rho, const double* grad, double* epuv, double* dfdrho,
-                                     double* dfdgrad, const double* w, double* partials, unsigned char* skipbuf);
+                                     double* dfdgrad, const double* w, double* partials, unsigned char* skipbuf,
+                                     bool pair = false);
 xcgpu_status launch_block_skip_flags_range(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
                                            double thr, unsigned char* skip, int b0, int b1);
 xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_block, const double* rho,
                                const double* grad, double* epuv, double* dfdrho, double* dfdgrad, const double* w,
                                double* partials /*2*nparts or null*/, int* nparts,
-                               unsigned char* skipbuf /*(n+skip_block-1)/skip_block, or null: context buffer*/);
+                               unsigned char* skipbuf /*(n+skip_block-1)/skip_block, or null: context buffer*/,
+                               bool pair = false /*restricted PBE in FP32 pairs, as the mixed build*/);
 xcgpu_status launch_block_skip_flags(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
                                      double thr, unsigned char* skip /*nspin*nblocks*/);
 xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0, long w1, int chunk_b0,

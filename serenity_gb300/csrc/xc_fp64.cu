@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(128) functional_kernel(int func, int nspin, lo
                                                          const double* __restrict__ grad, double* __restrict__ epuv,
                                                          double* __restrict__ dfdrho, double* __restrict__ dfdgrad,
                                                          const double* __restrict__ w, double* __restrict__ partials,
-                                                         long p0, long p1, int nparts) {
+                                                         long p0, long p1, int nparts, int pair) {
   const long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool gga = xc::is_gga(func);
   double e = 0.0, rtot = 0.0;
@@ -444,7 +444,10 @@ __global__ void __launch_bounds__(128) functional_kernel(int func, int nspin, lo
         gz = grad[2 * n + p];
       }
       double vn = 0.0, vs = 0.0;
-      if (!sk) xc::eval_restricted<double>(func, r, gx * gx + gy * gy + gz * gz, e, vn, vs);
+      if (!sk) {
+        if (pair && func == XCGPU_FUNC_PBE) xc::pbe_restricted_pair(r, gx * gx + gy * gy + gz * gz, e, vn, vs);
+        else xc::eval_restricted<double>(func, r, gx * gx + gy * gy + gz * gz, e, vn, vs);
+      }
       epuv[p] = e;
       dfdrho[p] = vn;
       if (gga) {
@@ -505,7 +508,8 @@ __global__ void __launch_bounds__(128) functional_kernel(int func, int nspin, lo
 // 128-point groups (nparts = ceil(n / 128)), the groups of the range written.
 xcgpu_status launch_functional_range(Ctx* c, int func, int nspin, long n, int skip_block, long p0, long p1,
                                      const double* rho, const double* grad, double* epuv, double* dfdrho,
-                                     double* dfdgrad, const double* w, double* partials, unsigned char* skipbuf) {
+                                     double* dfdgrad, const double* w, double* partials, unsigned char* skipbuf,
+                                     bool pair) {
   if (p1 <= p0) return XCGPU_OK;
   const int sb = skip_block > 0 ? skip_block : 1 << 30;
   const long nsk = (n + sb - 1) / sb;
@@ -525,16 +529,16 @@ xcgpu_status launch_functional_range(Ctx* c, int func, int nspin, long n, int sk
   }
   const unsigned grid = (unsigned)((p1 - p0 + 127) / 128);
   functional_kernel<<<grid, 128, 0, c->stream>>>(func, nspin, n, sb, skip, rho, grad, epuv, dfdrho, dfdgrad, w,
-                                                 partials, p0, p1, (int)((n + 127) / 128));
+                                                 partials, p0, p1, (int)((n + 127) / 128), pair ? 1 : 0);
   return c->check_launch("functional_kernel");
 }
 
 xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_block, const double* rho,
                                const double* grad, double* epuv, double* dfdrho, double* dfdgrad, const double* w,
-                               double* partials, int* nparts, unsigned char* skipbuf) {
+                               double* partials, int* nparts, unsigned char* skipbuf, bool pair) {
   if (nparts) *nparts = (int)((n + 127) / 128);
   return launch_functional_range(c, func, nspin, n, skip_block, 0, n, rho, grad, epuv, dfdrho, dfdgrad, w, partials,
-                                 skipbuf);
+                                 skipbuf, pair);
 }
 
 // ------------------------------------------------------------------------------------

@@ -929,7 +929,12 @@ __global__ void __launch_bounds__(kT, 1)
           const double r = s_rg[0 * 128 + q];
           const double gx = s_rg[1 * 128 + q], gy = s_rg[2 * 128 + q], gz = s_rg[3 * 128 + q];
           double vn = 0.0, vs = 0.0;
-          if (!fsk) xc::eval_restricted<double>(I.func, r, gga ? gx * gx + gy * gy + gz * gz : 0.0, e, vn, vs);
+          // restricted PBE in FP32 pairs (~1e-13 relative): FP64 at 1/64 of the FP32 rate
+          // would make it the longest step of the block
+          if (!fsk) {
+            if (I.func == XCGPU_FUNC_PBE) xc::pbe_restricted_pair(r, gx * gx + gy * gy + gz * gz, e, vn, vs);
+            else xc::eval_restricted<double>(I.func, r, gga ? gx * gx + gy * gy + gz * gz : 0.0, e, vn, vs);
+          }
           vv[0] = vn;
           if (gga) {
             gg[0][0] = 2.0 * vs * gx;

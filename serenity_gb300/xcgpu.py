@@ -97,6 +97,7 @@ def library(build_if_needed=True):
     L.xcgpu_plan_destroy.argtypes = [vp]
     L.xcgpu_density.argtypes = [vp, S, vp, vp, vp, S, S]
     L.xcgpu_functional.argtypes = [vp, S, S, ctypes.c_uint64, ctypes.c_uint32, vp, vp, vp, vp, vp, S]
+    L.xcgpu_functional_prec.argtypes = [vp, S, S, ctypes.c_uint64, ctypes.c_uint32, vp, vp, vp, vp, vp, S, S]
     L.xcgpu_functional_is_gga.argtypes = [S]
     L.xcgpu_add_scalar.argtypes = [vp, ctypes.c_double, S, vp, vp, vp, S, S]
     L.xcgpu_vxc.argtypes = [vp, S, S, S, ctypes.c_double, vp, vp, dp, dp, S]
@@ -122,7 +123,7 @@ def library(build_if_needed=True):
         getattr(L, name).restype = S
     for name in ["xcgpu_ctx_create", "xcgpu_set_stream", "xcgpu_synchronize", "xcgpu_grid_create", "xcgpu_grid_build",
                  "xcgpu_grid_build_partition", "xcgpu_grid_copy", "xcgpu_basis_create", "xcgpu_basis_coefs", "xcgpu_plan_create",
-                 "xcgpu_plan_get_stats", "xcgpu_block_on_grid", "xcgpu_density", "xcgpu_functional",
+                 "xcgpu_plan_get_stats", "xcgpu_block_on_grid", "xcgpu_density", "xcgpu_functional", "xcgpu_functional_prec",
                  "xcgpu_add_scalar", "xcgpu_vxc"]:
         getattr(L, name).restype = S
     _lib = L
@@ -217,9 +218,10 @@ class Context:
     def graph_destroy(self, g):
         self.L.xcgpu_graph_destroy(g)
 
-    def functional(self, func, rho, grad=None, skip_block=128):
+    def functional(self, func, rho, grad=None, skip_block=128, precision=PREC_FP64):
         """FunctionalLibrary::calcData(GRADIENTS, ., order 1) on host arrays
-        rho [nspin, n], grad [nspin, 3, n] -> (epuv, dfdrho, dfdgrad)."""
+        rho [nspin, n], grad [nspin, 3, n] -> (epuv, dfdrho, dfdgrad); precision
+        PREC_MIXED evaluates as the mixed build does (restricted PBE in FP32 pairs)."""
         fid = FUNC[func] if isinstance(func, str) else int(func)
         rho = _f64(rho)
         nspin, n = rho.shape
@@ -228,8 +230,8 @@ class Context:
         epuv = np.zeros(n)
         dr = np.zeros((nspin, n))
         dg = np.zeros((nspin, 3, n)) if gga else None
-        self.check(self.L.xcgpu_functional(self.h, fid, nspin, n, skip_block, _ptr(rho), _ptr(g), _ptr(epuv), _ptr(dr),
-                                           _ptr(dg), MEM_HOST))
+        self.check(self.L.xcgpu_functional_prec(self.h, fid, nspin, n, skip_block, _ptr(rho), _ptr(g), _ptr(epuv),
+                                                _ptr(dr), _ptr(dg), precision, MEM_HOST))
         return epuv, dr, dg
 
 

@@ -98,3 +98,38 @@ def test_mixed_vxc_benchmark_tolerance(ctx, nmol, dims, basis, nocc, n_rad, n_an
     assert abs(exc - rexc) <= 1e-7, abs(exc - rexc)
     assert abs(nel - rnel) <= 1e-8 * rnel, abs(nel - rnel)
     assert np.abs(V - rV).max() <= 1e-7, np.abs(V - rV).max()
+
+
+def test_pair_functional_matches_fp64(ctx):
+    """The mixed build evaluates restricted PBE in FP32 pairs: against the FP64 functional
+    on densities 1e-14..1e3 and reduced gradients 0..8.  Bounds: 1e-11 relative above a
+    density of 1e-6 (~48-bit pairs; the FP64 form itself rounds to ~1e-15); below it,
+    where both forms lose digits to the cancellations of the low-density limit, 1e-7
+    relative with a floor of 1e-13 rho^(4/3) (far below the points' weight in E_xc).
+    dF/d(grad rho) is measured against the exchange part's size, 1e-2 rho^(-4/3) |grad
+    rho|: PBE's mu = beta pi^2 / 3 makes the exchange and correlation parts cancel at
+    small reduced gradients (to 2e-8 of each at s = 1e-3), so the sum has fewer correct
+    digits than either part in FP64 as well."""
+    from serenity_gb300 import xcgpu
+    rng = np.random.default_rng(5)
+    rho = np.repeat(np.logspace(-14, 3, 171), 12)
+    s = np.tile([0.0, 1e-3, 0.01, 0.1, 0.3, 0.7, 1.0, 1.5, 2.0, 3.0, 5.0, 8.0], 171)
+    kf = (3 * np.pi ** 2 * rho) ** (1 / 3)
+    gnorm = s * 2 * kf * rho
+    d = rng.normal(size=(3, rho.size))
+    d /= np.linalg.norm(d, axis=0)
+    grad = (gnorm * d)[None]
+    ref = ctx.functional("PBE", rho[None], grad, skip_block=0, precision=xcgpu.PREC_FP64)
+    got = ctx.functional("PBE", rho[None], grad, skip_block=0, precision=xcgpu.PREC_MIXED)
+    hi = rho >= 1e-6
+    floor = 1e-13 * rho ** (4 / 3)
+    for name, a, b, fl_ in [("e", got[0], ref[0], floor), ("vrho", got[1][0], ref[1][0], floor / rho),
+                            ("vgrad", got[2][0], ref[2][0], None)]:
+        if fl_ is None:  # dF/d(grad rho): relative to the exchange part's size
+            nb = np.maximum(np.linalg.norm(b, axis=0), 1e-2 * rho ** (-4 / 3) * gnorm)
+            err = np.linalg.norm(a - b, axis=0) / np.maximum(nb, 1e-300)
+            err = np.where(gnorm > 0, err, 0.0)
+        else:
+            err = np.abs(a - b) / np.maximum(np.abs(b), fl_)
+        assert err[hi].max() < 1e-11, (name, err[hi].max(), rho[hi][np.argmax(err[hi])])
+        assert err[~hi].max() < 1e-7, (name, err[~hi].max(), rho[~hi][np.argmax(err[~hi])])
