@@ -52,6 +52,18 @@ constexpr Table solid(int l) {
   return T;
 }
 constexpr double dfact(int n) { return n <= 1 ? 1.0 : n * dfact(n - 2); }
+// per solid harmonic m of a table, the first monomial k with a nonzero coefficient
+struct FirstTerms {
+  int k[13];
+};
+constexpr FirstTerms first_terms(const Table& T, int ns, int nc) {
+  FirstTerms f{};
+  for (int m = 0; m < 13; ++m) f.k[m] = -1;
+  for (int m = 0; m < ns; ++m)
+    for (int k = 0; k < nc; ++k)
+      if (T.c[m][k] != 0.0 && f.k[m] < 0) f.k[m] = k;
+  return f;
+}
 constexpr Table cartesian(int l) {
   Table T{};
   int k = 0;
@@ -225,6 +237,7 @@ __device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, f
   constexpr int NS = 2 * L + 1;
   constexpr cx::Table TS = cx::solid(L);
   constexpr cx::Table TC = cx::cartesian(L);
+  constexpr cx::FirstTerms FK = cx::first_terms(TS, NS, (L + 1) * (L + 2) / 2);
   F2 px[L + 1], py[L + 1], pz[L + 1];
   px[0] = py[0] = pz[0] = F2{1.f, 0.f};
 #pragma unroll
@@ -259,29 +272,46 @@ __device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, f
         g1 = dmy * Rv + md * y.h;
         g2 = dmz * Rv + md * z.h;
       }
+      // (the coefficient tests below are on compile-time tables and fold away: a unit
+      // coefficient multiplies nothing, a function's first term starts its sum)
       if (pure) {
 #pragma unroll
         for (int m = 0; m < NS; ++m) {
           if (TS.c[m][k] != 0.0) {
             const float t = float(TS.c[m][k]);
             const float tl = float(TS.c[m][k] - (double)float(TS.c[m][k]));
-            F2 p = f2_mul1(mono, t);
-            if (tl != 0.f) p.l = fmaf(tl, mono.h, p.l);
-            f2_acc(sv[m], p);
-            if (DERIV >= 1) {
-              sg[3 * m] += t * g0;
-              sg[3 * m + 1] += t * g1;
-              sg[3 * m + 2] += t * g2;
+            F2 p = mono;
+            if (t != 1.f || tl != 0.f) {
+              p = f2_mul1(mono, t);
+              if (tl != 0.f) p.l = fmaf(tl, mono.h, p.l);
+            }
+            if (k == FK.k[m]) {
+              sv[m] = p;
+              if (DERIV >= 1) {
+                sg[3 * m] = t == 1.f ? g0 : t * g0;
+                sg[3 * m + 1] = t == 1.f ? g1 : t * g1;
+                sg[3 * m + 2] = t == 1.f ? g2 : t * g2;
+              }
+            } else {
+              f2_acc(sv[m], p);
+              if (DERIV >= 1) {
+                sg[3 * m] += t * g0;
+                sg[3 * m + 1] += t * g1;
+                sg[3 * m + 2] += t * g2;
+              }
             }
           }
         }
       } else {
         const float t = float(TC.c[0][k]);
         const float tl = float(TC.c[0][k] - (double)float(TC.c[0][k]));
-        F2 p = f2_mul1(mono, t);
-        if (tl != 0.f) p.l = fmaf(tl, mono.h, p.l);
+        F2 p = mono;
+        if (t != 1.f || tl != 0.f) {
+          p = f2_mul1(mono, t);
+          if (tl != 0.f) p.l = fmaf(tl, mono.h, p.l);
+        }
         const F2 v = f2_mul1(p, Rv);
-        emit(k, v.h, v.l, t * g0, t * g1, t * g2);
+        emit(k, v.h, v.l, t == 1.f ? g0 : t * g0, t == 1.f ? g1 : t * g1, t == 1.f ? g2 : t * g2);
       }
     }
   }
