@@ -327,6 +327,30 @@ __device__ __forceinline__ void issue_fixed_chunk2(uint32_t tmem, uint32_t acc0,
   }
 }
 
+// the same with the slice tiles of A and B `astride` / `bstride` bytes apart (a B operand
+// of N rows: N x 128 bytes per slice)
+__device__ __forceinline__ void issue_fixed_chunk3(uint32_t tmem, uint32_t acc0, uint32_t accR, uint32_t abase,
+                                                   uint32_t astride, uint32_t bbase, uint32_t bstride, int N,
+                                                   bool first) {
+  const uint32_t idesc = tc::idesc_f16(128, N);
+  uint64_t a[3], b[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    a[i] = tc::smem_desc_sw128(abase + i * astride);
+    b[i] = tc::smem_desc_sw128(bbase + i * bstride);
+  }
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+    const uint64_t o = 2u * ks;
+    tc::mma_f16(tmem + acc0, a[0] + o, b[0] + o, idesc, (first && ks == 0) ? 0u : 1u);
+    tc::mma_f16(tmem + accR, a[0] + o, b[1] + o, idesc, (first && ks == 0) ? 0u : 1u);
+    tc::mma_f16(tmem + accR, a[1] + o, b[0] + o, idesc, 1u);
+    tc::mma_f16(tmem + accR, a[0] + o, b[2] + o, idesc, 1u);
+    tc::mma_f16(tmem + accR, a[1] + o, b[1] + o, idesc, 1u);
+    tc::mma_f16(tmem + accR, a[2] + o, b[0] + o, idesc, 1u);
+  }
+}
+
 // the same with the stage layout of a streamed step: A slices, then B slices
 __device__ __forceinline__ void issue_fixed_chunk(uint32_t tmem, uint32_t acc0, uint32_t accR, uint32_t stage, int N,
                                                   bool first0, bool firstR) {
@@ -384,6 +408,11 @@ __device__ __forceinline__ void issue_density_chunk(uint32_t tmem, uint32_t stag
 //   (J >> 1) & 1 of that stage's barriers, so every waiter knows its parity.
 // =====================================================================================
 constexpr int kOpTileFloats = 2 * 3 * kTileFloats;  // one 128-function tile: 2 chunks x 3 slices
+// restricted build blocks of 129..kMidMax functions keep their G slice tiles (all
+// functions, both chunks: at most 2 x 3 x 192 x 128 bytes) in shared memory behind one
+// 48 KB slot for the Phi tile being multiplied
+constexpr int kMidMax = 192;
+constexpr uint32_t kMidB = 3 * kTileA;  // offset of the G tiles
 
 // =====================================================================================
 // The mixed kernels, one template in three modes:
@@ -405,7 +434,7 @@ __global__ void __launch_bounds__(kT, 1)
   constexpr bool HAS_D = MODE != kModeAdder, HAS_A = MODE != kModeDensity;
   constexpr int NOPS = TWO_SPINS ? 3 : 2;  // adder operands: Phi, G per spin
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t mbar[2], full[2], mdone[2], fdone;
+  __shared__ uint64_t mbar[2], full[2], mdone[2], fdone, mfull, mmma;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort, s_smask;
   __shared__ int s_next[4];  // basis phase: next shell of the block, per 32-point group
@@ -428,6 +457,8 @@ __global__ void __launch_bounds__(kT, 1)
       tc::mbar_init(&mdone[i], 1);
     }
     tc::mbar_init(&fdone, 1);
+    tc::mbar_init(&mfull, 1);
+    tc::mbar_init(&mmma, 1);
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -441,6 +472,7 @@ __global__ void __launch_bounds__(kT, 1)
   int J0 = 0;                         // adder: steps of earlier blocks (uniform)
   int last_copy = -1, last_mma = -1;  // adder, thread 0: highest step copied / issued
   uint32_t fphase = 0;                // parity of the shared-memory tile pair's barrier
+  uint32_t mphase = 0;                // parities of mfull (bit 0) and mmma (bit 1)
   float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
   const long rows_pad = (long)bt.ft_max * 128;
   // adder scratch: (adder mode) FP32 operand rows [2][NOPS][rows_pad][128]: values, low
@@ -541,6 +573,9 @@ __global__ void __launch_bounds__(kT, 1)
     // shared memory and the one tile pair's MMAs read them there (no round trip through
     // the global scratch and no bulk copies)
     const bool tiles_in_smem = MODE == kModeBuild && !TWO_SPINS && nft == 1;
+    // 129..kMidMax functions: G tiles in shared memory, T = Phi^T G one Phi tile at a time
+    const bool tiles_mid = MODE == kModeBuild && !TWO_SPINS && nft == 2 && nact <= kMidMax;
+    const int npad = (nact + 15) & ~15;
     int smask = 0;
     if constexpr (MODE == kModeAdder) {
       for (int s = 0; s < nspin; ++s)
@@ -887,18 +922,25 @@ __global__ void __launch_bounds__(kT, 1)
           fixed_slices2<7, 8>(__fmul_rn(x.y, inv), __fmul_rn(xl.y, inv), h[0][1], h[1][1], h[2][1]);
           fixed_slices2<7, 8>(__fmul_rn(x.z, inv), __fmul_rn(xl.z, inv), h[0][2], h[1][2], h[2][2]);
           fixed_slices2<7, 8>(__fmul_rn(x.w, inv), __fmul_rn(xl.w, inv), h[0][3], h[1][3], h[2][3]);
-          uint8_t* tb = tiles_in_smem ? sm + ((o == 0 ? 0 : 2) + (k4 >> 6)) * 3 * kTileA
-                                      : reinterpret_cast<uint8_t*>(
-                                            tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 * kTileFloats);
-          const uint32_t off = tc::swz_offset_h(m & 127, k4 & 63);
+          uint8_t* tb;
+          uint32_t sstride = kTileA, off = tc::swz_offset_h(m & 127, k4 & 63);
+          if (tiles_in_smem) {
+            tb = sm + ((o == 0 ? 0 : 2) + (k4 >> 6)) * 3 * kTileA;
+          } else if (tiles_mid && o != 0) {  // G rows of all functions, one tile per chunk
+            sstride = (uint32_t)npad * 128u;
+            tb = sm + kMidB + (k4 >> 6) * 3 * sstride;
+            off = tc::swz_offset_h(m, k4 & 63);
+          } else {
+            tb = reinterpret_cast<uint8_t*>(tiles + (((long)o * bt.ft_max + (m >> 7)) * 2 + (k4 >> 6)) * 3 * kTileFloats);
+          }
 #pragma unroll
           for (int i = 0; i < 3; ++i)
-            *reinterpret_cast<uint2*>(tb + i * kTileA + off) = make_uint2(
+            *reinterpret_cast<uint2*>(tb + i * sstride + off) = make_uint2(
                 (uint32_t)h[i][0] | ((uint32_t)h[i][1] << 16), (uint32_t)h[i][2] | ((uint32_t)h[i][3] << 16));
         }
       }
-      if (tiles_in_smem) tc::fence_async_smem();  // these generic writes are read by the MMAs below
-      else tc::fence_async_global();             // ... by the bulk copies below
+      if (tiles_in_smem || tiles_mid) tc::fence_async_smem();  // these generic writes are read by the MMAs below
+      if (!tiles_in_smem) tc::fence_async_global();            // ... by the bulk copies below
     };
     if constexpr (MODE == kModeBuild) {
     // ---- the functional at the block's points (build): the reference's steps, with the
@@ -1091,6 +1133,99 @@ __global__ void __launch_bounds__(kT, 1)
       slice_rows(nact, (1 + __popc(smask)) * nact, warp, kWarps);
     }
     __syncthreads();
+    if (tiles_mid) {
+      // ---- 2. T = Phi^T G over all functions, one 128-row tile of Phi at a time (the Phi
+      //      tile's chunks streamed from the scratch into the slot, G's from shared
+      //      memory; N = npad <= 192: accumulators at columns 0 and 256); T's first tile
+      //      goes to the scratch (the planes are consumed), its second and then the first
+      //      to shared memory as T[m][n] (row stride nact | 1), and F = T + T^T is paired
+      //      there ----
+      const float* const sGn = scl + rows_pad;
+      float* const Tg = my;  // first tile, column-major [npad][128]
+      const int ldT = nact | 1;
+      float* const Ts = reinterpret_cast<float*>(sm);
+      for (int a = 0; a < 2; ++a) {
+        const int ma = min(128, nact - 128 * a);
+        bool ok = true;
+        if (tid == 0) {
+          tc::fence_after_sync();
+          const uint32_t ab = (uint32_t)((ma + 7) & ~7) * 128u;
+          int stuck = 0;  // 1: a copy, 2: MMAs still in flight after a wait gave up
+          for (int kc = 0; kc < nkc; ++kc) {
+            const float* ta = tiles + ((long)a * 2 + kc) * 3 * kTileFloats;  // operand 0 (Phi), tile a
+            tc::mbar_arrive_expect_tx(&mfull, 3 * ab);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) tc::bulk_g2s(sm + q * kTileA, ta + q * kTileFloats, ab, &mfull);
+            if (!tc::mbar_wait_bounded(&mfull, mphase & 1u, kWaitLimitNs)) {
+              stuck = 1;
+              break;
+            }
+            mphase ^= 1u;
+            tc::fence_after_sync();
+            issue_fixed_chunk3(tmem, 0u, 256u, tc::smem_u32(sm), kTileA,
+                               tc::smem_u32(sm + kMidB + kc * 3 * npad * 128), (uint32_t)npad * 128u, npad, kc == 0);
+            tc::mma_commit(&mmma);
+            if (!tc::mbar_wait_bounded(&mmma, (mphase >> 1) & 1u, kWaitLimitNs)) {  // the slot is free again
+              stuck = 2;
+              break;
+            }
+            mphase ^= 2u;
+          }
+          if (stuck) {
+            ok = false;
+            atomicExch(err, kErrTimeout);
+            s_abort = 1;
+            // what was issued lands before the CTA gives up its memory
+            if (stuck == 1) tc::mbar_wait_bounded(&mfull, mphase & 1u, kWaitLimitNs);
+            else tc::mbar_wait_bounded(&mmma, (mphase >> 1) & 1u, kWaitLimitNs);
+          }
+        }
+        if (__syncthreads_or(!ok)) goto done;
+        tc::fence_after_sync();
+        // drain: row (lane) r of the tile, 8 columns at a time
+        const int r = 32 * (warp & 3) + lane;
+        const float sPm = r < ma ? scl[128 * a + r] : 0.f;
+#pragma unroll 1
+        for (int cb = 32 * (warp >> 2); cb < npad; cb += 128) {
+#pragma unroll 1
+          for (int c8 = cb; c8 < cb + 32 && c8 < npad; c8 += 8) {
+            float p0[8], pr[8];
+            tc::tmem_ld8x2(tmem + trow + c8, tmem + trow + 256 + c8, p0, pr);
+            if (r < ma) {
+#pragma unroll
+              for (int c = 0; c < 8; ++c) {
+                const int n = c8 + c;
+                if (n < nact) {
+                  const float t = __fmul_rn(__fadd_rn(p0[c], pr[c]), __fmul_rn(sPm, sGn[n]));
+                  if (a == 0) Tg[n * 128 + r] = t;
+                  else Ts[(128 + r) * ldT + n] = t;
+                }
+              }
+            }
+          }
+        }
+        tc::fence_before_sync();
+        __syncthreads();  // the accumulators are reused by the second tile
+      }
+      // the first tile from the scratch into shared memory
+      for (int e = tid; e < 128 * nact; e += kT) {
+        const int n = e >> 7, r = e & 127;
+        Ts[r * ldT + n] = Tg[e];
+      }
+      __syncthreads();
+      {
+        const int nbf_b = I.P.nbf;
+#pragma unroll 1
+        for (int n = warp; n < nact; n += kWarps) {
+          double* const Vc = I.V + (long)__ldg(fn + n) * nbf_b;
+#pragma unroll 1
+          for (int m = lane; m <= n; m += 32)
+            atomicAdd(Vc + __ldg(fn + m), (double)__fadd_rn(Ts[m * ldT + n], Ts[n * ldT + m]));
+        }
+      }
+      __syncthreads();  // the shared memory is reused by the next block
+      continue;
+    }
     if (tiles_in_smem) {
       // ---- 2. the one tile pair from shared memory: Phi tiles at the first stage, G at
       //      the second; T = Phi^T G over every chunk ----
