@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kT, 1)
   constexpr bool HAS_D = MODE != kModeAdder, HAS_A = MODE != kModeDensity;
   constexpr int NOPS = TWO_SPINS ? 3 : 2;  // adder operands: Phi, G per spin
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t mbar[2], full[2], mdone[2], fdone, mfull, mmma;
+  __shared__ uint64_t mbar[2], full[2], mdone[2], fdone, mfull, mmma, afull[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort, s_smask;
   __shared__ int s_next[4];  // basis phase: next shell of the block, per 32-point group
@@ -459,6 +459,8 @@ __global__ void __launch_bounds__(kT, 1)
     tc::mbar_init(&fdone, 1);
     tc::mbar_init(&mfull, 1);
     tc::mbar_init(&mmma, 1);
+    tc::mbar_init(&afull[0], 1);
+    tc::mbar_init(&afull[1], 1);
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -473,6 +475,7 @@ __global__ void __launch_bounds__(kT, 1)
   int last_copy = -1, last_mma = -1;  // adder, thread 0: highest step copied / issued
   uint32_t fphase = 0;                // parity of the shared-memory tile pair's barrier
   uint32_t mphase = 0;                // parities of mfull (bit 0) and mmma (bit 1)
+  uint32_t aphase = 0;                // density: per stage (bit) parity of afull
   float* const my = bt.scratch + (long)blockIdx.x * bt.cta_floats;
   const long rows_pad = (long)bt.ft_max * 128;
   // adder scratch: (adder mode) FP32 operand rows [2][NOPS][rows_pad][128]: values, low
@@ -588,7 +591,7 @@ __global__ void __launch_bounds__(kT, 1)
       continue;
     }
     if constexpr (HAS_D) {
-      if (5L * nact * 128 > bt.cta_floats) {  // scratch sized for a smaller block: report, skip
+      if (5L * rows_pad * 128 + (long)nft * kOpTileFloats > bt.cta_floats) {  // scratch sized for a smaller block
         if (tid == 0) atomicExch(err, kErrScratch);
         continue;
       }
@@ -672,8 +675,22 @@ __global__ void __launch_bounds__(kT, 1)
           }
           uint8_t* const stage = sm + st * kDStageBytes;
           const int mu0 = kc * 64;
+          // A of chunk kc is the same in every pass and for every spin: in the two-spin
+          // kernels it is sliced in the first pass of the first spin, kept in the scratch
+          // after the planes and copied back into the stage by the later passes (in the
+          // one-spin kernels the extra code cost more in the rest of the kernel, measured,
+          // than it saved in their few multi-pass blocks)
+          const bool reuseA = TWO_SPINS && (nu0 > 0 || s > 0);
+          const bool saveA = TWO_SPINS && !reuseA && (nact > kNT || nspin > 1);
+          uint8_t* const agl = reinterpret_cast<uint8_t*>(my + 5 * rows_pad * 128) + kc * 3 * kTileA;
+          if (reuseA) {
+            if (tid == 0) {
+              tc::mbar_arrive_expect_tx(&afull[st], 3 * kTileA);
+#pragma unroll
+              for (int q = 0; q < 3; ++q) tc::bulk_g2s(stage + q * kTileA, agl + q * kTileA, kTileA, &afull[st]);
+            }
+          } else {
           // ---- A: row p, 16-byte chunks j = 2 quarter, 2 quarter + 1 (8 functions each) ----
-          {
             float av[16], al[16];  // all loads in flight before any is used
 #pragma unroll
             for (int e = 0; e < 16; ++e) {
@@ -697,10 +714,18 @@ __global__ void __launch_bounds__(kT, 1)
                 w2[e >> 1] = (uint32_t)a2 | ((uint32_t)b2 << 16);
               }
               const uint32_t off = (uint32_t)(p * 128 + ((j ^ (p & 7)) << 4));
-              *reinterpret_cast<uint4*>(stage + off) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
-              *reinterpret_cast<uint4*>(stage + kTileA + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
-              *reinterpret_cast<uint4*>(stage + 2 * kTileA + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+              const uint4 q0 = make_uint4(w0[0], w0[1], w0[2], w0[3]), q1 = make_uint4(w1[0], w1[1], w1[2], w1[3]),
+                          q2 = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+              *reinterpret_cast<uint4*>(stage + off) = q0;
+              *reinterpret_cast<uint4*>(stage + kTileA + off) = q1;
+              *reinterpret_cast<uint4*>(stage + 2 * kTileA + off) = q2;
+              if (saveA) {
+                *reinterpret_cast<uint4*>(agl + off) = q0;
+                *reinterpret_cast<uint4*>(agl + kTileA + off) = q1;
+                *reinterpret_cast<uint4*>(agl + 2 * kTileA + off) = q2;
+              }
             }
+            if (saveA) tc::fence_async_global();  // read back by the later passes' bulk copies
           }
           // ---- B: row nu, elements mu0 + 2 lane, + 1: P[fn[mu]][fn[nu]] (symmetric P); a
           //      warp's rows (at most 8) loaded together, row offsets from shared memory ----
@@ -736,9 +761,19 @@ __global__ void __launch_bounds__(kT, 1)
           const int kw = kc % kWinChunks;  // chunk within the window
           if (tid == 0) {
             tc::fence_after_sync();
-            issue_density_chunk(tmem, tc::smem_u32(stage), N, kw == 0);
-            tc::mma_commit(&mbar[st]);
+            bool aok = true;
+            if (reuseA) {
+              aok = tc::mbar_wait_bounded(&afull[st], (aphase >> st) & 1u, kWaitLimitNs);
+              if (!aok) {  // report and leave after this block; the copy lands before the CTA exits
+                atomicExch(err, kErrTimeout);
+                s_abort = 1;
+                tc::mbar_wait_bounded(&afull[st], (aphase >> st) & 1u, kWaitLimitNs);
+              }
+            }
+            if (aok) issue_density_chunk(tmem, tc::smem_u32(stage), N, kw == 0);
+            tc::mma_commit(&mbar[st]);  // (with no MMAs issued it arrives at once)
           }
+          if (reuseA) aphase ^= 1u << st;
           pend |= 1u << st;
           ++gc;
           if ((kc % kWinChunks) != kWinChunks - 1 && kc != nkc - 1) continue;
