@@ -102,22 +102,41 @@ __global__ void __launch_bounds__(256) mirror_batch_kernel(const __grid_constant
   for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) M[(long)j * n + i] = M[(long)i * n + j];
 }
 
-// one CTA per build: E_xc and N_el from the per-block partial sums, in the order of
-// sum_partials_kernel
-__global__ void __launch_bounds__(256) sums_batch_kernel(const __grid_constant__ SmallBatch sb) {
-  __shared__ double red[256];
+// one CTA of 1024 threads per build: E_xc and N_el from the per-block partial sums (both
+// components at once, eight loads in flight per thread, then a tree over the threads)
+__global__ void __launch_bounds__(1024) sums_batch_kernel(const __grid_constant__ SmallBatch sb) {
+  __shared__ double red[2][1024];
   const SmallItem& I = sb.it[blockIdx.x];
-  for (int c = 0; c < 2; ++c) {
-    double a = 0.0;
-    for (int i = threadIdx.x; i < I.nparts; i += blockDim.x) a += I.partials[(long)c * I.nparts + i];
-    red[threadIdx.x] = a;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
+  const int n = I.nparts, t = threadIdx.x;
+  double a[2][8];
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[c][u] = 0.0;
+  for (int i0 = 0; i0 < n; i0 += 8 * 1024) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int i = i0 + u * 1024 + t;
+      if (i < n) {
+        a[0][u] += I.partials[i];
+        a[1][u] += I.partials[(long)n + i];
+      }
     }
-    if (threadIdx.x == 0) I.exc_nel[c] = red[0];
+  }
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+    red[c][t] = ((a[c][0] + a[c][1]) + (a[c][2] + a[c][3])) + ((a[c][4] + a[c][5]) + (a[c][6] + a[c][7]));
+  __syncthreads();
+  for (int w = 512; w > 0; w >>= 1) {
+    if (t < w) {
+      red[0][t] += red[0][t + w];
+      red[1][t] += red[1][t + w];
+    }
     __syncthreads();
+  }
+  if (t == 0) {
+    I.exc_nel[0] = red[0][0];
+    I.exc_nel[1] = red[1][0];
   }
 }
 
@@ -301,7 +320,7 @@ static xcgpu_status small_launches(Ctx* c, const std::vector<MixedWork>& work, b
       if (ncol > 0) split_zero_batch_kernel<<<(unsigned)ncol, 256, 0, c->stream>>>(sb);
     } else {
       if (ncol > 0) mirror_batch_kernel<<<(unsigned)ncol, 256, 0, c->stream>>>(sb);
-      sums_batch_kernel<<<(unsigned)sb.n, 256, 0, c->stream>>>(sb);
+      sums_batch_kernel<<<(unsigned)sb.n, 1024, 0, c->stream>>>(sb);
     }
     xcgpu_status st = c->check_launch(before ? "split_zero_batch_kernel" : "mirror_batch_kernel / sums_batch_kernel");
     if (st) return st;

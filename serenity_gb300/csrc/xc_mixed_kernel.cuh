@@ -138,6 +138,24 @@ __device__ __forceinline__ ShellRec load_rec(const ShellRec* p) {
   return r;
 }
 
+// FP32 -> FP64 by the IEEE 754 bit layouts on the integer pipe (exact; zeros, subnormals,
+// infinities and NaNs take the conversion instruction): GB300 converts on its FP64 pipe,
+// at 1/64 of the FP32 rate, and every Vxc element of a block passes through here
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  return __longlong_as_double((long long)(((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                                          ((uint64_t)(u & 0x7fffffu) << 29)));
+}
+
+// s += x for an FP32-pair running sum (two-sum; the pair keeps ~44 bits over a few dozen
+// terms, where an FP64 sum would cost FP64 instructions)
+__device__ __forceinline__ void f2_add1(F2& s, float x) {
+  const float t = __fadd_rn(s.h, x), bp = __fsub_rn(t, s.h);
+  s.l = __fadd_rn(s.l, __fadd_rn(__fsub_rn(s.h, __fsub_rn(t, bp)), __fsub_rn(x, bp)));
+  s.h = t;
+}
+
 __device__ __forceinline__ bool wait_or_abort(uint64_t* mbar, uint32_t parity, int* err) {
   const bool ok = tc::mbar_wait_bounded(mbar, parity, kWaitLimitNs);
   if (!ok) atomicExch(err, kErrTimeout);
@@ -438,6 +456,7 @@ __global__ void __launch_bounds__(kT, 1)
   __shared__ uint32_t tmem_slot;
   __shared__ int s_block, s_abort, s_smask;
   __shared__ int s_next[4];  // basis phase: next shell of the block, per 32-point group
+  __shared__ Pt s_pt[HAS_D ? 128 : 1];  // basis phase: the block's points as FP32 pairs (FP64 split once per point)
   __shared__ double s_part[4][kQ - 1][128];  // density: partial sums of a point's threads
   __shared__ unsigned s_amax[128];           // per point: largest |phi| (FP32 bits)
   __shared__ float s_bscale[kNT];            // per function nu of the pass: scale of its column of P
@@ -510,7 +529,7 @@ __global__ void __launch_bounds__(kT, 1)
           if (rok && n < nb && (a < bb || n >= row)) {
             const float f1 = __fmul_rn(__fadd_rn(p0[c], pr[c]), __fmul_rn(sPm, sGn[n]));
             const float f2 = __fmul_rn(__fadd_rn(q0[c], qr[c]), __fmul_rn(sGm, sPn[n]));
-            atomicAdd(Vrow + (long)__ldg(fnb + 128 * bb + n) * nbf_b, (double)__fadd_rn(f1, f2));
+            atomicAdd(Vrow + (long)__ldg(fnb + 128 * bb + n) * nbf_b, f32_to_f64(__fadd_rn(f1, f2)));
           }
         }
       }
@@ -546,7 +565,7 @@ __global__ void __launch_bounds__(kT, 1)
       for (int c = 0; c < 32; ++c) {
         const int n = c0 + c;
         if (n < nact_b && n >= row)
-          atomicAdd(Vrow + (long)__ldg(fnb + n) * nbf_b, (double)__fadd_rn(T[row * 129 + n], T[n * 129 + row]));
+          atomicAdd(Vrow + (long)__ldg(fnb + n) * nbf_b, f32_to_f64(__fadd_rn(T[row * 129 + n], T[n * 129 + row])));
       }
     }
   };
@@ -596,9 +615,11 @@ __global__ void __launch_bounds__(kT, 1)
         continue;
       }
       const bool live = p < npts;
+      if (quarter == 0) s_pt[p] = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
+      __syncthreads();
     // ---- 1. basis values (and gradients) of the block, largest |phi| per point ----
     {
-      const Pt pt = make_pt(P.xyz + 3 * (first + (live ? p : 0)));
+      const Pt pt = s_pt[p];
       const float expthr = (float)P.exponent_threshold, thr = (float)P.radial_threshold;
       float* const col = my + p;
       float vmax = 0.f;
@@ -649,7 +670,8 @@ __global__ void __launch_bounds__(kT, 1)
     for (int s = 0; s < nspin; ++s) {
       const uint2* __restrict__ Psl = I.Psl + (long)s * nbf * nbf;
       const float* __restrict__ Pcs = I.Pcs + (long)s * nbf;
-      double r_acc = 0.0, g_acc[3] = {0.0, 0.0, 0.0};
+      // this thread's share of rho and grad rho over its columns, summed in FP32 pairs
+      F2 r2{0.f, 0.f}, g2[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
       // the basis values' low parts enter through their own FP32 sum: added into rr, each
       // (about an ulp of rr) would mostly round away, a systematic loss of the corrections
       float r_lo = 0.f;
@@ -675,6 +697,26 @@ __global__ void __launch_bounds__(kT, 1)
           }
           uint8_t* const stage = sm + st * kDStageBytes;
           const int mu0 = kc * 64;
+          // B's elements (a warp's rows, at most 8, row offsets from shared memory) are
+          // loaded first, so their latency overlaps the A slices' loads and arithmetic
+          // (measured faster although the registers then spill a few values)
+          const int k0 = 2 * lane;
+          uint2 ea[kNT / kWarps], eb[kNT / kWarps];
+          {
+            const int muA = mu0 + k0, muB = muA + 1;
+            const long cA = muA < nact ? (long)__ldg(fn + muA) : -1;
+            const long cB = muB < nact ? (long)__ldg(fn + muB) : -1;
+#pragma unroll
+            for (int k = 0; k < kNT / kWarps; ++k) {
+              const int row = warp + k * kWarps;
+              ea[k] = eb[k] = make_uint2(0u, 0u);
+              if (row < nnu) {
+                const uint2* prow = Psl + s_rowoff[row];
+                if (cA >= 0) ea[k] = __ldg(prow + cA);
+                if (cB >= 0) eb[k] = __ldg(prow + cB);
+              }
+            }
+          }
           // A of chunk kc is the same in every pass and for every spin: in the two-spin
           // kernels it is sliced in the first pass of the first spin, kept in the scratch
           // after the planes and copied back into the stage by the later passes (in the
@@ -727,33 +769,15 @@ __global__ void __launch_bounds__(kT, 1)
             }
             if (saveA) tc::fence_async_global();  // read back by the later passes' bulk copies
           }
-          // ---- B: row nu, elements mu0 + 2 lane, + 1: P[fn[mu]][fn[nu]] (symmetric P); a
-          //      warp's rows (at most 8) loaded together, row offsets from shared memory ----
-          {
-            const int k0 = 2 * lane;
-            const int muA = mu0 + k0, muB = muA + 1;
-            const long cA = muA < nact ? (long)__ldg(fn + muA) : -1;
-            const long cB = muB < nact ? (long)__ldg(fn + muB) : -1;
-            uint2 ea[kNT / kWarps], eb[kNT / kWarps];
+          // ---- B: row nu, elements mu0 + 2 lane, + 1: P[fn[mu]][fn[nu]] (symmetric P), loaded above ----
 #pragma unroll
-            for (int k = 0; k < kNT / kWarps; ++k) {
-              const int row = warp + k * kWarps;
-              ea[k] = eb[k] = make_uint2(0u, 0u);
-              if (row < nnu) {
-                const uint2* prow = Psl + s_rowoff[row];
-                if (cA >= 0) ea[k] = __ldg(prow + cA);
-                if (cB >= 0) eb[k] = __ldg(prow + cB);
-              }
-            }
-#pragma unroll
-            for (int k = 0; k < kNT / kWarps; ++k) {
-              const int row = warp + k * kWarps;
-              if (row < N) {
-                const uint32_t off = tc::swz_offset_h(row, k0);
-                *reinterpret_cast<uint32_t*>(stage + 3 * kTileA + off) = (ea[k].x & 0xFFFFu) | (eb[k].x << 16);
-                *reinterpret_cast<uint32_t*>(stage + 4 * kTileA + off) = (ea[k].x >> 16) | (eb[k].x & 0xFFFF0000u);
-                *reinterpret_cast<uint32_t*>(stage + 5 * kTileA + off) = (ea[k].y & 0xFFFFu) | (eb[k].y << 16);
-              }
+          for (int k = 0; k < kNT / kWarps; ++k) {
+            const int row = warp + k * kWarps;
+            if (row < N) {
+              const uint32_t off = tc::swz_offset_h(row, k0);
+              *reinterpret_cast<uint32_t*>(stage + 3 * kTileA + off) = (ea[k].x & 0xFFFFu) | (eb[k].x << 16);
+              *reinterpret_cast<uint32_t*>(stage + 4 * kTileA + off) = (ea[k].x >> 16) | (eb[k].x & 0xFFFF0000u);
+              *reinterpret_cast<uint32_t*>(stage + 5 * kTileA + off) = (ea[k].y & 0xFFFFu) | (eb[k].y << 16);
             }
           }
           tc::fence_async_smem();
@@ -820,11 +844,11 @@ __global__ void __launch_bounds__(kT, 1)
                     }
                   }
                 }
-                r_acc += (double)rr;
+                f2_add1(r2, rr);
                 if (DERIV) {
-                  g_acc[0] += (double)gx;
-                  g_acc[1] += (double)gy;
-                  g_acc[2] += (double)gz;
+                  f2_add1(g2[0], gx);
+                  f2_add1(g2[1], gy);
+                  f2_add1(g2[2], gz);
                 }
               }
             }
@@ -833,7 +857,10 @@ __global__ void __launch_bounds__(kT, 1)
           __syncthreads();  // the accumulators and s_bscale are reused
         }
       }
-      r_acc += (double)r_lo;
+      double r_acc = ((double)r2.h + (double)r2.l) + (double)r_lo;
+      double g_acc[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) g_acc[k] = (double)g2[k].h + (double)g2[k].l;
       // combine the kQ partial sums of each point
       if (quarter > 0) {
         s_part[0][quarter - 1][p] = r_acc;
@@ -1255,7 +1282,7 @@ __global__ void __launch_bounds__(kT, 1)
           double* const Vc = I.V + (long)__ldg(fn + n) * nbf_b;
 #pragma unroll 1
           for (int m = lane; m <= n; m += 32)
-            atomicAdd(Vc + __ldg(fn + m), (double)__fadd_rn(Ts[m * ldT + n], Ts[n * ldT + m]));
+            atomicAdd(Vc + __ldg(fn + m), f32_to_f64(__fadd_rn(Ts[m * ldT + n], Ts[n * ldT + m])));
         }
       }
       __syncthreads();  // the shared memory is reused by the next block
