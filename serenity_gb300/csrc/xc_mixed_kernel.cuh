@@ -697,26 +697,6 @@ __global__ void __launch_bounds__(kT, 1)
           }
           uint8_t* const stage = sm + st * kDStageBytes;
           const int mu0 = kc * 64;
-          // B's elements (a warp's rows, at most 8, row offsets from shared memory) are
-          // loaded first, so their latency overlaps the A slices' loads and arithmetic
-          // (measured faster although the registers then spill a few values)
-          const int k0 = 2 * lane;
-          uint2 ea[kNT / kWarps], eb[kNT / kWarps];
-          {
-            const int muA = mu0 + k0, muB = muA + 1;
-            const long cA = muA < nact ? (long)__ldg(fn + muA) : -1;
-            const long cB = muB < nact ? (long)__ldg(fn + muB) : -1;
-#pragma unroll
-            for (int k = 0; k < kNT / kWarps; ++k) {
-              const int row = warp + k * kWarps;
-              ea[k] = eb[k] = make_uint2(0u, 0u);
-              if (row < nnu) {
-                const uint2* prow = Psl + s_rowoff[row];
-                if (cA >= 0) ea[k] = __ldg(prow + cA);
-                if (cB >= 0) eb[k] = __ldg(prow + cB);
-              }
-            }
-          }
           // A of chunk kc is the same in every pass and for every spin: in the two-spin
           // kernels it is sliced in the first pass of the first spin, kept in the scratch
           // after the planes and copied back into the stage by the later passes (in the
@@ -769,15 +749,33 @@ __global__ void __launch_bounds__(kT, 1)
             }
             if (saveA) tc::fence_async_global();  // read back by the later passes' bulk copies
           }
-          // ---- B: row nu, elements mu0 + 2 lane, + 1: P[fn[mu]][fn[nu]] (symmetric P), loaded above ----
+          // ---- B: row nu, elements mu0 + 2 lane, + 1: P[fn[mu]][fn[nu]] (symmetric P); a
+          //      warp's rows (at most 8) loaded together, row offsets from shared memory ----
+          {
+            const int k0 = 2 * lane;
+            const int muA = mu0 + k0, muB = muA + 1;
+            const long cA = muA < nact ? (long)__ldg(fn + muA) : -1;
+            const long cB = muB < nact ? (long)__ldg(fn + muB) : -1;
+            uint2 ea[kNT / kWarps], eb[kNT / kWarps];
 #pragma unroll
-          for (int k = 0; k < kNT / kWarps; ++k) {
-            const int row = warp + k * kWarps;
-            if (row < N) {
-              const uint32_t off = tc::swz_offset_h(row, k0);
-              *reinterpret_cast<uint32_t*>(stage + 3 * kTileA + off) = (ea[k].x & 0xFFFFu) | (eb[k].x << 16);
-              *reinterpret_cast<uint32_t*>(stage + 4 * kTileA + off) = (ea[k].x >> 16) | (eb[k].x & 0xFFFF0000u);
-              *reinterpret_cast<uint32_t*>(stage + 5 * kTileA + off) = (ea[k].y & 0xFFFFu) | (eb[k].y << 16);
+            for (int k = 0; k < kNT / kWarps; ++k) {
+              const int row = warp + k * kWarps;
+              ea[k] = eb[k] = make_uint2(0u, 0u);
+              if (row < nnu) {
+                const uint2* prow = Psl + s_rowoff[row];
+                if (cA >= 0) ea[k] = __ldg(prow + cA);
+                if (cB >= 0) eb[k] = __ldg(prow + cB);
+              }
+            }
+#pragma unroll
+            for (int k = 0; k < kNT / kWarps; ++k) {
+              const int row = warp + k * kWarps;
+              if (row < N) {
+                const uint32_t off = tc::swz_offset_h(row, k0);
+                *reinterpret_cast<uint32_t*>(stage + 3 * kTileA + off) = (ea[k].x & 0xFFFFu) | (eb[k].x << 16);
+                *reinterpret_cast<uint32_t*>(stage + 4 * kTileA + off) = (ea[k].x >> 16) | (eb[k].x & 0xFFFF0000u);
+                *reinterpret_cast<uint32_t*>(stage + 5 * kTileA + off) = (ea[k].y & 0xFFFFu) | (eb[k].y << 16);
+              }
             }
           }
           tc::fence_async_smem();
