@@ -181,9 +181,10 @@ xcgpu_status xcgpu_density(xcgpu_plan* plan, int nspin, const double* P, double*
  * scratch lives in a fixed 64 MiB static device array that every GPU loading the library
  * holds until exit, so a block needing more (more than ~16 000 active functions) is
  * rejected with XCGPU_ERR_BUDGET.  P, rho, grad (may be NULL) are device pointers; the call
- * synchronises the context stream.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
- * share the array, so calls that overlap on the GPU race. */
+ * synchronises the context stream.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress, which allocates nothing), so a reset device or another context gets
+ * the right address; make the first call on a device before any stream capture (it may load
+ * the module).  All calls share the array, so calls that overlap on the GPU race. */
 xcgpu_status xcgpu_density_fp64_noalloc(xcgpu_plan* plan, int nspin, const double* P, double* rho, double* grad);
 /* FunctionalLibrary::calcData(GRADIENTS, f, ., order 1) (FunctionalLibrary.cpp:40-71,
  * XCFun.cpp:39-158): epuv (energy per volume), dF/drho and, for GGAs, dF/d(grad rho).

@@ -62,10 +62,13 @@ def test_mixed_adder_vs_fp64(ctx):
     assert np.abs(Fmx - F64).max() <= 1.5e-6 * max(1.0, np.abs(F64).max())
 
 
+# def2-SVP at the benchmark's 1e-7 (measured: dE_xc <= 4.7e-8, max|dV| <= 9.2e-8); the
+# def2-TZVP tetramer on this coarse grid reaches max|dV| 3.1e-7 (dE_xc <= 6e-8), so its bound is
+# looser (on the 99 x 434 grid the benchmark-tolerance test below holds TZVP to 1e-7)
 @pytest.mark.parametrize("func,unrestricted,basis,spherical,etol,vtol", [
-    ("LDA", False, "DEF2-SVP", True, 1e-7, 1.5e-7), ("PBE", False, "DEF2-SVP", True, 1e-7, 1.5e-7),
-    ("BLYP", False, "DEF2-SVP", True, 1e-7, 1.5e-7), ("PBE", True, "DEF2-SVP", True, 1e-7, 1.5e-7),
-    ("PBE", False, "DEF2-TZVP", True, 3e-7, 4e-7), ("PBE", False, "DEF2-TZVP", False, 3e-7, 4e-7)])
+    ("LDA", False, "DEF2-SVP", True, 1e-7, 1e-7), ("PBE", False, "DEF2-SVP", True, 1e-7, 1e-7),
+    ("BLYP", False, "DEF2-SVP", True, 1e-7, 1e-7), ("PBE", True, "DEF2-SVP", True, 1e-7, 1e-7),
+    ("PBE", False, "DEF2-TZVP", True, 1e-7, 4e-7), ("PBE", False, "DEF2-TZVP", False, 1e-7, 4e-7)])
 def test_mixed_vxc_vs_oracle(ctx, func, unrestricted, basis, spherical, etol, vtol):
     from serenity_gb300 import xcgpu
     w, pts, wts = _case(func, unrestricted, basis=basis, spherical=spherical)
@@ -73,6 +76,8 @@ def test_mixed_vxc_vs_oracle(ctx, func, unrestricted, basis, spherical, etol, vt
     P = w.density()
     V, exc, nel = plan.vxc(func, P, precision=xcgpu.PREC_MIXED)
     rV, rexc, rnel = po.Basis(w.shells).vxc(pts, wts, func, P)
+    print("mixed vs oracle %s %s %s: dExc %.3e max dV %.3e" % (func, basis, "U" if unrestricted else "R",
+                                                               exc - rexc, np.abs(V - rV).max()))
     assert abs(exc - rexc) <= etol, abs(exc - rexc)
     assert abs(nel - rnel) <= 1e-8 * rnel
     assert np.abs(V - rV).max() <= vtol, np.abs(V - rV).max()
