@@ -240,39 +240,15 @@ __device__ __forceinline__ const MxItem& locate(const MxBatch& bt, int gb, int& 
 constexpr uint32_t kDStageBytes = 6 * kTileA;  // A slices 0-2, B slices 0-2 (64 FP16 wide)
 constexpr int kWinChunks = 2;                  // density: chunks per exact window (128 functions)
 
-// Fixed-point slices of a value v scaled into (-2^R, 2^R): v = s0 + s1 / 2^B + s2 / 2^(2B)
-// + r with integers s0 in [-2^R, 2^R], s1, s2 in [-2^(B-1), 2^(B-1)], |r| <= 2^-(2B+1);
-// every step is exact (each remainder is a multiple of the unit of v) except the
-// rounding of s2.  Stored pre-scaled, (s0, s1 / 2^B, s2 / 2^(2B)), in FP16, which holds
-// each exactly (the smallest in its subnormal range).
+// Fixed-point slices of a value v = vh + vl (|vl| at most about an ulp of vh) scaled into
+// (-2^R, 2^R): v = s0 + s1 / 2^B + s2 / 2^(2B) + r with integers s0 in [-2^R, 2^R], s1, s2
+// in [-2^(B-1), 2^(B-1)], |r| <= 2^-(2B+1); every step is exact (each remainder is a
+// multiple of the unit of v; the remainder after s0 takes vl in) except the rounding of s2.
+// Returned pre-scaled, (s0, s1 / 2^B, s2 / 2^(2B)), as FP32 values that FP16 holds exactly
+// (the smallest in its subnormal range), packed two to a word by pack_h2.
 //   adder   R = 7, B = 8: 24 bits; leading products below 2^14, exact sums over 1024
 //   (the density uses density_slices below)
-template <int R, int B>
-__device__ __forceinline__ void fixed_slices(float v, uint16_t& h0, uint16_t& h1, uint16_t& h2) {
-  constexpr float up = (float)(1 << B), down = 1.f / (float)(1 << B), down2 = down * down;
-  const float s0 = rintf(v);
-  const float r1 = __fmul_rn(__fsub_rn(v, s0), up);
-  const float s1 = rintf(r1);
-  const float s2 = rintf(__fmul_rn(__fsub_rn(r1, s1), up));
-  h0 = __half_as_ushort(__float2half_rn(s0));
-  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, down)));
-  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, down2)));
-}
-
-// fixed_slices of v = vh + vl (|vl| at most about an ulp of vh): the remainder after s0
-// takes vl in
-template <int R, int B>
-__device__ __forceinline__ void fixed_slices2(float vh, float vl, uint16_t& h0, uint16_t& h1, uint16_t& h2) {
-  constexpr float up = (float)(1 << B), down = 1.f / (float)(1 << B), down2 = down * down;
-  const float s0 = rintf(vh);
-  const float r1 = __fmul_rn(__fadd_rn(__fsub_rn(vh, s0), vl), up);
-  const float s1 = rintf(r1);
-  const float s2 = rintf(__fmul_rn(__fsub_rn(r1, s1), up));
-  h0 = __half_as_ushort(__float2half_rn(s0));
-  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, down)));
-  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, down2)));
-}
-
+//
 // Density slices of v = vh + vl (|vl| at most about an ulp of vh) scaled into (-256, 256):
 // v = s0 + s1 / 2^9 + s2 / 2^18 + r, s0 in [-256, 256], s1, s2 in [-256, 256], |r| <
 // 2^-18; stored as FP16 (s0, s1 / 2^9, s2 / 2^9), all exact and (but zero) normal
@@ -281,15 +257,27 @@ __device__ __forceinline__ void fixed_slices2(float vh, float vl, uint16_t& h0, 
 // (Connolly, Higham & Mary, SIAM J. Sci. Comput. 43 (2021) A1508): an s function has the
 // same value at every point of a radial shell of its atom (and at every atom of the
 // element), where round-to-nearest would repeat one error; the dither makes it zero-mean.
-__device__ __forceinline__ void density_slices(float vh, float vl, float u, uint16_t& h0, uint16_t& h1,
-                                               uint16_t& h2) {
-  const float s0 = rintf(vh);
-  const float r1 = __fmul_rn(__fadd_rn(__fsub_rn(vh, s0), vl), 512.f);
+__device__ __forceinline__ void density_slices(float vh, float vl, float u, float& f0, float& f1, float& f2) {
+  f0 = rintf(vh);
+  const float r1 = __fmul_rn(__fadd_rn(__fsub_rn(vh, f0), vl), 512.f);
   const float s1 = rintf(r1);
-  const float s2 = floorf(__fadd_rn(__fmul_rn(__fsub_rn(r1, s1), 512.f), u));
-  h0 = __half_as_ushort(__float2half_rn(s0));
-  h1 = __half_as_ushort(__float2half_rn(__fmul_rn(s1, 1.f / 512.f)));
-  h2 = __half_as_ushort(__float2half_rn(__fmul_rn(s2, 1.f / 512.f)));
+  f2 = __fmul_rn(floorf(__fadd_rn(__fmul_rn(__fsub_rn(r1, s1), 512.f), u)), 1.f / 512.f);
+  f1 = __fmul_rn(s1, 1.f / 512.f);
+}
+
+template <int R, int B>
+__device__ __forceinline__ void fixed_slices2(float vh, float vl, float& f0, float& f1, float& f2) {
+  constexpr float up = (float)(1 << B), down = 1.f / (float)(1 << B), down2 = down * down;
+  f0 = rintf(vh);
+  const float r1 = __fmul_rn(__fadd_rn(__fsub_rn(vh, f0), vl), up);
+  const float s1 = rintf(r1);
+  f2 = __fmul_rn(rintf(__fmul_rn(__fsub_rn(r1, s1), up)), down2);
+  f1 = __fmul_rn(s1, down);
+}
+// two FP16-exact values as one 32-bit word (a in the low half): one packing conversion
+__device__ __forceinline__ uint32_t pack_h2(float a, float b) {
+  const __half2 h = __floats2half2_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&h);
 }
 
 // dither of point g (global index): a hash to [0, 1); a function mu adds mu times the
@@ -726,14 +714,14 @@ __global__ void __launch_bounds__(kT, 1)
               uint32_t w0[4], w1[4], w2[4];
 #pragma unroll
               for (int e = 0; e < 8; e += 2) {
-                uint16_t a0, a1, a2, b0, b1, b2;
+                float a0, a1, a2, b0, b1, b2;
                 const int k = 8 * jj + e, mu = mu0 + 16 * quarter + k;
                 density_slices(__fmul_rn(av[k], inva), __fmul_rn(al[k], inva), function_dither(up, mu), a0, a1, a2);
-                density_slices(__fmul_rn(av[k + 1], inva), __fmul_rn(al[k + 1], inva), function_dither(up, mu + 1), b0,
-                               b1, b2);
-                w0[e >> 1] = (uint32_t)a0 | ((uint32_t)b0 << 16);
-                w1[e >> 1] = (uint32_t)a1 | ((uint32_t)b1 << 16);
-                w2[e >> 1] = (uint32_t)a2 | ((uint32_t)b2 << 16);
+                density_slices(__fmul_rn(av[k + 1], inva), __fmul_rn(al[k + 1], inva), function_dither(up, mu + 1),
+                                 b0, b1, b2);
+                w0[e >> 1] = pack_h2(a0, b0);
+                w1[e >> 1] = pack_h2(a1, b1);
+                w2[e >> 1] = pack_h2(a2, b2);
               }
               const uint32_t off = (uint32_t)(p * 128 + ((j ^ (p & 7)) << 4));
               const uint4 q0 = make_uint4(w0[0], w0[1], w0[2], w0[3]), q1 = make_uint4(w1[0], w1[1], w1[2], w1[3]),
@@ -977,7 +965,7 @@ __global__ void __launch_bounds__(kT, 1)
           float scale, inv;
           fixed_scale<7>(mx, scale, inv);
           if (lane == 0) scl[o * rows_pad + m] = scale;
-          uint16_t h[3][4];
+          float h[3][4];
           fixed_slices2<7, 8>(__fmul_rn(x.x, inv), __fmul_rn(xl.x, inv), h[0][0], h[1][0], h[2][0]);
           fixed_slices2<7, 8>(__fmul_rn(x.y, inv), __fmul_rn(xl.y, inv), h[0][1], h[1][1], h[2][1]);
           fixed_slices2<7, 8>(__fmul_rn(x.z, inv), __fmul_rn(xl.z, inv), h[0][2], h[1][2], h[2][2]);
@@ -995,8 +983,7 @@ __global__ void __launch_bounds__(kT, 1)
           }
 #pragma unroll
           for (int i = 0; i < 3; ++i)
-            *reinterpret_cast<uint2*>(tb + i * sstride + off) = make_uint2(
-                (uint32_t)h[i][0] | ((uint32_t)h[i][1] << 16), (uint32_t)h[i][2] | ((uint32_t)h[i][3] << 16));
+            *reinterpret_cast<uint2*>(tb + i * sstride + off) = make_uint2(pack_h2(h[i][0], h[i][1]), pack_h2(h[i][2], h[i][3]));
         }
       }
       if (tiles_in_smem || tiles_mid) tc::fence_async_smem();  // these generic writes are read by the MMAs below
