@@ -614,8 +614,8 @@ static xcgpu_status stage_adder(xcgpu_plan* P, int nspin, const double* v, const
     const int b0 = P->chunk_bounds[k], b1 = P->chunk_bounds[k + 1];
     const long* so = P->w_slab.as<long>() + b0;
     XC_TRY(fp64_eval_chunk(c, P->basis->dev, P->dev, b0, b1, so, scr, 1));
-    XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, so, scr, nspin, v,
-                            g, skip, F));
+    XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, b1, so, scr, nspin,
+                            v, g, skip, F));
   }
   return XCGPU_OK;
 }
@@ -779,7 +779,7 @@ static xcgpu_status run_builds(Ctx* c, std::vector<BuildReq>& reqs, int precisio
         XC_TRY(launch_functional_range(c, r.func, r.nspin, n, kSkipBlock, p0, p1, w.rho, w.grad, w.epuv, w.dfdrho,
                                        w.dfdgrad, P->dev.w, w.partials, w.fskip));
         XC_TRY(launch_block_skip_flags_range(c, P->dev, r.nspin, w.dfdrho, w.dfdgrad, r.thr, w.skip, b0, b1));
-        XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, so, scr,
+        XC_TRY(fp64_adder_chunk(c, P->dev, P->d_work.as<int>(), P->work_off[b0], P->work_off[b1], b0, b1, so, scr,
                                 r.nspin, w.dfdrho, w.dfdgrad, w.skip, r.V));
       }
       const int nparts = (int)((n + 127) / 128);

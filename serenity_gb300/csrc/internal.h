@@ -238,8 +238,9 @@ xcgpu_status launch_functional(Ctx* c, int func, int nspin, long n, int skip_blo
                                bool pair = false /*restricted PBE in FP32 pairs, as the mixed build*/);
 xcgpu_status launch_block_skip_flags(Ctx* c, const DevPlan& P, int nspin, const double* v, const double* g,
                                      double thr, unsigned char* skip /*nspin*nblocks*/);
+// forms G over the chunk's gradient planes, then adds every tile pair of [w0, w1)
 xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0, long w1, int chunk_b0,
-                              const long* slab_off, const double* scratch, int nspin, const double* v,
+                              int chunk_b1, const long* slab_off, double* scratch, int nspin, const double* v,
                               const double* g, const unsigned char* skip, double* F);
 xcgpu_status launch_axpy(Ctx* c, long n, const double* x, double* y);  // y += x
 xcgpu_status fp64_xc_gradient_chunk(Ctx* c, const DevBasis& B, const DevPlan& P, int b0, int b1, const long* slab_off,

@@ -612,9 +612,6 @@ __global__ void __launch_bounds__(256) fp64_adder_kernel(DevPlan P, const int* _
   const int* fn = P.fn_list + P.fn_off[b];
   const double* slab = scratch + slab_off[b - chunk_b0];
   const int ci = min(kAT, nact - ti * kAT), cj = min(kAT, nact - tj * kAT);
-  const double* vs = v + (long)s * P.npoints + first;
-  const double* gs = g ? g + (long)s * 3 * P.npoints + first : nullptr;
-  const long gstride = P.npoints;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   double acc[4][4];
 #pragma unroll
@@ -631,17 +628,8 @@ __global__ void __launch_bounds__(256) fp64_adder_kernel(DevPlan P, const int* _
       if (which == 0) {
         if (r < ci && pk < n) val = slab[(long)(ti * kAT + r) * kBlockPoints + pk];
         Pi[r * kAPad + q] = val;
-      } else {
-        if (r < cj && pk < n) {
-          const int f = tj * kAT + r;
-          const double w = P.w[first + pk];
-          double gg = 0.5 * vs[pk] * slab[(long)f * kBlockPoints + pk];
-          if (gs)
-            gg += gs[pk] * slab[(long)(nact + f) * kBlockPoints + pk] +
-                  gs[gstride + pk] * slab[(long)(2 * nact + f) * kBlockPoints + pk] +
-                  gs[2 * gstride + pk] * slab[(long)(3 * nact + f) * kBlockPoints + pk];
-          val = gg * w;
-        }
+      } else {  // G of spin s, formed once per block into the slab's plane 1 + s
+        if (r < cj && pk < n) val = slab[(long)((1 + s) * nact + tj * kAT + r) * kBlockPoints + pk];
         Gj[r * kAPad + q] = val;
       }
     }
@@ -678,9 +666,55 @@ __global__ void __launch_bounds__(256) fp64_adder_kernel(DevPlan P, const int* _
   }
 }
 
+// G = w (v/2 phi + g . grad phi) of every active function of the blocks [b0, b0 + grid)
+// at their points, per spin, written over the slab's gradient planes (plane 1 + s; the
+// density is done with them): formed once per block instead of once per tile pair
+__global__ void __launch_bounds__(128) fp64_form_g_kernel(DevPlan P, int b0, const long* __restrict__ slab_off,
+                                                          double* __restrict__ scratch, int nspin,
+                                                          const double* __restrict__ v, const double* __restrict__ g) {
+  const int b = b0 + blockIdx.x;
+  const long first = (long)b * P.max_block;
+  const int n = (int)min((long)P.max_block, P.npoints - first);
+  const int nact = P.fn_off[b + 1] - P.fn_off[b];
+  double* slab = scratch + slab_off[blockIdx.x];
+  const int p = threadIdx.x;
+  if (p >= n) return;
+  const double w = P.w[first + p];
+  double a[2] = {0.0, 0.0}, gx[2] = {0.0, 0.0}, gy[2] = {0.0, 0.0}, gz[2] = {0.0, 0.0};
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    if (s >= nspin) break;
+    a[s] = 0.5 * v[(long)s * P.npoints + first + p];
+    if (g) {
+      gx[s] = g[((long)s * 3 + 0) * P.npoints + first + p];
+      gy[s] = g[((long)s * 3 + 1) * P.npoints + first + p];
+      gz[s] = g[((long)s * 3 + 2) * P.npoints + first + p];
+    }
+  }
+  for (int f = 0; f < nact; ++f) {
+    const double phi = slab[(long)f * kBlockPoints + p];
+    const double dx = slab[(long)(nact + f) * kBlockPoints + p];
+    const double dy = slab[(long)(2 * nact + f) * kBlockPoints + p];
+    const double dz = slab[(long)(3 * nact + f) * kBlockPoints + p];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      if (s >= nspin) break;
+      double gg = a[s] * phi;
+      if (g) gg += gx[s] * dx + gy[s] * dy + gz[s] * dz;
+      slab[(long)((1 + s) * nact + f) * kBlockPoints + p] = gg * w;
+    }
+  }
+}
+
 xcgpu_status fp64_adder_chunk(Ctx* c, const DevPlan& P, const int* work, long w0, long w1, int chunk_b0,
-                              const long* slab_off, const double* scratch, int nspin, const double* v,
+                              int chunk_b1, const long* slab_off, double* scratch, int nspin, const double* v,
                               const double* g, const unsigned char* skip, double* F) {
+  if (chunk_b1 > chunk_b0) {
+    KernelTimer kt(c, kAdder);
+    fp64_form_g_kernel<<<chunk_b1 - chunk_b0, kBlockPoints, 0, c->stream>>>(P, chunk_b0, slab_off, scratch, nspin, v, g);
+    xcgpu_status st = c->check_launch("fp64_form_g_kernel");
+    if (st) return st;
+  }
   if (w1 <= w0) return XCGPU_OK;
   const size_t smem = 2 * kAT * kAPad * sizeof(double);
   xcgpu_status st = c->cuda(cudaFuncSetAttribute(fp64_adder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
