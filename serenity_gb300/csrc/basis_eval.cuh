@@ -231,9 +231,16 @@ __device__ __forceinline__ void f2_acc(F2& s, F2 p) {  // s += p
 // radial value Rv times the exact angular factor to about 2^-44: every FP32 rounding of
 // the angular part would otherwise be one relative error repeated wherever the same
 // offset recurs (on a radial shell of the function's own atom, at every atom of an
-// element), a bias rather than noise.  The gradients stay FP32.
+// element), a bias rather than noise.
+// The gradients are FP32 numbers formed as d_i phi = R A_i + R' x_i S, with A_i the
+// FP32 sum of the coefficients times d_i of the monomials and S the angular sum above
+// (the value before R): R = Rv + Rl and R' = dR + dRl enter with their low parts, as on
+// a radial shell of the function's own atom they are one number each, and their FP32
+// roundings would be the same relative error of the gradient at every point of the
+// shell; what is left rounds differently from point to point.
 template <int L, int DERIV, class Emit>
-__device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, float dR, bool pure, Emit&& emit) {
+__device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, float Rl, float dR, float dRl,
+                                                   bool pure, Emit&& emit) {
   constexpr int NS = 2 * L + 1;
   constexpr cx::Table TS = cx::solid(L);
   constexpr cx::Table TC = cx::cartesian(L);
@@ -262,15 +269,12 @@ __device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, f
       F2 mono = px[a];
       if (b > 0) mono = a > 0 ? f2_mul(mono, py[b]) : py[b];
       if (c > 0) mono = (a > 0 || b > 0) ? f2_mul(mono, pz[c]) : pz[c];
+      // d_i of the monomial (FP32)
       float g0 = 0.f, g1 = 0.f, g2 = 0.f;
       if (DERIV >= 1) {
-        const float dmx = a > 0 ? float(a) * px[a > 0 ? a - 1 : 0].h * py[b].h * pz[c].h : 0.f;
-        const float dmy = b > 0 ? float(b) * px[a].h * py[b > 0 ? b - 1 : 0].h * pz[c].h : 0.f;
-        const float dmz = c > 0 ? float(c) * px[a].h * py[b].h * pz[c > 0 ? c - 1 : 0].h : 0.f;
-        const float md = mono.h * dR;
-        g0 = dmx * Rv + md * x.h;
-        g1 = dmy * Rv + md * y.h;
-        g2 = dmz * Rv + md * z.h;
+        g0 = a > 0 ? float(a) * px[a > 0 ? a - 1 : 0].h * py[b].h * pz[c].h : 0.f;
+        g1 = b > 0 ? float(b) * px[a].h * py[b > 0 ? b - 1 : 0].h * pz[c].h : 0.f;
+        g2 = c > 0 ? float(c) * px[a].h * py[b].h * pz[c > 0 ? c - 1 : 0].h : 0.f;
       }
       // (the coefficient tests below are on compile-time tables and fold away: a unit
       // coefficient multiplies nothing, a function's first term starts its sum)
@@ -311,7 +315,14 @@ __device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, f
           if (tl != 0.f) p.l = fmaf(tl, mono.h, p.l);
         }
         const F2 v = f2_mul1(p, Rv);
-        emit(k, v.h, v.l, t == 1.f ? g0 : t * g0, t == 1.f ? g1 : t * g1, t == 1.f ? g2 : t * g2);
+        if (DERIV >= 1) {
+          const float u = dR * p.h, ul = dRl * p.h;
+          const float a0 = t == 1.f ? g0 : t * g0, a1 = t == 1.f ? g1 : t * g1, a2 = t == 1.f ? g2 : t * g2;
+          emit(k, v.h, v.l, fmaf(Rv, a0, fmaf(u, x.h, fmaf(Rl, a0, ul * x.h))),
+               fmaf(Rv, a1, fmaf(u, y.h, fmaf(Rl, a1, ul * y.h))), fmaf(Rv, a2, fmaf(u, z.h, fmaf(Rl, a2, ul * z.h))));
+        } else {
+          emit(k, v.h, v.l, 0.f, 0.f, 0.f);
+        }
       }
     }
   }
@@ -319,26 +330,34 @@ __device__ __forceinline__ void shell_functions_px(F2 x, F2 y, F2 z, float Rv, f
 #pragma unroll
     for (int m = 0; m < NS; ++m) {
       const F2 v = f2_mul1(sv[m], Rv);
-      emit(m, v.h, v.l, sg[3 * m], sg[3 * m + 1], sg[3 * m + 2]);
+      if (DERIV >= 1) {
+        const float u = dR * sv[m].h, ul = dRl * sv[m].h;
+        const float* A = sg + 3 * m;
+        emit(m, v.h, v.l, fmaf(Rv, A[0], fmaf(u, x.h, fmaf(Rl, A[0], ul * x.h))),
+             fmaf(Rv, A[1], fmaf(u, y.h, fmaf(Rl, A[1], ul * y.h))),
+             fmaf(Rv, A[2], fmaf(u, z.h, fmaf(Rl, A[2], ul * z.h))));
+      } else {
+        emit(m, v.h, v.l, 0.f, 0.f, 0.f);
+      }
     }
   }
 }
 
 // dispatch on l <= MAXL at run time (the callers select MAXL from the basis)
 template <int DERIV, int MAXL, class Emit>
-__device__ __forceinline__ void shell_functions_px_l(int l, F2 x, F2 y, F2 z, float Rv, float dR, bool pure,
-                                                     Emit&& emit) {
+__device__ __forceinline__ void shell_functions_px_l(int l, F2 x, F2 y, F2 z, float Rv, float Rl, float dR, float dRl,
+                                                     bool pure, Emit&& emit) {
   switch (l) {
-    case 0: shell_functions_px<0, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 1: shell_functions_px<1, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 2: shell_functions_px<2, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-    case 3: shell_functions_px<3, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+    case 0: shell_functions_px<0, DERIV>(x, y, z, Rv, Rl, dR, dRl, pure, emit); break;
+    case 1: shell_functions_px<1, DERIV>(x, y, z, Rv, Rl, dR, dRl, pure, emit); break;
+    case 2: shell_functions_px<2, DERIV>(x, y, z, Rv, Rl, dR, dRl, pure, emit); break;
+    case 3: shell_functions_px<3, DERIV>(x, y, z, Rv, Rl, dR, dRl, pure, emit); break;
     default:
       if constexpr (MAXL >= 4) {
         switch (l) {
-          case 4: shell_functions_px<4, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-          case 5: shell_functions_px<5, DERIV>(x, y, z, Rv, dR, pure, emit); break;
-          case 6: shell_functions_px<6, DERIV>(x, y, z, Rv, dR, pure, emit); break;
+          case 4: shell_functions_px<4, DERIV>(x, y, z, Rv, Rl, dR, dRl, pure, emit); break;
+          case 5: shell_functions_px<5, DERIV>(x, y, z, Rv, Rl, dR, dRl, pure, emit); break;
+          case 6: shell_functions_px<6, DERIV>(x, y, z, Rv, Rl, dR, dRl, pure, emit); break;
           default: break;
         }
       }

@@ -56,12 +56,13 @@ __device__ __forceinline__ int rec_f0(int info) { return info >> 14; }
 
 // Evaluate one shell record at a point in FP32; Emit(f, value, value_lo, dx, dy, dz)
 // (value_lo: the angular part's and the coefficients' rounding, shell_functions_px).
-// Negligible shells (|R| below the radial threshold) emit zeros.  The radial factor is
-// summed as an FP32 pair (exp_tang2, products and sums with their rounding errors) and
-// *rlo receives R_lo / R_hi: all grid points of one radial shell of an atom share the
-// atom's functions' R, so its FP32 rounding would be the same error at all of them (and
-// at every atom of the element) instead of averaging out; value * (1 + *rlo) carries R
-// to ~2^-30.  The point-centre offset is a pair too: x = (p_hi - A_hi) + (p_lo - A_lo)
+// Negligible shells (|R| below the radial threshold) emit zeros.  The radial factor and
+// its derivative are summed as FP32 pairs (exp_tang2, products and sums with their
+// rounding errors) and *rlo receives R_lo / R_hi: all grid points of one radial shell of
+// an atom share the atom's functions' R, so its FP32 rounding would be the same error at
+// all of them (and at every atom of the element) instead of averaging out; value * (1 +
+// *rlo) carries R to ~2^-30, and the gradients take both pairs' low parts
+// (shell_functions_px).  The point-centre offset is a pair too: x = (p_hi - A_hi) + (p_lo - A_lo)
 // with the first difference's rounding kept (two-sum), so r^2 and the angular factors
 // see p - A to ~2^-48 instead of one FP32 rounding per coordinate.
 template <int DERIV, int MAXL, class Emit>
@@ -93,7 +94,7 @@ __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __
     r2 = s2;
   }
   const int np = rec_nprim(r.info);
-  float Rv = 0.f, Rl = 0.f, dR = 0.f;
+  float Rv = 0.f, Rl = 0.f, D = 0.f, Dl = 0.f;  // R and D = sum alpha c exp(-alpha r^2) = -R'/2
   for (int i = 0; i < np; ++i) {
     const float4 ac = __ldg(prim4 + r.prim0 + i);  // alpha = x + z, coef = y + w
     const float t = __fmul_rn(ac.x, r2);           // alpha r^2 = t + tl
@@ -110,7 +111,13 @@ __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __
       const float err = __fadd_rn(__fsub_rn(Rv, __fsub_rn(s, bp)), __fsub_rn(eh, bp));
       Rl = __fadd_rn(Rl, __fadd_rn(err, el));
       Rv = s;
-      if (DERIV >= 1) dR = fmaf(-2.f * ac.z, eh, fmaf(-2.f * ac.x, eh, dR));
+      if (DERIV >= 1) {  // D += alpha (eh + el), a pair like R
+        const float ph = __fmul_rn(ac.x, eh);
+        const float pl = fmaf(ac.x, el, fmaf(ac.z, eh, fmaf(ac.x, eh, -ph)));
+        const float sd = __fadd_rn(D, ph), bd = __fsub_rn(sd, D);
+        Dl = __fadd_rn(Dl, __fadd_rn(__fadd_rn(__fsub_rn(D, __fsub_rn(sd, bd)), __fsub_rn(ph, bd)), pl));
+        D = sd;
+      }
     }
   }
   const int l = rec_l(r.info);
@@ -120,7 +127,7 @@ __device__ __forceinline__ void shell_rec_at(const ShellRec& r, const float4* __
     return;
   }
   *rlo = Rv != 0.f ? __fdividef(Rl, Rv) : 0.f;  // a correction of ~2^-24 relative: a few ulp of it suffice
-  shell_functions_px_l<DERIV, MAXL>(l, d[0], d[1], d[2], Rv, dR, rec_pure(r.info), emit);
+  shell_functions_px_l<DERIV, MAXL>(l, d[0], d[1], d[2], Rv, Rl, -2.f * D, -2.f * Dl, rec_pure(r.info), emit);
 }
 
 __device__ __forceinline__ ShellRec load_rec(const ShellRec* p) {
