@@ -33,7 +33,7 @@ sys.path.insert(0, ROOT)
 METRIC = "XC builds/s & Mpts/s, (H2O)32 PBE, mixed vs FP64 GPU at 1e-7 Eh; p50/p99 latency"
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the whole-build mixed kernel
 # on the (H2O)32 workload, from one ncu capture of that kernel
-MIXED_DRAM_BYTES = {"build": 473.2e6 + 2845.7e6}
+MIXED_DRAM_BYTES = {"build": 476.3e6 + 2837.6e6}
 WORKLOADS = {0: "(H2O)4 def2-SVP LDA restricted, 50x194 Becke grid, 128-point blocks",
              1: "(H2O)32 def2-SVP PBE restricted, 75x302 Becke grid, 128-point blocks",
              2: "(H2O)64 def2-TZVP PBE unrestricted, 99x434 Becke grid, 128-point blocks"}

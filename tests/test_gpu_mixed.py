@@ -5,8 +5,9 @@ the oracle on the same inputs.
 
 Stated tolerances (water tetramer, 30 x 110 grid): density relative to max rho 1e-6,
 adder 1.5e-6 (random v and g), N_el 1e-8 relative; whole builds against the oracle
-E_xc 1e-7 Eh and max|dVxc| 1.5e-7 with def2-SVP (measured 2-6e-8 and 0.8-1.0e-7),
-3e-7 Eh and 4e-7 with def2-TZVP (measured 1.3-1.9e-7 and 2.6-2.8e-7)."""
+E_xc 1e-7 Eh and max|dVxc| 1e-7 with def2-SVP (measured 0.4-1.7e-8 and 0.6-0.9e-7),
+1e-7 Eh and 4e-7 with def2-TZVP (measured 3.4-5.2e-8 and 2.7-3.2e-7); on the benchmark grids
+1e-7 in both (test_mixed_vxc_benchmark_tolerance)."""
 import numpy as np
 import pytest
 
@@ -62,9 +63,9 @@ def test_mixed_adder_vs_fp64(ctx):
     assert np.abs(Fmx - F64).max() <= 1.5e-6 * max(1.0, np.abs(F64).max())
 
 
-# def2-SVP at the benchmark's 1e-7 (measured: dE_xc <= 4.7e-8, max|dV| <= 9.2e-8); the
-# def2-TZVP tetramer on this coarse grid reaches max|dV| 3.1e-7 (dE_xc <= 6e-8), so its bound is
-# looser (on the 99 x 434 grid the benchmark-tolerance test below holds TZVP to 1e-7)
+# def2-SVP at the benchmark's 1e-7 (measured: |dE_xc| <= 1.7e-8, max|dV| <= 9.2e-8); the
+# def2-TZVP tetramer on this coarse grid reaches max|dV| 3.2e-7 (|dE_xc| <= 5.2e-8), so its V
+# bound is looser (on the 99 x 434 grid the benchmark-tolerance test below holds TZVP to 1e-7)
 @pytest.mark.parametrize("func,unrestricted,basis,spherical,etol,vtol", [
     ("LDA", False, "DEF2-SVP", True, 1e-7, 1e-7), ("PBE", False, "DEF2-SVP", True, 1e-7, 1e-7),
     ("BLYP", False, "DEF2-SVP", True, 1e-7, 1e-7), ("PBE", True, "DEF2-SVP", True, 1e-7, 1e-7),
