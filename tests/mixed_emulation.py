@@ -4,12 +4,14 @@ Restates, operation by operation in numpy float32 (FMAs through float64, exact f
 products), what the mixed build kernel computes for rho and grad rho, so that its errors
 against FP64 can be attributed stage by stage without a GPU:
 
-  * basis values (serenity_gb300/csrc/xc_mixed.cu: shell_rec_at; basis_eval.cuh:
+  * basis values (serenity_gb300/csrc/xc_mixed_kernel.cuh: shell_rec_at; basis_eval.cuh:
     shell_functions_px): point and centre as FP32 high + remainder, the point-centre
-    offset as an FP32 pair (two-sum), r^2 and alpha r^2 as FP32 pairs, the radial sum as
-    a pair (the exponential taken exact: the kernel's pair exponential is accurate to
-    2e-11), the monomials, the coefficients and the solid-harmonic sums as FP32 pairs,
-    the value's low part fma(v, R_lo / R, v_low), the gradients in FP32;
+    offset as an FP32 pair (two-sum), r^2 and alpha r^2 as FP32 pairs, the radial sum and
+    its derivative as pairs (the exponential taken exact: the kernel's pair exponential is
+    accurate to 2e-11), the monomials, the coefficients and the solid-harmonic sums as
+    FP32 pairs, the value's low part fma(v, R_lo / R, v_low), the gradients as
+    R A_i + R' x_i S in FP32 with the low parts of R and R' (A_i the FP32 sum of the
+    coefficients times the monomials' derivatives, S the angular pair sum);
   * the plan's screening (xc_fp64.cu: screen_kernel) and 128-point blocks;
   * the fixed-point slices of A (density_slices: row scale from the point's largest |phi|,
     dithered last digit, point_dither / function_dither) and of P (split_p_kernel);
@@ -89,8 +91,9 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
     mode "kernel": the kernel's arithmetic, the offset and the whole angular part
     (powers, monomials, the solid-harmonic sums) carried as FP32 pairs (error-free
     products by FMA, two-sum); "fp32": the kernel's former arithmetic, offset and angular
-    part rounded to FP32 at every operation; "exact": the exact value split into FP32
-    high and low parts (gradients as in "kernel")."""
+    part rounded to FP32 at every operation (values and gradients); "exact": the exact
+    value split into FP32 high and low parts, the gradients in the kernel's form with the
+    exact angular sum."""
     ethr = -math.log(thr)
     d = xyz - A[None, :]
     r2e = (d * d).sum(1)
@@ -146,6 +149,8 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
     Rv = np.zeros_like(x)
     Rl = np.zeros_like(x)
     dR = np.zeros_like(x)
+    Dh = np.zeros_like(x)  # D = sum alpha c exp(-alpha r^2) = -R'/2 as a pair (kernel mode)
+    Dl = np.zeros_like(x)
     for a, c in zip(alpha, coef):
         a_h, c_h = f32(a), f32(c)
         a_l, c_l = f32(a - float(a_h)), f32(c - float(c_h))
@@ -164,6 +169,11 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
         Rl = np.where(on, Rl + (err + el), Rl)
         Rv = np.where(on, s, Rv)
         dR = np.where(on, fma(f32(-2) * a_l * one, eh, fma(f32(-2) * a_h * one, eh, dR)), dR)
+        ph = a_h * eh
+        pl = fma(a_h * one, el, fma(a_l * one, eh, fma(a_h * one, eh, -ph)))
+        sd, ed = two_sum(Dh, ph)
+        Dl = np.where(on, Dl + (ed + pl), Dl)
+        Dh = np.where(on, sd, Dh)
     zero = ~(np.abs(Rv) >= f32(thr))
     rlo = np.where(Rv != 0, Rl / np.where(Rv != 0, Rv, f32(1)), f32(0)).astype(f32)
     px, py, pz = [np.ones_like(x)], [np.ones_like(x)], [np.ones_like(x)]
@@ -175,6 +185,7 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
     sv = [np.zeros_like(x) for _ in range(NS)]
     svl = [np.zeros_like(x) for _ in range(NS)]
     sg = [[np.zeros_like(x) for _ in range(NS)] for _ in range(3)]
+    sa = [[np.zeros_like(x) for _ in range(NS)] for _ in range(3)]  # sum t d_i(monomial)
     for k, (a, b, c) in enumerate(ks):
         m_ = (px[a] * py[b]) * pz[c]
         v = m_ * Rv
@@ -193,6 +204,7 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
                 svl[m] = fma(tl * np.ones_like(v), v, svl[m])
             for ax in range(3):
                 sg[ax][m] = fma(t * np.ones_like(v), g[ax], sg[ax][m])
+                sa[ax][m] = fma(t * np.ones_like(v), (dmx, dmy, dmz)[ax], sa[ax][m])
     if mode == "kernel":
         def pmul(ah_, al_, bh_, bl_):
             h = ah_ * bh_
@@ -204,21 +216,39 @@ def shell_values(xyz, A, l, alpha, coef, mode="kernel", thr=1e-9):
             qx.append(list(pmul(qx[-1][0], qx[-1][1], x, XL[0])))
             qy.append(list(pmul(qy[-1][0], qy[-1][1], y, XL[1])))
             qz.append(list(pmul(qz[-1][0], qz[-1][1], z, XL[2])))
+        # the angular sum S as a pair, then the value S R (pair times FP32)
         sh_ = [np.zeros_like(x) for _ in range(NS)]
         sl_ = [np.zeros_like(x) for _ in range(NS)]
         for k, (a, b, c) in enumerate(ks):
             mh, ml = pmul(qx[a][0], qx[a][1], qy[b][0], qy[b][1])
             mh, ml = pmul(mh, ml, qz[c][0], qz[c][1])
-            vh, vl_ = pmul(mh, ml, Rv, np.zeros_like(Rv))
             for m in range(NS):
                 T = TS[l][m, k]
                 if T == 0.0:
                     continue
                 t, tl = f32(T), f32(T - float(f32(T)))
-                ph, pl = pmul(t * np.ones_like(vh), tl * np.ones_like(vh), vh, vl_)
+                ph, pl = pmul(t * np.ones_like(mh), tl * np.ones_like(mh), mh, ml)
                 sh_[m], e = two_sum(sh_[m], ph)
                 sl_[m] = sl_[m] + (e + pl)
-        sv, svl = sh_, sl_
+        sv, svl = [], []
+        for m in range(NS):
+            vh, vl_ = pmul(sh_[m], sl_[m], Rv, np.zeros_like(Rv))
+            sv.append(vh)
+            svl.append(vl_)
+            # gradient R A_i + R' x_i S, R and R' with their low parts
+            u = (f32(-2) * Dh) * sh_[m]
+            ul = (f32(-2) * Dl) * sh_[m]
+            for ax in range(3):
+                A_ = sa[ax][m]
+                sg[ax][m] = fma(Rv, A_, fma(u, X[ax], fma(Rl, A_, ul * X[ax])))
+    if mode == "exact":
+        for m in range(NS):
+            Sh = fl(S64[:, m])
+            u = (f32(-2) * Dh) * Sh
+            ul = (f32(-2) * Dl) * Sh
+            for ax in range(3):
+                A_ = sa[ax][m]
+                sg[ax][m] = fma(Rv, A_, fma(u, X[ax], fma(Rl, A_, ul * X[ax])))
     V = np.zeros((len(xyz), NS), f32)
     VL = np.zeros_like(V)
     G32 = np.zeros((3, len(xyz), NS), f32)

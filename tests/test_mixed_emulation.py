@@ -2,7 +2,7 @@
 part equals the oracle's basis values and gradients; the kernel's pair arithmetic carries
 the basis values (high + low part) to about 2^-44 of the shell's largest value, the
 former per-operation FP32 form to 1e-10..1e-6 (the error the pairs remove), the exact
-mode to FP64; and on one water the emulated mixed density integrates to the FP64
+mode to FP64; the kernel's gradients carry no per-radial-shell bias; and on one water the emulated mixed density integrates to the FP64
 electron count within the slices' noise."""
 import numpy as np
 import pytest
@@ -58,6 +58,36 @@ def test_basis_value_errors_by_mode(water):
     assert worst["exact"] < 1e-14
     assert worst["kernel"] < 1e-12  # the radial factor's pair and the pair angular part
     assert 1e-10 < worst["fp32"] < 1e-6  # FP32 rounding of the offsets and angular parts
+
+
+def test_basis_gradient_bias_by_mode(water):
+    """On a radial shell of a function's own atom R and R' are one number each: the former
+    FP32 gradients carried their rounding as one relative error at every point of the
+    shell (a bias, measured as the least-squares relative error over the shell's points);
+    the kernel's form R A_i + R' x_i S with the pairs' low parts leaves errors that differ
+    from point to point (measured: median bias 2.7e-8 against 2.7e-9)."""
+    w, _, _ = water
+    sh, b, off, cen = _shells(w)
+    rng = np.random.default_rng(1)
+    u = rng.normal(size=(302, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    bias = {"fp32": [], "kernel": []}
+    for mode in bias:
+        for r in [0.3, 0.7, 1.2, 2.0]:
+            for s in range(sh.nshell):
+                if np.linalg.norm(cen[s] - cen[0]) > 1e-9:  # the oxygen's shells
+                    continue
+                _, G64, _, _, G32 = me.shell_values(cen[s][None, :] + r * u, cen[s], int(sh.l[s]),
+                                                    sh.alpha[off[s]:off[s + 1]], b.shell_coefs(s), mode)
+                for m in range(G64.shape[2]):
+                    g = G64[:, :, m].ravel()
+                    if not np.abs(g).max() > 0:  # below the radial threshold at this distance
+                        continue
+                    e = G32[:, :, m].astype(np.float64).ravel() - g
+                    bias[mode].append(abs((e * g).sum() / (g * g).sum()))
+    fp32, kern = np.median(bias["fp32"]), np.median(bias["kernel"])
+    assert fp32 > 1e-8
+    assert kern < 0.25 * fp32 and kern < 6e-9, (kern, fp32)
 
 
 def test_emulated_mixed_density_of_one_water(water):
