@@ -119,6 +119,8 @@ class Server:
         return S
 
     def _evict(self):
+        """Drop least recently used residents that have no request in flight until the
+        budget holds; a geometry's grid goes with the last resident that shares it."""
         while self.ctx.bytes_in_use + self.reserved > self.budget and self.cache:
             key, r = next(iter(self.cache.items()))
             if r.busy:
@@ -127,6 +129,8 @@ class Server:
                     return
                 continue
             self.cache.pop(key)
+            if not any(k[0] == key[0] for k in self.cache):
+                self.grids.pop(key[0], None)
 
     # -- batches --------------------------------------------------------------------------
     def _arrive(self, rq):

@@ -1,7 +1,8 @@
 """Host logic of the serving loop (serenity_gb300/serve.py) on the CPU: admission of waiting
 requests into batches under the HBM budget, the batch cap and the work cap, continuous
 batching over two streams, LRU eviction that never drops a geometry with requests in
-flight (and whose evicted geometries still serve later requests), rejection beyond a
+flight (and whose evicted geometries still serve later requests; a grid goes with the last
+resident that uses it), rejection beyond a
 latency budget, and the bookkeeping of reserved bytes and latencies.  The GPU pieces (streams, events, the library's
 batched build, the request's density matrix) are replaced by fakes that record what the loop
 asks of them; the builds themselves are covered by tests/test_gpu_batch.py."""
@@ -172,6 +173,21 @@ def test_eviction_spares_geometries_with_requests_in_flight(make_server):
     a.release(0)
     srv._evict()
     assert not srv.cache
+
+
+def test_eviction_drops_a_grid_with_its_last_resident(make_server):
+    srv, ctx = make_server(budget=10 ** 9)
+    w = workload()
+    srv.resident((0, "SVP"), w)
+    srv.resident((0, "TZVP"), w)  # the same geometry in a second basis shares the grid
+    srv.resident((1, "SVP"), w).plan()  # in flight: stays, and so does its grid
+    assert srv.cache[(0, "SVP")].grid is srv.cache[(0, "TZVP")].grid
+    srv.budget = 0
+    srv._evict()
+    assert list(srv.cache) == [(1, "SVP")]
+    assert 0 not in srv.grids and 1 in srv.grids
+    r = srv.resident((0, "SVP"), w)  # a later request rebuilds the geometry's grid
+    assert 0 in srv.grids and r.grid is srv.grids[0]
 
 
 def test_work_bytes_grow_with_points_functions_and_spins():
