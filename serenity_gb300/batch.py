@@ -113,7 +113,8 @@ def autotune_block(ctx, workloads, precision=xcgpu.PREC_MIXED, candidates=(64, 9
     key = "%s/%s/%d/%d" % (workloads[0].basis_name, workloads[0].func, precision,
                            int(math.log2(max(1, sum(len(w.Z) for w in workloads)))))
     try:
-        cache = json.load(open(cache_path))
+        with open(cache_path) as f:
+            cache = json.load(f)
     except (OSError, ValueError):
         cache = {}
     if key in cache:
@@ -127,9 +128,12 @@ def autotune_block(ctx, workloads, precision=xcgpu.PREC_MIXED, candidates=(64, 9
         b.close()
     best = min(timings, key=timings.get)
     cache[key] = best
-    try:
+    try:  # written whole and renamed, so a concurrent reader never sees a partial file
         os.makedirs(os.path.dirname(cache_path), exist_ok=True)
-        json.dump(cache, open(cache_path, "w"))
+        tmp = "%s.%d.tmp" % (cache_path, os.getpid())
+        with open(tmp, "w") as f:
+            json.dump(cache, f)
+        os.replace(tmp, cache_path)
     except OSError:
         pass
     return best, timings
