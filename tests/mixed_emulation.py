@@ -294,6 +294,25 @@ def slice_digits(vh, vl, u):
     return s0.astype(f64), s1.astype(f64) / 512, s2.astype(f64) / 512
 
 
+def adder_slices(vh, vl):
+    """fixed_scale<7> and fixed_slices2<7, 8> (the adder's operands, a function's values over
+    a block's points): a power-of-two scale with max|x| / scale < 128, then three 8-bit
+    slices, the last rounded to nearest.  Returns (f0, f1, f2, scale): x ~ (f0 + f1 + f2) scale,
+    f0 an integer, f1 a multiple of 2^-8, f2 of 2^-16."""
+    m = float(np.abs(vh).max())
+    if not m > 0:
+        z = np.zeros_like(vh)
+        return z, z, z, 0.0
+    e = np.frexp(m)[1]
+    inv = f32(np.ldexp(1.0, 7 - e))
+    x, xl = (vh * inv).astype(f32), (vl * inv).astype(f32)
+    f0 = np.rint(x)
+    r1 = ((x - f0) + xl) * f32(256)
+    s1 = np.rint(r1)
+    f2 = np.rint((r1 - s1) * f32(256)) * f32(1.0 / 65536)
+    return f0, s1 * f32(1.0 / 256), f2.astype(f32), float(np.ldexp(1.0, e - 7))
+
+
 def split_p(P, exact=False):
     """split_p_kernel: per column a power-of-two scale and three stored slices (exact: the
     scaled column itself as the leading slice, for bounding what the slicing costs)."""

@@ -2,7 +2,8 @@
 part equals the oracle's basis values and gradients; the kernel's pair arithmetic carries
 the basis values (high + low part) to about 2^-44 of the shell's largest value, the
 former per-operation FP32 form to 1e-10..1e-6 (the error the pairs remove), the exact
-mode to FP64; the kernel's gradients carry no per-radial-shell bias; and on one water the emulated mixed density integrates to the FP64
+mode to FP64; the kernel's gradients carry no per-radial-shell bias; the adder's
+operand slices are FP16-exact with leading products that sum exactly; and on one water the emulated mixed density integrates to the FP64
 electron count within the slices' noise."""
 import numpy as np
 import pytest
@@ -99,3 +100,34 @@ def test_emulated_mixed_density_of_one_water(water):
     # the exact basis values leave only the slices' and the epilogue's noise
     dNx, dEx, _ = me.density_errors(w.shells, pts, wts, P, "PBE", "exact")
     assert abs(dNx) < 2e-7 and abs(dEx) < 2e-7
+
+
+def test_adder_slices_are_fp16_exact_and_leading_products_sum_exactly():
+    """The adder's operands: every slice is an FP16 number, the three reconstruct the value
+    and its low part to about half a unit of 2^-16 of the row's scale, and the leading products
+    (integers below 2^14) sum over a block's 128 points below 2^24, so their FP32 sum is
+    exact in any order."""
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        mag = np.exp(rng.uniform(-12.0, 3.0)) * np.exp(rng.normal(0.0, 2.0, 128))
+        v = mag * rng.choice([-1.0, 1.0], 128)
+        vh = v.astype(np.float32)
+        vl = (v - vh.astype(np.float64)).astype(np.float32)
+        f0, f1, f2, sc = me.adder_slices(vh, vl)
+        for sl in (f0, f1, f2):
+            assert np.array_equal(sl.astype(np.float16).astype(np.float32), sl)
+        assert np.abs(f0).max() <= 128 and np.abs(f1).max() <= 0.5 and np.abs(f2).max() <= 2.0 ** -9
+        x = (vh.astype(np.float64) + vl.astype(np.float64)) / sc
+        rec = f0.astype(np.float64) + f1.astype(np.float64) + f2.astype(np.float64)
+        # half a unit of 2^-16 from the last slice's rounding, plus the FP32 rounding of
+        # the low part's addition to the remainder
+        assert np.abs(rec - x).max() <= 2.0 ** -17 + 2.0 ** -23
+        g0 = me.adder_slices(vh[::-1].copy(), vl[::-1].copy())[0]
+        prods = f0.astype(np.float64) * g0.astype(np.float64)
+        exact = prods.sum()
+        assert np.abs(prods).sum() < 2.0 ** 24
+        acc = np.float32(0)
+        for q in rng.permutation(128):
+            acc = np.float32(acc + np.float32(prods[q]))
+        assert float(acc) == exact
+
