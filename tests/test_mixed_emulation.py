@@ -131,3 +131,36 @@ def test_adder_slices_are_fp16_exact_and_leading_products_sum_exactly():
             acc = np.float32(acc + np.float32(prods[q]))
         assert float(acc) == exact
 
+
+
+def test_density_slice_products_sum_exactly_in_the_first_three_accumulators():
+    """The density's operands: a point's basis values (row scale below 2^8, slices of 9 bits,
+    the last dithered) against P's columns (the same digits).  Over a 128-function window
+    the accumulators s0t0, s0t1 + s1t0 and s1t1, each in its unit, sum absolute values of at
+    most 2^24, so their FP32 sums are exact in any order; the fourth (s0t2 + s2t0 + s1t2 +
+    s2t1, 2^-18 of the first) is not bounded so and is summed to FP32."""
+    rng = np.random.default_rng(11)
+    worst = [0.0, 0.0, 0.0]
+    for _ in range(40):
+        v = np.exp(rng.normal(0.0, 2.5, 128)) * rng.choice([-1.0, 1.0], 128)
+        vh = v.astype(np.float32)
+        vl = (v - vh.astype(np.float64)).astype(np.float32)
+        m = np.abs(vh).max()
+        _, inva = me.row_scale(np.array([m], dtype=np.float32))
+        h0, h1, h2 = me.slice_digits(vh * inva[0], vl * inva[0], rng.uniform(size=128).astype(np.float32))
+        Pm = rng.normal(size=(128, 128)) * np.exp(rng.normal(0.0, 2.0, (128, 1)))
+        T0, T1, T2, _ = me.split_p(Pm)  # (square, as P is; four of its columns are used)
+        for j in range(4):
+            # each accumulator's terms in its unit (1, 2^-9, 2^-18) and the sum of the
+            # absolute values of the products that form them
+            terms = [h0 * T0[:, j], (h0 * T1[:, j] + h1 * T0[:, j]) * 512.0, h1 * T1[:, j] * 512.0 ** 2]
+            mags = [np.abs(terms[0]).sum(), (np.abs(h0 * T1[:, j]) + np.abs(h1 * T0[:, j])).sum() * 512.0,
+                    np.abs(terms[2]).sum()]
+            for k, t in enumerate(terms):
+                assert np.array_equal(t, np.rint(t))  # integers in the accumulator's unit
+                worst[k] = max(worst[k], mags[k])
+                acc = np.float32(0)
+                for q in rng.permutation(128):
+                    acc = np.float32(acc + np.float32(t[q]))
+                assert float(acc) == t.sum()
+    assert max(worst) <= 2.0 ** 24
