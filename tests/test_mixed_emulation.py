@@ -2,9 +2,10 @@
 part equals the oracle's basis values and gradients; the kernel's pair arithmetic carries
 the basis values (high + low part) to about 2^-44 of the shell's largest value, the
 former per-operation FP32 form to 1e-10..1e-6 (the error the pairs remove), the exact
-mode to FP64; the kernel's gradients carry no per-radial-shell bias; the adder's
-operand slices are FP16-exact with leading products that sum exactly; and on one water the emulated mixed density integrates to the FP64
-electron count within the slices' noise."""
+mode to FP64; the kernel's gradients carry no per-radial-shell bias; the density's
+first three slice accumulators and the adder's leading products sum exactly; and on one
+water the emulated mixed density integrates to the FP64 electron count within the
+slices' noise."""
 import numpy as np
 import pytest
 
